@@ -1,0 +1,151 @@
+/*
+ * vajax_gb300 — C ABI of the GB300 transient Newton path.
+ *
+ * Every entry point returns an int status (0 = success, see VGB_* below) and
+ * never aborts; vgb_last_error() returns the message of the last failure on a
+ * handle.  Array arguments are plain pointers with explicit sizes.  Pointers
+ * documented as "device" are CUDA device pointers; all others are host
+ * memory.  A stream argument of NULL means the handle's own stream.
+ *
+ * Node numbering follows the reference: circuit node 0 is ground; the
+ * solution vector X = [V_0 .. V_{n_nodes-1}, I_branch_0 .. I_branch_{m-1}]
+ * keeps the ground entry (always 0) at index 0 (vajax/analysis/mna_builder.py:
+ * 526-533).  The augmented system has n_aug = n_nodes - 1 + m unknowns.
+ */
+#ifndef VAJAX_GB300_H
+#define VAJAX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VGB_OK 0
+#define VGB_ERR_INVALID 1
+#define VGB_ERR_CUDA 2
+#define VGB_ERR_NUMERIC 3
+#define VGB_ERR_TIMEOUT 4
+#define VGB_ERR_STATE 5
+
+typedef void* vgb_stream_t; /* cudaStream_t */
+
+/* Library version and the compiled-model registry ------------------------ */
+
+int vgb_version(void);
+/* Number of compiled device models linked into the library. */
+int vgb_num_models(void);
+/* Shape of model `id`: nodes, Jacobian entries, user parameters; name copied
+ * into `name` (NUL-terminated, at most name_cap bytes).  jrow/jcol (may be
+ * NULL) receive the model-local node indices of each Jacobian entry.
+ * Replaces the per-model metadata the reference reads from
+ * OpenVAFToJAX.get_dae_metadata() (openvaf_jax/__init__.py:253-280). */
+int vgb_model_info(int id, char* name, int name_cap, int* nn, int* nj, int* np, int* jrow, int* jcol);
+
+/* Circuit construction ------------------------------------------------------ */
+
+/* Create a circuit with n_nodes nodes (including ground) and the given
+ * voltage / current sources (terminal node indices, 0 = ground).  Mirrors
+ * the source description the reference passes to make_mna_build_system_fn
+ * (vajax/analysis/mna_builder.py:258-330). */
+int vgb_circuit_create(int n_nodes, int n_vsrc, const int* vsrc_p, const int* vsrc_n,
+                       int n_isrc, const int* isrc_p, const int* isrc_n, void** out_handle);
+int vgb_circuit_destroy(void* h);
+const char* vgb_last_error(void* h);
+
+/* Add a group of instances of compiled model `model_id`.
+ * node_map: [nn][n_dev] circuit node of each model node (struct of arrays).
+ * shared_params: [np] values of parameters common to the group.
+ * n_varying / varying_idx / varying_values: parameters that vary per instance,
+ *   varying_values laid out [n_varying][n_dev].
+ * temperatures: [n_dev] kelvin per instance, or NULL to use temp_shared.
+ * This is the device-parameter split of prepare_static_inputs
+ * (vajax/analysis/openvaf_models.py:668-1056: shared vs varying columns). */
+int vgb_circuit_add_group(void* h, int model_id, int n_dev, const int* node_map,
+                          const double* shared_params, int n_varying, const int* varying_idx,
+                          const double* varying_values, const double* temperatures, double temp_shared);
+
+/* Source waveforms.  kind: 0 DC [v], 1 PULSE [val0,val1,rise,fall,width,period,delay],
+ * 2 PWL [period, t0, v0, t1, v1, ...], 3 SINE [dc, ampl, freq, phase];
+ * params of source k start at offsets[k] and hold counts[k] doubles
+ * (vajax/analysis/sources.py:31-294). is_current selects the isource table. */
+int vgb_circuit_set_sources(void* h, int is_current, int n, const int* kinds, const int* offsets,
+                            const int* counts, const double* params);
+
+/* Circuit node indices of internal device nodes, skipped by the residual
+ * convergence test (solver_factories.py:37-100, residual_conv_mask). */
+int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx);
+
+/* Build the CSR pattern, stamp maps, gather lists and the sparse symbolic
+ * factorisation; allocate device state.  precision: 0 = FP64 LU,
+ * 1 = FP32 LU with FP64-residual iterative refinement (refine_sweeps <= 3).
+ * Replaces FullMNAStrategy._ensure_full_mna_solver
+ * (vajax/analysis/transient/full_mna.py:344-690). */
+int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps);
+
+/* Pattern and maps (bit-exact contract with the reference) ----------------- */
+
+/* Sizes: n_aug, CSR nnz, LU nnz, LU flops (2 * multiply-adds). */
+int vgb_pattern_info(void* h, int* n_aug, int* nnz, int64_t* nnz_lu, int64_t* lu_flops);
+/* CSR of the augmented Jacobian: indptr[n_aug+1], indices[nnz]
+ * (full_mna.py:461-513). */
+int vgb_pattern_csr(void* h, int* indptr, int* indices);
+/* CSR data position of each (instance, Jacobian entry) of group g,
+ * [n_dev][nj], -1 where a terminal is ground (mna_builder.py:126-160). */
+int vgb_stamp_positions(void* h, int group, int* out);
+/* diag[n_unknowns]; vsrc[4][n_vsrc] = b_p, b_n, bt_p, bt_n (mna_builder.py:163-255). */
+int vgb_special_positions(void* h, int* diag, int* vsrc);
+
+/* One system build at X (device, n_nodes+n_vsrc): CSR values, residual f
+ * (n_aug), charges Q, max residual contribution and f_resist (n_nodes-1).
+ * coeffs = {c0, c1, d1, c2, gshunt}.  Q_prev/dQdt_prev/Q_prev2 may be NULL
+ * (zeros).  Equivalent of build_system_mna in CSR-direct mode
+ * (mna_builder.py:759-1076).  All array arguments are device pointers. */
+int vgb_build_system(void* h, const double* X, const double* vsrc_vals, const double* isrc_vals,
+                     const double* Q_prev, const double* dQdt_prev, const double* Q_prev2,
+                     const double* coeffs, double* csr_vals, double* f, double* Q, double* maxc,
+                     double* fres, vgb_stream_t stream);
+
+/* Raw model outputs of group g at X (device): out[(2 nn + 2 nj)][n_dev] =
+ * residual_resist, residual_react, jac_resist, jac_react (device).  The
+ * per-instance eval contract of the generated eval_fn
+ * (openvaf_jax/codegen/function_builder.py:971-981). */
+int vgb_eval_group(void* h, int group, const double* X, double* out, vgb_stream_t stream);
+
+/* Linear solve J x = rhs with the circuit's sparse LU (device pointers).
+ * Replaces the linear_solve_fn plug-in (solver_factories.py:140-202,
+ * 895-922). */
+int vgb_linear_solve(void* h, const double* csr_vals, const double* rhs, double* x, vgb_stream_t stream);
+
+/* Newton solve from X (device, updated in place).  opts = {c0, c1, d1, c2,
+ * gshunt, reltol, abstol, vntol, damping, max_step}; res_tol_floor (device,
+ * n_unknowns) may be NULL for abstol.  Outputs (host): iterations,
+ * converged, max_f.  Q_out/dQdt_out/I_vsrc/maxc_out are device pointers
+ * (may be NULL) filled from the post-convergence rebuild, as nr_solve does
+ * (solver_factories.py:604-725). */
+int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc_vals,
+                 const double* Q_prev, const double* dQdt_prev, const double* Q_prev2,
+                 const double* res_tol_floor, const double* opts, int max_iter,
+                 int* iterations, int* converged, double* max_f,
+                 double* Q_out, double* dQdt_out, double* I_vsrc, double* maxc_out, vgb_stream_t stream);
+
+/* Transient analysis, device resident.  All arrays are host memory.
+ * cfg (doubles): {t_stop, dt, max_dt, min_dt, reltol, abstol, vntol, lte_ratio,
+ *   redo_factor, grow_factor, tran_ft, nr_damping, gshunt_init, gshunt_target,
+ *   gshunt_steps, warmup_steps, max_consecutive_rejects, fixed_step, method,
+ *   n_external, max_steps, tran_itl}
+ *   method: 0 BE, 1 trap, 2 gear2.  fixed_step != 0 selects the fixed-step
+ *   loop (full_mna.py:1198-1441), else the adaptive loop (full_mna.py:1792-2196).
+ * X0 [n_nodes+n_vsrc], Q0 [n_nodes-1], I0 [n_vsrc], maxc0 [n_nodes-1] (NULL = 0):
+ *   initial state (DC operating point or initial conditions).
+ * Outputs: times[max_steps], V_out[max_steps][n_external], I_out[max_steps][max(n_vsrc,1)],
+ * stats[8] = {n_steps, rejected, total_nr_iters, min_dt_used, max_dt_used,
+ *             device_ms, nr_failures, kernel_launches}. */
+int vgb_transient(void* h, const double* cfg, const double* X0, const double* Q0, const double* I0,
+                  const double* maxc0, double* times, double* V_out, double* I_out, double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VAJAX_GB300_H */

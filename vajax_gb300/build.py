@@ -1,0 +1,104 @@
+"""Build the CUDA extension ``libvajax_gb300.so`` for sm_103a.
+
+Steps: emit the CUDA source of every bundled device model from its committed
+MIR fixture (``devices/*.json``), compile each translation unit with nvcc in
+parallel, and link one shared library next to this file.  The library is a
+plain C ABI (``include/vajax_gb300.h``); Python reaches it through ctypes.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libvajax_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["vgb_api.cu", "vgb_transient.cu", "vgb_kernels.cu", "vgb_host.cpp"]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build vajax_gb300")
+    return exe
+
+
+def _flags():
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(CSRC),
+                   "-I", str(ROOT / "include"), "--expt-relaxed-constexpr"]
+
+
+def _compile(src: Path, obj: Path, extra=()):
+    cmd = [nvcc(), *(_flags()), *extra, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [nvcc(), "-x", "cu", *(_flags()), *extra, "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stderr[-4000:]}")
+    return obj
+
+
+def generate_models() -> Path:
+    sys.path.insert(0, str(ROOT))
+    from vajax_gb300.codegen.cuda import write_generated
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "vgb_models_gen.cu"
+    tmp = BUILD / "vgb_models_gen.cu.tmp"
+    write_generated(PKG / "devices", tmp)
+    if not out.exists() or out.read_bytes() != tmp.read_bytes():
+        tmp.replace(out)
+    else:
+        tmp.unlink()
+    return out
+
+
+def _digest(paths) -> str:
+    h = hashlib.sha256()
+    for p in paths:
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    h.update(" ".join(_flags()).encode())
+    return h.hexdigest()
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    gen = generate_models()
+    srcs = [CSRC / s for s in SOURCES] + [gen]
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "vajax_gb300.h"]
+    digest = _digest(srcs + headers)
+    stamp = BUILD / "stamp"
+    if not force and LIB.exists() and stamp.exists() and stamp.read_text() == digest:
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    objs = []
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        futs = []
+        for s in srcs:
+            obj = BUILD / (s.stem + ".o")
+            extra = ["-Xptxas", "-v"] if verbose else []
+            futs.append(ex.submit(_compile, s, obj, extra))
+        for f in futs:
+            objs.append(f.result())
+    tmp_lib = BUILD / "libvajax_gb300.so.tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp_lib), *map(str, objs)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
+    tmp_lib.replace(LIB)
+    stamp.write_text(digest)
+    return LIB
+
+
+if __name__ == "__main__":
+    import time
+    t = time.time()
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv), f"{time.time() - t:.1f}s")

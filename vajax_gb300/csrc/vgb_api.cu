@@ -1,0 +1,499 @@
+// C ABI of the vajax_gb300 transient Newton path (see include/vajax_gb300.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "vgb_core.h"
+
+namespace vgb {
+
+Circuit::~Circuit() {
+    if (h_status) cudaFreeHost(h_status);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+static thread_local std::string g_last_error;
+
+template <class F>
+static int guarded(Circuit* c, F&& fn) {
+    try {
+        fn();
+        return VGB_OK;
+    } catch (const Error& e) {
+        if (c) c->last_error = e.what();
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        if (c) c->last_error = e.what();
+        g_last_error = e.what();
+        return VGB_ERR_INVALID;
+    }
+}
+
+static Circuit* as_circuit(void* h) {
+    if (!h) throw Error(VGB_ERR_INVALID, "null handle");
+    return static_cast<Circuit*>(h);
+}
+
+static cudaStream_t pick(Circuit* c, vgb_stream_t s) { return s ? (cudaStream_t)s : c->stream; }
+
+static void require_final(Circuit* c) {
+    if (!c->finalized) throw Error(VGB_ERR_STATE, "circuit is not finalized");
+}
+
+// ---------------------------------------------------------------------------
+// Core steps
+// ---------------------------------------------------------------------------
+
+static double bits_to_double(unsigned long long b) {
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+// Newton loop (solver_factories.py:526-725, while_loop mode).
+NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
+                        const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
+                        const NROpts& o, int max_iter, cudaStream_t s) {
+    NRResult r;
+    NRUpdateArgs u{};
+    u.n_unk = c.n_unk;
+    u.n_aug = c.n_aug;
+    u.delta = c.d_delta.p;
+    u.X = X;
+    u.reltol = o.reltol;
+    u.vntol = o.vntol;
+    u.abstol = o.abstol;
+    u.damping = o.damping;
+    u.max_step = o.max_step;
+    u.st = c.d_status.p;
+    for (int it = 0; it < max_iter; ++it) {
+        launch_status_reset(c.d_status.p, s);
+        build_system(c, X, vs, is, Qp, dQp, Qp2, k, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p,
+                     c.d_maxc.p, c.d_fres.p, s);
+        launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
+        linear_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, s);
+        launch_nr_reduce(u, s);
+        launch_nr_apply(u, s);
+        VGB_CUDA(cudaMemcpyAsync(c.h_status, c.d_status.p, sizeof(NRStatus), cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        const NRStatus st = *c.h_status;
+        r.iterations = it + 1;
+        r.max_f = bits_to_double(st.max_f);
+        r.dev_err |= st.dev_err;
+        if (st.dev_err & DEV_ERR_TIMEOUT) throw Error(VGB_ERR_TIMEOUT, "sparse LU dependency wait timed out");
+        const bool conv = st.res_ok && (it == 0 || st.delta_ok);
+        if (conv) {
+            r.converged = true;
+            break;
+        }
+    }
+    return r;
+}
+
+} // namespace vgb
+
+using namespace vgb;
+
+extern "C" {
+
+int vgb_version(void) { return 100; }
+
+int vgb_num_models(void) {
+    int n = 0;
+    model_table(&n);
+    return n;
+}
+
+int vgb_model_info(int id, char* name, int name_cap, int* nn, int* nj, int* np, int* jrow, int* jcol) {
+    return guarded(nullptr, [&] {
+        int n = 0;
+        const ModelEntry* t = model_table(&n);
+        VGB_REQUIRE(id >= 0 && id < n, "model id out of range");
+        const ModelEntry& m = t[id];
+        if (name && name_cap > 0) {
+            std::strncpy(name, m.name, name_cap - 1);
+            name[name_cap - 1] = 0;
+        }
+        if (nn) *nn = m.nn;
+        if (nj) *nj = m.nj;
+        if (np) *np = m.np;
+        for (int k = 0; k < m.nj; ++k) {
+            if (jrow) jrow[k] = m.jrow[k];
+            if (jcol) jcol[k] = m.jcol[k];
+        }
+    });
+}
+
+int vgb_circuit_create(int n_nodes, int n_vsrc, const int* vsrc_p, const int* vsrc_n, int n_isrc,
+                       const int* isrc_p, const int* isrc_n, void** out_handle) {
+    return guarded(nullptr, [&] {
+        VGB_REQUIRE(out_handle, "out_handle is null");
+        VGB_REQUIRE(n_nodes >= 1 && n_vsrc >= 0 && n_isrc >= 0, "invalid sizes");
+        auto* c = new Circuit();
+        c->n_nodes = n_nodes;
+        c->n_unk = n_nodes - 1;
+        c->n_vsrc = n_vsrc;
+        c->n_isrc = n_isrc;
+        c->n_aug = c->n_unk + n_vsrc;
+        for (int k = 0; k < n_vsrc; ++k) {
+            VGB_REQUIRE(vsrc_p[k] >= 0 && vsrc_p[k] < n_nodes && vsrc_n[k] >= 0 && vsrc_n[k] < n_nodes,
+                        "vsource terminal out of range");
+            c->vsrc_p.push_back(vsrc_p[k]);
+            c->vsrc_n.push_back(vsrc_n[k]);
+        }
+        for (int k = 0; k < n_isrc; ++k) {
+            VGB_REQUIRE(isrc_p[k] >= 0 && isrc_p[k] < n_nodes && isrc_n[k] >= 0 && isrc_n[k] < n_nodes,
+                        "isource terminal out of range");
+            c->isrc_p.push_back(isrc_p[k]);
+            c->isrc_n.push_back(isrc_n[k]);
+        }
+        *out_handle = c;
+    });
+}
+
+int vgb_circuit_destroy(void* h) {
+    return guarded(nullptr, [&] { delete as_circuit(h); });
+}
+
+const char* vgb_last_error(void* h) {
+    if (!h) return g_last_error.c_str();
+    return static_cast<Circuit*>(h)->last_error.c_str();
+}
+
+int vgb_circuit_add_group(void* h, int model_id, int n_dev, const int* node_map, const double* shared_params,
+                          int n_varying, const int* varying_idx, const double* varying_values,
+                          const double* temperatures, double temp_shared) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(!c->finalized, "circuit already finalized");
+        int n = 0;
+        const ModelEntry* t = model_table(&n);
+        VGB_REQUIRE(model_id >= 0 && model_id < n, "model id out of range");
+        VGB_REQUIRE(n_dev >= 0, "negative instance count");
+        Group g;
+        g.model = model_id;
+        g.me = &t[model_id];
+        g.n_dev = n_dev;
+        g.nn = g.me->nn;
+        g.nj = g.me->nj;
+        g.np = g.me->np;
+        g.node_map.assign(node_map, node_map + (size_t)g.nn * n_dev);
+        for (int v : g.node_map) VGB_REQUIRE(v >= 0 && v < c->n_nodes, "node map entry out of range");
+        g.shared.assign(shared_params, shared_params + g.np);
+        g.vidx.assign(g.np, -1);
+        for (int k = 0; k < n_varying; ++k) {
+            VGB_REQUIRE(varying_idx[k] >= 0 && varying_idx[k] < g.np, "varying parameter index out of range");
+            g.vidx[varying_idx[k]] = k;
+        }
+        if (n_varying) g.varying.assign(varying_values, varying_values + (size_t)n_varying * n_dev);
+        if (temperatures) g.temps.assign(temperatures, temperatures + n_dev);
+        g.temp_shared = temp_shared;
+        c->groups.push_back(std::move(g));
+    });
+}
+
+int vgb_circuit_set_sources(void* h, int is_current, int n, const int* kinds, const int* offsets,
+                            const int* counts, const double* params) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(n == (is_current ? c->n_isrc : c->n_vsrc), "source count mismatch");
+        Sources& s = is_current ? c->isrc_wave : c->vsrc_wave;
+        s.kind.assign(kinds, kinds + n);
+        s.off.assign(offsets, offsets + n);
+        s.cnt.assign(counts, counts + n);
+        size_t total = 0;
+        for (int k = 0; k < n; ++k) {
+            VGB_REQUIRE(kinds[k] >= 0 && kinds[k] <= 3, "unknown source kind");
+            VGB_REQUIRE(offsets[k] >= 0 && counts[k] >= 1, "bad source parameter range");
+            if (kinds[k] == SRC_PWL) VGB_REQUIRE(counts[k] >= 3 && (counts[k] - 1) % 2 == 0, "PWL needs pairs");
+            if (kinds[k] == SRC_PULSE) VGB_REQUIRE(counts[k] >= 7, "PULSE needs 7 parameters");
+            if (kinds[k] == SRC_SINE) VGB_REQUIRE(counts[k] >= 4, "SINE needs 4 parameters");
+            total = std::max(total, (size_t)offsets[k] + counts[k]);
+        }
+        s.data.assign(params, params + total);
+        if (c->finalized) {
+            s.d_kind.upload(s.kind);
+            s.d_off.upload(s.off);
+            s.d_cnt.upload(s.cnt);
+            s.d_data.upload(s.data);
+        }
+    });
+}
+
+int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(!c->finalized, "circuit already finalized");
+        c->internal_idx.assign(node_idx, node_idx + n);
+    });
+}
+
+int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(!c->finalized, "circuit already finalized");
+        VGB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (FP64) or 1 (FP32+refinement)");
+        VGB_REQUIRE(refine_sweeps >= 0 && refine_sweeps <= 3, "refine_sweeps must be in [0, 3]");
+        c->gmin = gmin;
+        c->solver_kind = precision;
+        c->refine_sweeps = refine_sweeps;
+        build_pattern(*c);
+        build_sparse_symbolic(*c);
+        VGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        VGB_CUDA(cudaHostAlloc((void**)&c->h_status, sizeof(NRStatus), cudaHostAllocDefault));
+        for (auto& g : c->groups) {
+            g.d_node_map.upload(g.node_map);
+            g.d_vidx.upload(g.vidx);
+            g.d_shared.upload(g.shared.empty() ? std::vector<double>{0.0} : g.shared);
+            if (!g.varying.empty()) g.d_varying.upload(g.varying);
+            if (!g.temps.empty()) g.d_temps.upload(g.temps);
+        }
+        c->d_csr_src_ptr.upload(c->csr_src_ptr);
+        c->d_csr_src.upload(c->csr_src);
+        c->d_csr_const.upload(c->csr_const);
+        c->d_csr_diag.upload(c->csr_diag);
+        c->d_res_src_ptr.upload(c->res_src_ptr);
+        c->d_res_src.upload(c->res_src);
+        c->d_rq_src.upload(c->rq_src);
+        c->d_nb_ptr.upload(c->nb_ptr);
+        c->d_nb_idx.upload(c->nb_idx);
+        c->d_ni_ptr.upload(c->ni_ptr);
+        c->d_ni_idx.upload(c->ni_idx);
+        c->d_vsrc_p.upload(c->vsrc_p);
+        c->d_vsrc_n.upload(c->vsrc_n);
+        c->d_conv_mask.upload(c->conv_mask);
+        c->d_indptr.upload(c->indptr);
+        c->d_indices.upload(c->indices);
+        c->d_contrib.alloc(std::max<long long>(c->n_contrib, 1));
+        for (Sources* s : {&c->vsrc_wave, &c->isrc_wave}) {
+            if (s->kind.empty()) continue;
+            s->d_kind.upload(s->kind);
+            s->d_off.upload(s->off);
+            s->d_cnt.upload(s->cnt);
+            s->d_data.upload(s->data);
+        }
+        SparseLU& L = c->lu;
+        L.d_col_ptr.upload(L.col_ptr);
+        L.d_nU.upload(L.nU);
+        L.d_rows.upload(L.rows);
+        L.d_f2a.upload(L.f2a);
+        L.d_ustart.upload(L.ustart);
+        L.d_umap_ptr.upload(L.umap_ptr);
+        L.d_umap.upload(L.umap.empty() ? std::vector<int>{0} : L.umap);
+        L.d_lrow_ptr.upload(L.lrow_ptr);
+        L.d_lrow_pos.upload(L.lrow_pos.empty() ? std::vector<long long>{0} : L.lrow_pos);
+        L.d_lrow_col.upload(L.lrow_col.empty() ? std::vector<int>{0} : L.lrow_col);
+        L.d_urow_ptr.upload(L.urow_ptr);
+        L.d_urow_pos.upload(L.urow_pos.empty() ? std::vector<long long>{0} : L.urow_pos);
+        L.d_urow_col.upload(L.urow_col.empty() ? std::vector<int>{0} : L.urow_col);
+        std::vector<int> brow(L.n);
+        for (int i = 0; i < L.n; ++i) brow[i] = L.perm_r[L.q[i]];
+        L.d_brow.upload(brow);
+        L.d_q.upload(L.q);
+        if (precision == 1) L.d_vals32.alloc(std::max<long long>(L.nnz_lu, 1));
+        else L.d_vals64.alloc(std::max<long long>(L.nnz_lu, 1));
+        L.d_done.alloc(3 * (size_t)std::max(L.n, 1));
+        L.d_done.zero(c->stream);
+        L.d_counters.alloc(4);
+        const size_t na = std::max(c->n_aug, 1), nu = std::max(c->n_unk, 1);
+        c->d_csr_vals.alloc(std::max(c->nnz, 1));
+        c->d_f.alloc(na);
+        c->d_delta.alloc(na);
+        c->d_rhs.alloc(na);
+        c->d_work.alloc(na);
+        c->d_work2.alloc(2 * na);
+        c->d_Q.alloc(nu);
+        c->d_maxc.alloc(nu);
+        c->d_fres.alloc(nu);
+        c->d_status.alloc(1);
+        c->d_status.zero(c->stream);
+        VGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->finalized = true;
+    });
+}
+
+int vgb_pattern_info(void* h, int* n_aug, int* nnz, int64_t* nnz_lu, int64_t* lu_flops) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        if (n_aug) *n_aug = c->n_aug;
+        if (nnz) *nnz = c->nnz;
+        if (nnz_lu) *nnz_lu = c->lu.nnz_lu;
+        if (lu_flops) *lu_flops = c->lu.flops;
+    });
+}
+
+int vgb_pattern_csr(void* h, int* indptr, int* indices) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        std::memcpy(indptr, c->indptr.data(), c->indptr.size() * sizeof(int));
+        std::memcpy(indices, c->indices.data(), c->indices.size() * sizeof(int));
+    });
+}
+
+int vgb_stamp_positions(void* h, int group, int* out) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        VGB_REQUIRE(group >= 0 && group < (int)c->groups.size(), "group out of range");
+        const auto& p = c->groups[group].csr_pos;
+        std::memcpy(out, p.data(), p.size() * sizeof(int));
+    });
+}
+
+int vgb_special_positions(void* h, int* diag, int* vsrc) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        if (diag) std::memcpy(diag, c->diag_pos.data(), c->diag_pos.size() * sizeof(int));
+        if (vsrc)
+            for (int q = 0; q < 4; ++q)
+                std::memcpy(vsrc + (size_t)q * c->n_vsrc, c->vs_pos[q].data(), c->n_vsrc * sizeof(int));
+    });
+}
+
+} // extern "C"
+
+namespace vgb {
+
+
+
+DefaultVecs& defaults_for(Circuit& c, double abstol, cudaStream_t s) {
+    static thread_local std::vector<std::pair<Circuit*, DefaultVecs*>> cache;
+    for (auto& e : cache)
+        if (e.first == &c) {
+            if (e.second->floor_value != abstol) {
+                std::vector<double> fl(std::max(c.n_unk, 1), abstol);
+                e.second->floor_abstol.upload(fl);
+                e.second->floor_value = abstol;
+            }
+            return *e.second;
+        }
+    auto* d = new DefaultVecs();
+    const size_t m = std::max({c.n_unk, c.n_vsrc, c.n_isrc, 1});
+    d->zeros.alloc(m);
+    d->zeros.zero(s);
+    std::vector<double> fl(std::max(c.n_unk, 1), abstol);
+    d->floor_abstol.upload(fl);
+    d->floor_value = abstol;
+    VGB_CUDA(cudaStreamSynchronize(s));
+    cache.push_back({&c, d});
+    return *d;
+}
+
+} // namespace vgb
+
+extern "C" {
+
+int vgb_build_system(void* h, const double* X, const double* vsrc_vals, const double* isrc_vals,
+                     const double* Q_prev, const double* dQdt_prev, const double* Q_prev2, const double* coeffs,
+                     double* csr_vals, double* f, double* Q, double* maxc, double* fres, vgb_stream_t stream) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        cudaStream_t s = pick(c, stream);
+        DefaultVecs& dv = defaults_for(*c, 1e-12, s);
+        Coeffs k;
+        k.c0 = coeffs[0];
+        k.c1 = coeffs[1];
+        k.d1 = coeffs[2];
+        k.c2 = coeffs[3];
+        k.gshunt = coeffs[4];
+        const double* z = dv.zeros.p;
+        launch_status_reset(c->d_status.p, s);
+        build_system(*c, X, vsrc_vals ? vsrc_vals : z, isrc_vals ? isrc_vals : z, Q_prev ? Q_prev : z,
+                     dQdt_prev ? dQdt_prev : z, Q_prev2 ? Q_prev2 : z, k, dv.floor_abstol.p, 1e-3, 1e-6,
+                     csr_vals ? csr_vals : c->d_csr_vals.p, f ? f : c->d_f.p, Q ? Q : c->d_Q.p,
+                     maxc ? maxc : c->d_maxc.p, fres ? fres : c->d_fres.p, s);
+        VGB_CUDA(cudaGetLastError());
+        VGB_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int vgb_eval_group(void* h, int group, const double* X, double* out, vgb_stream_t stream) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        VGB_REQUIRE(group >= 0 && group < (int)c->groups.size(), "group out of range");
+        cudaStream_t s = pick(c, stream);
+        auto& g = c->groups[group];
+        g.me->launch_raw(g.args(c->d_contrib.p), X, out, s);
+        VGB_CUDA(cudaGetLastError());
+        VGB_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int vgb_linear_solve(void* h, const double* csr_vals, const double* rhs, double* x, vgb_stream_t stream) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        cudaStream_t s = pick(c, stream);
+        launch_status_reset(c->d_status.p, s);
+        VGB_CUDA(cudaMemsetAsync(&c->d_status.p->dev_err, 0, sizeof(int), s));
+        linear_solve(*c, csr_vals, rhs, x, s);
+        VGB_CUDA(cudaMemcpyAsync(c->h_status, c->d_status.p, sizeof(NRStatus), cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        if (c->h_status->dev_err & DEV_ERR_TIMEOUT) throw Error(VGB_ERR_TIMEOUT, "sparse LU wait timed out");
+        if (c->h_status->dev_err & DEV_ERR_PIVOT) throw Error(VGB_ERR_NUMERIC, "zero or non-finite pivot");
+    });
+}
+
+int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc_vals, const double* Q_prev,
+                 const double* dQdt_prev, const double* Q_prev2, const double* res_tol_floor, const double* opts,
+                 int max_iter, int* iterations, int* converged, double* max_f, double* Q_out, double* dQdt_out,
+                 double* I_vsrc, double* maxc_out, vgb_stream_t stream) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        VGB_REQUIRE(max_iter >= 1, "max_iter must be >= 1");
+        cudaStream_t s = pick(c, stream);
+        Coeffs k{opts[0], opts[1], opts[2], opts[3], opts[4]};
+        NROpts o;
+        o.reltol = opts[5];
+        o.abstol = opts[6];
+        o.vntol = opts[7];
+        o.damping = opts[8];
+        o.max_step = opts[9];
+        DefaultVecs& dv = defaults_for(*c, o.abstol, s);
+        const double* z = dv.zeros.p;
+        const double* vs = vsrc_vals ? vsrc_vals : z;
+        const double* is = isrc_vals ? isrc_vals : z;
+        const double* Qp = Q_prev ? Q_prev : z;
+        const double* dQp = dQdt_prev ? dQdt_prev : z;
+        const double* Qp2 = Q_prev2 ? Q_prev2 : z;
+        VGB_CUDA(cudaMemsetAsync(&c->d_status.p->dev_err, 0, sizeof(int), s));
+        NRResult r = nr_loop(*c, X, vs, is, Qp, dQp, Qp2, res_tol_floor ? res_tol_floor : dv.floor_abstol.p, k, o,
+                             max_iter, s);
+        // post-convergence rebuild for Q, I_vsource, max_res_contrib (solver_factories.py:689-713)
+        launch_status_reset(c->d_status.p, s);
+        build_system(*c, X, vs, is, Qp, dQp, Qp2, k, dv.floor_abstol.p, o.reltol, o.vntol, c->d_csr_vals.p,
+                     c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
+        if (Q_out) VGB_CUDA(cudaMemcpyAsync(Q_out, c->d_Q.p, c->n_unk * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (maxc_out)
+            VGB_CUDA(cudaMemcpyAsync(maxc_out, c->d_maxc.p, c->n_unk * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (I_vsrc) launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, I_vsrc, c->n_vsrc, s);
+        if (dQdt_out) launch_dqdt(c->d_Q.p, Qp, dQp, Qp2, k.c0, k.c1, k.d1, k.c2, dQdt_out, c->n_unk, s);
+        VGB_CUDA(cudaStreamSynchronize(s));
+        if (iterations) *iterations = r.iterations;
+        if (converged) *converged = r.converged ? 1 : 0;
+        if (max_f) *max_f = r.max_f;
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,93 @@
+// Core steps shared by the C-ABI entry points and the transient driver.
+#pragma once
+
+#include "vgb_kernels.cuh"
+
+namespace vgb {
+
+struct Coeffs {
+    double c0 = 0, c1 = 0, d1 = 0, c2 = 0, gshunt = 0;
+};
+
+inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
+    for (auto& g : c.groups) g.me->launch(g.args(c.d_contrib.p), X, c0, s);
+}
+
+// build_system: eval + assemble (+ residual check into d_status)
+inline void build_system(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
+                         const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
+                         double reltol, double vntol, double* csr, double* f, double* Q, double* maxc,
+                         double* fres, cudaStream_t s) {
+    eval_all(c, X, k.c0, s);
+    AssembleArgs a{};
+    a.nnz = c.nnz;
+    a.n_unk = c.n_unk;
+    a.n_vsrc = c.n_vsrc;
+    a.n_nodes = c.n_nodes;
+    a.csr_src_ptr = c.d_csr_src_ptr.p;
+    a.csr_src = c.d_csr_src.p;
+    a.csr_const = c.d_csr_const.p;
+    a.csr_diag = c.d_csr_diag.p;
+    a.res_src_ptr = c.d_res_src_ptr.p;
+    a.res_src = c.d_res_src.p;
+    a.rq_src = c.d_rq_src.p;
+    a.nb_ptr = c.d_nb_ptr.p;
+    a.nb_idx = c.d_nb_idx.p;
+    a.ni_ptr = c.d_ni_ptr.p;
+    a.ni_idx = c.d_ni_idx.p;
+    a.vsrc_p = c.d_vsrc_p.p;
+    a.vsrc_n = c.d_vsrc_n.p;
+    a.contrib = c.d_contrib.p;
+    a.X = X;
+    a.vsrc_vals = vs;
+    a.isrc_vals = is;
+    a.Q_prev = Qp;
+    a.dQdt_prev = dQp;
+    a.Q_prev2 = Qp2;
+    a.c0 = k.c0;
+    a.c1 = k.c1;
+    a.d1 = k.d1;
+    a.c2 = k.c2;
+    a.gdiag = c.gmin + k.gshunt;
+    a.res_tol_floor = res_tol_floor;
+    a.reltol = reltol;
+    a.vntol = vntol;
+    a.conv_mask = c.d_conv_mask.p;
+    a.csr_vals = csr;
+    a.f = f;
+    a.Q = Q;
+    a.maxc = maxc;
+    a.fres = fres;
+    a.st = c.d_status.p;
+    launch_assemble(a, s);
+}
+
+inline void linear_solve(Circuit& c, const double* csr, const double* rhs, double* x, cudaStream_t s) {
+    const bool fp32 = c.solver_kind == 1;
+    lu_factor(c, csr, fp32, s);
+    lu_solve(c, csr, rhs, x, fp32, c.refine_sweeps, s);
+}
+
+struct NROpts {
+    double reltol = 1e-3, abstol = 1e-12, vntol = 1e-6, damping = 1.0, max_step = 1e30;
+};
+
+struct NRResult {
+    int iterations = 0;
+    bool converged = false;
+    double max_f = 0.0;
+    int dev_err = 0;
+    bool nonfinite = false;
+};
+
+struct DefaultVecs {
+    DevBuf<double> zeros, floor_abstol;
+    double floor_value = -1;
+};
+
+NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
+                 const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
+                 const NROpts& o, int max_iter, cudaStream_t s);
+DefaultVecs& defaults_for(Circuit& c, double abstol, cudaStream_t s);
+
+} // namespace vgb

@@ -1,0 +1,128 @@
+// Kernel skeleton for generated device models.
+//
+// One thread evaluates one instance: it gathers the instance's node voltages
+// through the node map, reads its parameters (shared across the group or
+// per instance, struct-of-arrays), runs the generated model body and writes
+// the per-instance contributions that the assembly pass gathers into the CSR
+// values and the residual vectors.  No atomics: every output has exactly one
+// writer, which keeps stamping deterministic.
+//
+// Contribution layout of a group with n instances, NJ Jacobian entries and
+// NN model nodes (slot-major, so each store is coalesced across the warp):
+//   slot k < NJ           : jac_resist[k] + c0 * jac_react[k]   (NaN -> 0)
+//   slot NJ + r           : residual_resist[r]
+//   slot NJ + NN + r      : residual_react[r]
+// This mirrors the reference's per-model stamping step
+// (vajax/analysis/mna_builder.py:927-966), which forms jac_r + c0*jac_c,
+// masks NaN to 0 and scatter-adds into the CSR data and the dense vectors.
+#pragma once
+
+#include "vgb_common.cuh"
+
+namespace vgb {
+
+struct GroupArgs {
+    int n_dev;
+    const int* __restrict__ node_map;     // [NN][n_dev] circuit node index, 0 = ground
+    const double* __restrict__ shared;    // [NP] parameter values common to the group
+    const int* __restrict__ vidx;         // [NP] -1 = shared, else column in `varying`
+    const double* __restrict__ varying;   // [n_var][n_dev]
+    const double* __restrict__ temperature; // [n_dev] or nullptr (use temp_shared)
+    double temp_shared;
+    double* __restrict__ contrib;         // [NJ + 2 NN][n_dev]
+    long long batch_stride_x;             // stride of X between circuit replicas (batched mode)
+    int inst_per_replica;                 // instances per replica (batched mode), else n_dev
+};
+
+template <class M>
+struct ParamReader {
+    const GroupArgs& g;
+    int i;
+    __device__ __forceinline__ double operator()(int k) const {
+        int v = __ldg(g.vidx + k);
+        return v < 0 ? __ldg(g.shared + k) : __ldg(g.varying + (size_t)v * g.n_dev + i);
+    }
+};
+
+template <class M>
+__global__ void __launch_bounds__(128) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n_dev) return;
+    const double* Xr = X;
+    if (g.batch_stride_x) Xr = X + (long long)(i / g.inst_per_replica) * g.batch_stride_x;
+    double V[M::NN];
+#pragma unroll
+    for (int t = 0; t < M::NN; ++t) V[t] = Xr[__ldg(g.node_map + (size_t)t * g.n_dev + i)];
+    const double T = g.temperature ? __ldg(g.temperature + i) : g.temp_shared;
+    double rr[M::NN], rq[M::NN], jr[M::NJ > 0 ? M::NJ : 1], jq[M::NJ > 0 ? M::NJ : 1];
+    ParamReader<M> P{g, i};
+    M::eval(P, T, V, rr, rq, jr, jq);
+    const size_t n = g.n_dev;
+#pragma unroll
+    for (int k = 0; k < M::NJ; ++k) g.contrib[k * n + i] = nan0(jr[k] + c0 * jq[k]);
+#pragma unroll
+    for (int r = 0; r < M::NN; ++r) {
+        g.contrib[(M::NJ + r) * n + i] = rr[r];
+        g.contrib[(M::NJ + M::NN + r) * n + i] = rq[r];
+    }
+}
+
+// Raw per-instance outputs (no c0 combination) for parity tests of the model body.
+template <class M>
+__global__ void __launch_bounds__(128) eval_raw_kernel(GroupArgs g, const double* __restrict__ X,
+                                                       double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n_dev) return;
+    double V[M::NN];
+#pragma unroll
+    for (int t = 0; t < M::NN; ++t) V[t] = X[__ldg(g.node_map + (size_t)t * g.n_dev + i)];
+    const double T = g.temperature ? __ldg(g.temperature + i) : g.temp_shared;
+    double rr[M::NN], rq[M::NN], jr[M::NJ > 0 ? M::NJ : 1], jq[M::NJ > 0 ? M::NJ : 1];
+    ParamReader<M> P{g, i};
+    M::eval(P, T, V, rr, rq, jr, jq);
+    const size_t n = g.n_dev;
+    for (int r = 0; r < M::NN; ++r) {
+        out[(size_t)r * n + i] = rr[r];
+        out[(size_t)(M::NN + r) * n + i] = rq[r];
+    }
+    for (int k = 0; k < M::NJ; ++k) {
+        out[(size_t)(2 * M::NN + k) * n + i] = jr[k];
+        out[(size_t)(2 * M::NN + M::NJ + k) * n + i] = jq[k];
+    }
+}
+
+struct ModelEntry {
+    const char* name;
+    int nn, nj, np;
+    const int* jrow;
+    const int* jcol;
+    void (*launch)(const GroupArgs&, const double* X, double c0, cudaStream_t s);
+    void (*launch_raw)(const GroupArgs&, const double* X, double* out, cudaStream_t s);
+};
+
+template <class M>
+void launch_eval(const GroupArgs& g, const double* X, double c0, cudaStream_t s)
+{
+    if (g.n_dev == 0) return;
+    eval_kernel<M><<<ceil_div(g.n_dev, 128), 128, 0, s>>>(g, X, c0);
+}
+
+template <class M>
+void launch_eval_raw(const GroupArgs& g, const double* X, double* out, cudaStream_t s)
+{
+    if (g.n_dev == 0) return;
+    eval_raw_kernel<M><<<ceil_div(g.n_dev, 128), 128, 0, s>>>(g, X, out);
+}
+
+template <class M>
+ModelEntry make_model_entry(const char* name)
+{
+    return ModelEntry{name, M::NN, M::NJ, M::NP, M::JROW, M::JCOL, &launch_eval<M>, &launch_eval_raw<M>};
+}
+
+// Defined in the generated translation unit.
+const ModelEntry* model_table(int* count);
+
+} // namespace vgb

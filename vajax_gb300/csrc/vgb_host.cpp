@@ -1,0 +1,368 @@
+// Host-side, one-time construction for a circuit:
+//  * the CSR pattern of the augmented MNA Jacobian and the integer stamp maps
+//    (reference: vajax/analysis/transient/full_mna.py:421-548 and
+//    vajax/analysis/mna_builder.py:44-255), reproduced bit-exactly;
+//  * the atomic-free gather lists the assembly kernel consumes;
+//  * ordering and symbolic factorisation for the static-pivot sparse LU.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <queue>
+
+#include "vgb_circuit.h"
+
+namespace vgb {
+
+static int find_pos(const std::vector<long long>& ul, long long key) {
+    auto it = std::lower_bound(ul.begin(), ul.end(), key);
+    if (it == ul.end() || *it != key) return -1;
+    return (int)(it - ul.begin());
+}
+
+void build_pattern(Circuit& c) {
+    const int n_unk = c.n_unk, n_aug = c.n_aug;
+    const long long N = n_aug;
+    std::vector<long long> lin;
+    size_t est = (size_t)n_unk + 4 * (size_t)c.n_vsrc;
+    for (auto& g : c.groups) est += (size_t)g.n_dev * g.nj;
+    lin.reserve(est);
+    bool masked = false;
+    // device Jacobian entries (mna_builder.py:44-118, masked pairs -> (0,0) as in mna.py:mask_coo_matrix)
+    for (auto& g : c.groups) {
+        for (int i = 0; i < g.n_dev; ++i) {
+            for (int k = 0; k < g.nj; ++k) {
+                int r = g.node_map[(size_t)g.me->jrow[k] * g.n_dev + i];
+                int col = g.node_map[(size_t)g.me->jcol[k] * g.n_dev + i];
+                if (r > 0 && col > 0) lin.push_back((long long)(r - 1) * N + (col - 1));
+                else masked = true;
+            }
+        }
+    }
+    // vsource incidence (mna.py:build_vsource_incidence_coo); invalid terminals -> (0,0)
+    for (int k = 0; k < c.n_vsrc; ++k) {
+        int p = c.vsrc_p[k], n = c.vsrc_n[k];
+        long long b = n_unk + k;
+        if (p > 0) { lin.push_back((long long)(p - 1) * N + b); lin.push_back(b * N + (p - 1)); }
+        else masked = true;
+        if (n > 0) { lin.push_back((long long)(n - 1) * N + b); lin.push_back(b * N + (n - 1)); }
+        else masked = true;
+    }
+    // node diagonals (mna.py:assemble_sparse_jacobian)
+    for (int i = 0; i < n_unk; ++i) lin.push_back((long long)i * N + i);
+    if (masked && n_aug > 0) lin.push_back(0);
+    std::sort(lin.begin(), lin.end());
+    lin.erase(std::unique(lin.begin(), lin.end()), lin.end());
+    c.unique_linear = lin;
+    c.nnz = (int)lin.size();
+    c.indptr.assign(n_aug + 1, 0);
+    c.indices.resize(c.nnz);
+    for (int e = 0; e < c.nnz; ++e) {
+        int r = (int)(lin[e] / N);
+        c.indices[e] = (int)(lin[e] % N);
+        c.indptr[r + 1]++;
+    }
+    for (int r = 0; r < n_aug; ++r) c.indptr[r + 1] += c.indptr[r];
+
+    // stamp positions (mna_builder.py:126-160)
+    long long base = 0;
+    for (auto& g : c.groups) {
+        g.contrib_base = base;
+        base += (long long)g.n_dev * (g.nj + 2 * g.nn);
+        g.csr_pos.assign((size_t)g.n_dev * g.nj, -1);
+        for (int i = 0; i < g.n_dev; ++i)
+            for (int k = 0; k < g.nj; ++k) {
+                int r = g.node_map[(size_t)g.me->jrow[k] * g.n_dev + i];
+                int col = g.node_map[(size_t)g.me->jcol[k] * g.n_dev + i];
+                if (r > 0 && col > 0) g.csr_pos[(size_t)i * g.nj + k] = find_pos(lin, (long long)(r - 1) * N + (col - 1));
+            }
+    }
+    c.n_contrib = base;
+    VGB_REQUIRE(base < (1LL << 31), "contribution buffer exceeds 2^31 entries");
+
+    // diagonal positions (mna_builder.py:163-184): every node diagonal exists
+    c.diag_pos.resize(n_unk);
+    for (int i = 0; i < n_unk; ++i) c.diag_pos[i] = find_pos(lin, (long long)i * N + i);
+    // vsource positions (mna_builder.py:187-255)
+    for (auto& v : c.vs_pos) v.assign(c.n_vsrc, -1);
+    for (int k = 0; k < c.n_vsrc; ++k) {
+        int p = c.vsrc_p[k], n = c.vsrc_n[k];
+        long long b = n_unk + k;
+        if (p > 0) { c.vs_pos[0][k] = find_pos(lin, (long long)(p - 1) * N + b); c.vs_pos[2][k] = find_pos(lin, b * N + (p - 1)); }
+        if (n > 0) { c.vs_pos[1][k] = find_pos(lin, (long long)(n - 1) * N + b); c.vs_pos[3][k] = find_pos(lin, b * N + (n - 1)); }
+    }
+
+    // gather lists for the CSR values
+    std::vector<int> cnt(c.nnz + 1, 0);
+    for (auto& g : c.groups)
+        for (size_t t = 0; t < g.csr_pos.size(); ++t)
+            if (g.csr_pos[t] >= 0) cnt[g.csr_pos[t] + 1]++;
+    for (int e = 0; e < c.nnz; ++e) cnt[e + 1] += cnt[e];
+    c.csr_src_ptr = cnt;
+    c.csr_src.assign(cnt[c.nnz], 0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (auto& g : c.groups)
+        for (int i = 0; i < g.n_dev; ++i)
+            for (int k = 0; k < g.nj; ++k) {
+                int pos = g.csr_pos[(size_t)i * g.nj + k];
+                if (pos >= 0) c.csr_src[fill[pos]++] = (int)(g.contrib_base + (long long)k * g.n_dev + i);
+            }
+    c.csr_const.assign(c.nnz, 0.0);
+    c.csr_diag.assign(c.nnz, 0);
+    for (int k = 0; k < c.n_vsrc; ++k) {
+        if (c.vs_pos[0][k] >= 0) c.csr_const[c.vs_pos[0][k]] += 1.0;
+        if (c.vs_pos[1][k] >= 0) c.csr_const[c.vs_pos[1][k]] -= 1.0;
+        if (c.vs_pos[2][k] >= 0) c.csr_const[c.vs_pos[2][k]] += 1.0;
+        if (c.vs_pos[3][k] >= 0) c.csr_const[c.vs_pos[3][k]] -= 1.0;
+    }
+    for (int i = 0; i < n_unk; ++i) c.csr_diag[c.diag_pos[i]] = 1;
+
+    // residual gather lists (per node row)
+    std::vector<int> rc(n_unk + 1, 0);
+    for (auto& g : c.groups)
+        for (int t = 0; t < g.nn; ++t)
+            for (int i = 0; i < g.n_dev; ++i) {
+                int node = g.node_map[(size_t)t * g.n_dev + i];
+                if (node > 0) rc[node]++;
+            }
+    for (int r = 0; r < n_unk; ++r) rc[r + 1] += rc[r];
+    c.res_src_ptr = rc;
+    c.res_src.assign(rc[n_unk], 0);
+    c.rq_src.assign(rc[n_unk], 0);
+    std::vector<int> rf(rc.begin(), rc.end() - 1);
+    for (auto& g : c.groups)
+        for (int i = 0; i < g.n_dev; ++i)
+            for (int t = 0; t < g.nn; ++t) {
+                int node = g.node_map[(size_t)t * g.n_dev + i];
+                if (node <= 0) continue;
+                int slot = rf[node - 1]++;
+                c.res_src[slot] = (int)(g.contrib_base + (long long)(g.nj + t) * g.n_dev + i);
+                c.rq_src[slot] = (int)(g.contrib_base + (long long)(g.nj + g.nn + t) * g.n_dev + i);
+            }
+
+    auto incidence = [&](const std::vector<int>& P, const std::vector<int>& Nn, std::vector<int>& ptr,
+                         std::vector<int>& idx) {
+        ptr.assign(n_unk + 1, 0);
+        for (size_t k = 0; k < P.size(); ++k) {
+            if (P[k] > 0) ptr[P[k]]++;
+            if (Nn[k] > 0) ptr[Nn[k]]++;
+        }
+        for (int r = 0; r < n_unk; ++r) ptr[r + 1] += ptr[r];
+        idx.assign(ptr[n_unk], 0);
+        std::vector<int> f(ptr.begin(), ptr.end() - 1);
+        for (size_t k = 0; k < P.size(); ++k) {
+            if (P[k] > 0) idx[f[P[k] - 1]++] = (int)k + 1;
+            if (Nn[k] > 0) idx[f[Nn[k] - 1]++] = -((int)k + 1);
+        }
+    };
+    incidence(c.vsrc_p, c.vsrc_n, c.nb_ptr, c.nb_idx);
+    incidence(c.isrc_p, c.isrc_n, c.ni_ptr, c.ni_idx);
+
+    c.conv_mask.assign(n_aug, 1);
+    for (int idx : c.internal_idx)
+        if (idx > 0 && idx - 1 < n_unk) c.conv_mask[idx - 1] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Sparse LU symbolic phase
+// ---------------------------------------------------------------------------
+
+// Minimum-degree ordering on a symmetric pattern.  Rows whose degree is far
+// above the average (supply rails) are set aside and ordered last, the usual
+// dense-row rule of approximate-minimum-degree codes.
+static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> adj) {
+    std::vector<int> order;
+    order.reserve(n);
+    const int dense_thr = std::max(16, (int)(10.0 * std::sqrt((double)std::max(n, 1))));
+    std::vector<char> state(n, 0);  // 0 live, 1 eliminated, 2 dense
+    for (int v = 0; v < n; ++v)
+        if ((int)adj[v].size() > dense_thr) state[v] = 2;
+    for (int v = 0; v < n; ++v) {
+        if (state[v] == 2) continue;
+        auto& a = adj[v];
+        a.erase(std::remove_if(a.begin(), a.end(), [&](int u) { return state[u] == 2; }), a.end());
+    }
+    using P = std::pair<int, int>;
+    std::priority_queue<P, std::vector<P>, std::greater<P>> pq;
+    for (int v = 0; v < n; ++v)
+        if (state[v] == 0) pq.push({(int)adj[v].size(), v});
+    std::vector<int> tmp;
+    while (!pq.empty()) {
+        auto [d, v] = pq.top();
+        pq.pop();
+        if (state[v] != 0 || d != (int)adj[v].size()) continue;
+        state[v] = 1;
+        order.push_back(v);
+        std::vector<int> nb;
+        nb.swap(adj[v]);
+        for (int u : nb) {
+            auto& au = adj[u];
+            tmp.clear();
+            std::set_union(au.begin(), au.end(), nb.begin(), nb.end(), std::back_inserter(tmp));
+            tmp.erase(std::remove_if(tmp.begin(), tmp.end(), [&](int w) { return w == u || w == v; }), tmp.end());
+            au.swap(tmp);
+            pq.push({(int)au.size(), u});
+        }
+    }
+    for (int v = 0; v < n; ++v)
+        if (state[v] == 2) order.push_back(v);
+    return order;
+}
+
+void build_sparse_symbolic(Circuit& c) {
+    SparseLU& L = c.lu;
+    const int n = c.n_aug;
+    L.n = n;
+    // 1. static-pivot transversal for the voltage-source rows: swap the KCL row
+    //    of a source terminal with the source's branch row so both diagonals
+    //    are exactly +-1 (the branch rows have a structurally zero diagonal).
+    L.perm_r.resize(n);
+    std::iota(L.perm_r.begin(), L.perm_r.end(), 0);
+    std::vector<char> used(n, 0);
+    for (int k = 0; k < c.n_vsrc; ++k) {
+        int b = c.n_unk + k;
+        int p = c.vsrc_p[k], m = c.vsrc_n[k];
+        int r = -1;
+        if (p > 0 && !used[p - 1]) r = p - 1;
+        else if (m > 0 && !used[m - 1]) r = m - 1;
+        if (r < 0) continue;
+        std::swap(L.perm_r[r], L.perm_r[b]);
+        used[r] = used[b] = 1;
+    }
+    std::vector<int> pinv_r(n);
+    for (int r = 0; r < n; ++r) pinv_r[L.perm_r[r]] = r;
+
+    // 2. symmetric pattern of B = P_r A
+    std::vector<std::vector<int>> adj(n);
+    for (int ra = 0; ra < n; ++ra) {
+        int r = pinv_r[ra];
+        for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
+            int col = c.indices[e];
+            if (col == r) continue;
+            adj[r].push_back(col);
+            adj[col].push_back(r);
+        }
+    }
+    for (auto& a : adj) { std::sort(a.begin(), a.end()); a.erase(std::unique(a.begin(), a.end()), a.end()); }
+
+    // 3. fill-reducing order
+    L.q = min_degree_order(n, adj);
+    L.qinv.resize(n);
+    for (int i = 0; i < n; ++i) L.qinv[L.q[i]] = i;
+
+    // 4. elimination tree and row structure of L on the permuted pattern
+    std::vector<std::vector<int>> low(n);  // permuted neighbours below the diagonal
+    for (int v = 0; v < n; ++v) {
+        int i = L.qinv[v];
+        for (int u : adj[v]) {
+            int k = L.qinv[u];
+            if (k < i) low[i].push_back(k);
+        }
+    }
+    std::vector<int> parent(n, -1), ancestor(n, -1);
+    for (int i = 0; i < n; ++i) {
+        for (int k : low[i]) {
+            int r = k;
+            while (ancestor[r] != -1 && ancestor[r] != i) { int t = ancestor[r]; ancestor[r] = i; r = t; }
+            if (ancestor[r] == -1) { ancestor[r] = i; parent[r] = i; }
+        }
+    }
+    std::vector<std::vector<int>> rowstruct(n);
+    std::vector<int> mark(n, -1);
+    for (int i = 0; i < n; ++i) {
+        mark[i] = i;
+        auto& rs = rowstruct[i];
+        for (int k : low[i]) {
+            int r = k;
+            while (r != -1 && mark[r] != i) { rs.push_back(r); mark[r] = i; r = parent[r]; }
+        }
+        std::sort(rs.begin(), rs.end());
+    }
+    std::vector<std::vector<int>> lcol(n);
+    for (int i = 0; i < n; ++i)
+        for (int k : rowstruct[i]) lcol[k].push_back(i);  // ascending i
+
+    // 5. column storage: [U rows asc][diag][L rows asc]
+    L.col_ptr.assign(n + 1, 0);
+    L.nU.resize(n);
+    for (int j = 0; j < n; ++j) {
+        L.nU[j] = (int)rowstruct[j].size();
+        L.col_ptr[j + 1] = L.col_ptr[j] + rowstruct[j].size() + 1 + lcol[j].size();
+    }
+    L.nnz_lu = L.col_ptr[n];
+    L.rows.resize(L.nnz_lu);
+    for (int j = 0; j < n; ++j) {
+        long long s = L.col_ptr[j];
+        for (int r : rowstruct[j]) L.rows[s++] = r;
+        L.rows[s++] = j;
+        for (int r : lcol[j]) L.rows[s++] = r;
+    }
+    auto slot_of = [&](int i, int j) -> long long {
+        long long s0 = L.col_ptr[j], s1 = L.col_ptr[j + 1];
+        if (i < j) {
+            auto b = L.rows.begin() + s0, e = b + L.nU[j];
+            auto it = std::lower_bound(b, e, i);
+            return (it != e && *it == i) ? (long long)(it - L.rows.begin()) : -1;
+        }
+        if (i == j) return s0 + L.nU[j];
+        auto b = L.rows.begin() + s0 + L.nU[j] + 1, e = L.rows.begin() + s1;
+        auto it = std::lower_bound(b, e, i);
+        return (it != e && *it == i) ? (long long)(it - L.rows.begin()) : -1;
+    };
+    // 6. A -> factor slot
+    L.f2a.assign(L.nnz_lu, -1);
+    for (int ra = 0; ra < n; ++ra) {
+        int i = L.qinv[pinv_r[ra]];
+        for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
+            int j = L.qinv[c.indices[e]];
+            long long s = slot_of(i, j);
+            VGB_REQUIRE(s >= 0, "symbolic factor misses an entry of A");
+            L.f2a[s] = e;
+        }
+    }
+    // 7. left-looking update maps
+    L.ustart.assign(n + 1, 0);
+    for (int j = 0; j < n; ++j) L.ustart[j + 1] = L.ustart[j] + L.nU[j];
+    long long nUtot = L.ustart[n];
+    L.umap_ptr.assign(nUtot + 1, 0);
+    L.umap.clear();
+    std::vector<int> lookup(n, -1);
+    long long u = 0;
+    for (int j = 0; j < n; ++j) {
+        long long s0 = L.col_ptr[j], s1 = L.col_ptr[j + 1];
+        for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = (int)(s - s0);
+        for (int t = 0; t < L.nU[j]; ++t, ++u) {
+            int k = rowstruct[j][t];
+            for (int i : lcol[k]) {
+                int pos = lookup[i];
+                VGB_REQUIRE(pos >= 0, "fill pattern is not closed under elimination");
+                L.umap.push_back(pos);
+            }
+            L.umap_ptr[u + 1] = (long long)L.umap.size();
+        }
+        for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = -1;
+    }
+    L.flops = 2 * (long long)L.umap.size();
+    // 8. row access for the triangular solves
+    L.lrow_ptr.assign(n + 1, 0);
+    L.lrow_pos.clear();
+    L.lrow_col.clear();
+    for (int i = 0; i < n; ++i) {
+        for (int k : rowstruct[i]) {
+            L.lrow_pos.push_back(slot_of(i, k));
+            L.lrow_col.push_back(k);
+        }
+        L.lrow_ptr[i + 1] = (long long)L.lrow_pos.size();
+    }
+    L.urow_ptr.assign(n + 1, 0);
+    L.urow_pos.clear();
+    L.urow_col.clear();
+    for (int i = 0; i < n; ++i) {
+        for (int j : lcol[i]) {
+            L.urow_pos.push_back(slot_of(i, j));
+            L.urow_col.push_back(j);
+        }
+        L.urow_ptr[i + 1] = (long long)L.urow_pos.size();
+    }
+}
+
+} // namespace vgb

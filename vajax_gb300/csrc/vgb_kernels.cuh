@@ -1,0 +1,52 @@
+// Device kernels of the transient Newton path (declarations + launch helpers).
+#pragma once
+
+#include "vgb_circuit.h"
+
+namespace vgb {
+
+struct AssembleArgs {
+    int nnz, n_unk, n_vsrc, n_nodes;
+    const int* csr_src_ptr; const int* csr_src; const double* csr_const; const unsigned char* csr_diag;
+    const int* res_src_ptr; const int* res_src; const int* rq_src;
+    const int* nb_ptr; const int* nb_idx; const int* ni_ptr; const int* ni_idx;
+    const int* vsrc_p; const int* vsrc_n;
+    const double* contrib;
+    const double* X;
+    const double* vsrc_vals; const double* isrc_vals;
+    const double* Q_prev; const double* dQdt_prev; const double* Q_prev2;
+    double c0, c1, d1, c2, gdiag;
+    const double* res_tol_floor; double reltol, vntol;
+    const unsigned char* conv_mask;
+    double* csr_vals; double* f; double* Q; double* maxc; double* fres;
+    NRStatus* st;
+};
+
+void launch_assemble(const AssembleArgs& a, cudaStream_t s);
+
+struct NRUpdateArgs {
+    int n_unk, n_aug;
+    const double* delta;
+    double* X;
+    double reltol, vntol, abstol, damping, max_step;
+    NRStatus* st;
+};
+void launch_nr_reduce(const NRUpdateArgs& a, cudaStream_t s);
+void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s);
+void launch_status_reset(NRStatus* st, cudaStream_t s);
+
+// Sparse LU (static pivoting, sync-free left-looking)
+void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s);
+// Solve J x = rhs for x (all double, device); fp32 uses FP32 factors with
+// FP64-residual refinement sweeps.
+void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp32, int sweeps, cudaStream_t s);
+
+// misc vector kernels
+void launch_negate(const double* in, double* out, int n, cudaStream_t s);
+void launch_vsrc_current(const double* fres, const int* vsrc_p, double* I, int n_vsrc, cudaStream_t s);
+void launch_eval_sources(const Sources& src, int n, double t, double* out, cudaStream_t s);
+// dQdt = c0 Q + c1 Q_prev + d1 dQdt_prev + c2 Q_prev2 (solver_factories.py:715-720)
+void launch_dqdt(const double* Q, const double* Qp, const double* dQp, const double* Qp2, double c0, double c1,
+                 double d1, double c2, double* out, int n, cudaStream_t s);
+
+} // namespace vgb

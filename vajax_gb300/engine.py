@@ -1,0 +1,229 @@
+"""Reference-shaped engine API on top of the GB300 transient path.
+
+Mirrors ``vajax.analysis.engine.CircuitEngine`` (``vajax/analysis/engine.py``):
+``parse()`` → ``prepare(t_stop=, dt=, ...)`` → ``run_transient()`` returning a
+:class:`TransientResult` with ``times``, ``voltages`` (by node name),
+``currents`` (by voltage-source name) and ``stats`` (the keys of
+``FullMNAStrategy.run``: ``full_mna.py:1168-1186``).  The transient loop, the
+Newton iterations, device evaluation, stamping and the sparse LU all run on
+the GPU inside ``libvajax_gb300.so``; this module only prepares inputs.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Any, Dict, Optional
+
+import numpy as np
+
+from vajax_gb300.circuit import Circuit, ResolvedCircuit
+
+METHODS = {"be": 0, "euler": 0, "backward_euler": 0, "trap": 1, "trapezoidal": 1, "am2": 1,
+           "gear2": 2, "gear": 2, "bdf2": 2, "bdf": 2}
+
+
+@dataclass
+class SimulationOptions:
+    """Subset of ``vajax.analysis.options.SimulationOptions`` (options.py:35-140)."""
+
+    temp: float = 27.0
+    nr_damping: float = 1.0
+    tran_itl: int = 20
+    tran_ft: float = 0.25
+    tran_method: str = "trap"
+    tran_lteratio: float = 3.5
+    tran_redofactor: float = 2.5
+    tran_fs: float = 0.25
+    tran_minpts: int = 50
+    reltol: float = 1e-3
+    abstol: float = 1e-12
+    vntol: float = 1e-6
+    tran_gshunt: float = 0.0
+    gmin: float = 1e-12
+    icmode: str = "op"
+    fixed_step_transient: bool = False
+    maxstep: Optional[float] = None
+    # extension: per-node initial conditions used with icmode='uic'
+    ic: Dict[str, float] = field(default_factory=dict)
+
+
+@dataclass
+class AdaptiveConfig:
+    """``vajax.analysis.transient.adaptive.AdaptiveConfig`` (adaptive.py:37-91)."""
+
+    lte_ratio: float = 3.5
+    redo_factor: float = 2.5
+    reltol: float = 1e-3
+    abstol: float = 1e-12
+    min_dt: float = 1e-15
+    max_dt: float = float("inf")
+    tran_minpts: int = 50
+    warmup_steps: int = 2
+    max_order: int = 2
+    grow_factor: float = 2.0
+    gshunt_init: float = 0.0
+    gshunt_steps: int = 5
+    gshunt_target: float = 0.0
+    tran_fs: float = 0.25
+    tran_ft: float = 0.25
+    integration_method: str = "trap"
+    max_consecutive_rejects: int = 5
+
+
+@dataclass
+class TransientResult:
+    times: np.ndarray
+    voltages: Dict[str, np.ndarray]
+    currents: Dict[str, np.ndarray]
+    stats: Dict[str, Any]
+
+    @property
+    def num_steps(self) -> int:
+        return len(self.times)
+
+    def voltage(self, node: str) -> np.ndarray:
+        if node in self.voltages:
+            return self.voltages[node]
+        for k in self.voltages:
+            if k.lower() == node.lower():
+                return self.voltages[k]
+        raise KeyError(f"Node '{node}' not found")
+
+    def current(self, source: str) -> np.ndarray:
+        return self.currents[source]
+
+
+class CircuitEngine:
+    def __init__(self, circuit: Circuit, options: Optional[SimulationOptions] = None, precision: str = "fp64"):
+        self.circuit = circuit
+        self.options = options or SimulationOptions()
+        self.precision = precision
+        self.rc: Optional[ResolvedCircuit] = None
+        self.device = None
+        self._prepared = False
+        self.analysis_params: Dict[str, float] = {}
+
+    # parse: resolve node numbering and device groups (engine.py:421-486)
+    def parse(self):
+        self.circuit.temperature = self.options.temp + 273.15
+        self.rc = self.circuit.resolve()
+        self.node_names = dict(self.rc.node_names)
+        self.num_nodes = self.rc.n_nodes
+        return self
+
+    def _config(self, t_stop: float, dt: float, cfg: Optional[AdaptiveConfig]) -> AdaptiveConfig:
+        o = self.options
+        if cfg is None:
+            cfg = AdaptiveConfig(lte_ratio=o.tran_lteratio, redo_factor=o.tran_redofactor, reltol=o.reltol,
+                                 abstol=o.abstol, tran_fs=o.tran_fs, tran_ft=o.tran_ft, tran_minpts=o.tran_minpts,
+                                 integration_method=o.tran_method, gshunt_init=o.tran_gshunt)
+            if o.maxstep is not None:
+                cfg.max_dt = o.maxstep
+        return cfg
+
+    def prepare(self, *, t_stop: float, dt: float, adaptive_config: Optional[AdaptiveConfig] = None,
+                max_steps: Optional[int] = None, temperature: Optional[float] = None):
+        from vajax_gb300.runtime import DeviceCircuit
+        if temperature is not None:
+            self.options.temp = temperature - 273.15
+        if self.rc is None or temperature is not None:
+            self.parse()
+        self.t_stop = float(t_stop)
+        self.dt = float(dt)
+        self.config = self._config(t_stop, dt, adaptive_config)
+        # max_steps with 10% headroom (engine.py:875)
+        self.max_steps = max_steps if max_steps is not None else int(t_stop / dt * 1.1) + 10
+        if self.device is None:
+            prec = {"fp64": 0, "fp32": 1, "mixed": 1}[self.precision]
+            self.device = DeviceCircuit(self.rc, precision=prec, refine_sweeps=3, gmin=self.options.gmin)
+        self._prepared = True
+        return self
+
+    # initial state (full_mna.py:694-745 mid-rail, :874-957 DC / uic)
+    def _vdd_value(self) -> float:
+        vmax = 0.0
+        for s in self.rc.vsources:
+            if s.kind == "dc":
+                vmax = max(vmax, abs(s.dc_value()))
+        return vmax if vmax > 0 else 1.0
+
+    def init_mid_rail(self) -> np.ndarray:
+        rc = self.rc
+        vdd = self._vdd_value()
+        V = np.full(rc.n_nodes, vdd / 2.0)
+        V[0] = 0.0
+        for name, idx in rc.node_names.items():
+            low = name.lower()
+            if "vdd" in low or "vcc" in low:
+                V[idx] = vdd
+            elif low in ("gnd", "vss", "0"):
+                V[idx] = 0.0
+        for s, p, n in zip(rc.vsources, rc.vsrc_p, rc.vsrc_n):
+            if n == 0 and p > 0:
+                V[p] = s.dc_value()
+        return V
+
+    def initial_state(self):
+        import torch
+        rc = self.rc
+        dev = self.device
+        n_x = rc.n_nodes + len(rc.vsources)
+        vs0 = torch.as_tensor(rc.source_values(0.0), dtype=torch.float64, device="cuda")
+        is0 = torch.as_tensor(rc.source_values(0.0, True), dtype=torch.float64, device="cuda") if rc.isources else None
+        if self.options.icmode == "uic":
+            X0 = np.zeros(n_x)
+            for node, v in self.options.ic.items():
+                X0[rc.node_names[node]] = v
+            Xd = torch.as_tensor(X0, device="cuda")
+            _, _, Q, _, fres = dev.build_system(Xd, vs0 if len(rc.vsources) else None, is0)
+            I0 = np.where(rc.vsrc_p > 0, -fres.cpu().numpy()[np.maximum(rc.vsrc_p - 1, 0)], 0.0)
+            return X0, Q.cpu().numpy(), I0, np.zeros(rc.n_nodes - 1), True
+        X0 = np.zeros(n_x)
+        X0[: rc.n_nodes] = self.init_mid_rail()
+        Xd = torch.as_tensor(X0, device="cuda")
+        r = dev.nr_solve(Xd, vs0 if len(rc.vsources) else None, is0, c0=0.0, reltol=self.options.reltol,
+                         abstol=self.options.abstol, vntol=self.options.vntol, damping=self.options.nr_damping,
+                         max_iter=self.options.tran_itl)
+        return (r["X"].cpu().numpy(), r["Q"].cpu().numpy(), r["I_vsource"].cpu().numpy(),
+                r["max_res_contrib"].cpu().numpy(), r["converged"])
+
+    def transient_cfg(self) -> Dict[str, float]:
+        cfg = self.config
+        t_stop, dt = self.t_stop, self.dt
+        max_dt = cfg.max_dt
+        if cfg.tran_minpts > 0:
+            max_dt = min(max_dt, t_stop / cfg.tran_minpts)
+        if cfg.tran_fs != 1.0:
+            dt = dt * cfg.tran_fs
+        return dict(t_stop=t_stop, dt=dt, max_dt=max_dt, min_dt=cfg.min_dt, reltol=cfg.reltol, abstol=cfg.abstol,
+                    vntol=self.options.vntol, lte_ratio=cfg.lte_ratio, redo_factor=cfg.redo_factor,
+                    grow_factor=cfg.grow_factor, tran_ft=cfg.tran_ft, nr_damping=self.options.nr_damping,
+                    gshunt_init=cfg.gshunt_init, gshunt_target=cfg.gshunt_target, gshunt_steps=cfg.gshunt_steps,
+                    warmup_steps=cfg.warmup_steps, max_consecutive_rejects=cfg.max_consecutive_rejects,
+                    fixed_step=1.0 if self.options.fixed_step_transient else 0.0,
+                    method=METHODS[str(cfg.integration_method).lower()], n_external=self.rc.n_external,
+                    max_steps=self.max_steps, tran_itl=self.options.tran_itl)
+
+    def run_transient(self) -> TransientResult:
+        if not self._prepared:
+            raise RuntimeError("call prepare(t_stop=..., dt=...) first")
+        X0, Q0, I0, maxc0, dc_conv = self.initial_state()
+        cfg = self.transient_cfg()
+        t0 = time.perf_counter()
+        out = self.device.transient(cfg, X0, Q0, I0, maxc0)
+        wall = time.perf_counter() - t0
+        rc = self.rc
+        n = out["n_steps"]
+        voltages = {name: out["V"][:, idx] for name, idx in rc.node_names.items() if 0 < idx < rc.n_external}
+        currents = {name: out["I"][:, k] for k, name in enumerate(rc.vsrc_names)}
+        accepted = n - 1 if cfg["fixed_step"] else n
+        stats = dict(n_steps=n, total_timesteps=n, accepted_steps=accepted, rejected_steps=out["rejected"],
+                     total_nr_iterations=out["total_nr_iters"],
+                     avg_nr_iterations=out["total_nr_iters"] / max(accepted, 1), wall_time=wall,
+                     time_per_step_ms=wall / max(accepted, 1) * 1e3, device_ms=out["device_ms"],
+                     min_dt_used=out["min_dt_used"], max_dt_used=out["max_dt_used"],
+                     nr_failures=out["nr_failures"], dc_converged=dc_conv,
+                     strategy="fixed_step_full_mna" if cfg["fixed_step"] else "adaptive_full_mna",
+                     solver=f"gb300-sparse-{self.precision}", X0=X0)
+        return TransientResult(times=out["times"], voltages=voltages, currents=currents, stats=stats)
