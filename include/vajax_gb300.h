@@ -76,6 +76,21 @@ int vgb_circuit_set_sources(void* h, int is_current, int n, const int* kinds, co
  * convergence test (solver_factories.py:37-100, residual_conv_mask). */
 int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx);
 
+/* Host-only analysis: CSR pattern, stamp maps, gather lists, ordering and
+ * symbolic factorisation.  Touches no GPU; the pattern getters below work
+ * after this call.  finalize() runs it when it has not been run. */
+int vgb_circuit_analyze(void* h);
+/* Solver statistics after analysis, out[8] = {n_aug, nnz, nnz_lu, lu_flops,
+ * etree_height, max_factor_column, critical_path_steps, contribution_slots}. */
+int vgb_solver_info(void* h, int64_t* out);
+
+/* Per-phase device timing of the Newton loop (CUDA events on the handle's
+ * stream).  mode 1 enables and resets, 0 disables and resets, -1 only reads.
+ * out[7] (may be NULL) = {eval_ms, assemble_ms, factor_ms, solve_ms,
+ * update_ms, newton_iterations_timed, kernel_launches}.  No counterpart in
+ * the reference (it profiles through the JAX profiler). */
+int vgb_profile(void* h, int mode, double* out);
+
 /* Build the CSR pattern, stamp maps, gather lists and the sparse symbolic
  * factorisation; allocate device state.  precision: 0 = FP64 LU,
  * 1 = FP32 LU with FP64-residual iterative refinement (refine_sweeps <= 3).

@@ -74,10 +74,14 @@ def test_device_eval_matches_interpreter(cuda, name, make):
         gpu = {k: v.cpu().numpy() for k, v in dc.eval_group(gi, Xd).items()}
         rr, rq, jr, jq = S.eval_group(gi, X)
         for key, ref in (("res_resist", rr), ("res_react", rq), ("jac_resist", jr), ("jac_react", jq)):
-            # per-entry relative error, with a floor at 1e-12 of the column scale
-            col = np.maximum(np.max(np.abs(ref), axis=0, keepdims=True), 1e-300)
-            err = np.abs(gpu[key] - ref) / np.maximum(np.abs(ref), 1e-12 * col)
-            assert np.max(err) < REL, (name, gi, key, float(np.max(err)))
+            # allclose-style, as the reference's OSDI comparison (rtol 1e-10 plus an absolute
+            # floor): |gpu - ref| <= 1e-10 |ref| + 1e-13 max|column|.  The floor covers values
+            # that are the small residue of a cancellation, where fused multiply-adds on the
+            # GPU and separately rounded products in numpy differ in the last bits.
+            col = np.max(np.abs(ref), axis=0, keepdims=True)
+            bound = REL * np.abs(ref) + 1e-13 * col
+            excess = np.abs(gpu[key] - ref) - bound
+            assert np.all(excess <= 0), (name, gi, key, float(np.max(excess)))
 
 
 @pytest.mark.parametrize("name,make", CIRCUITS)
@@ -134,21 +138,22 @@ def test_newton_divider(cuda):
 
 
 @pytest.mark.parametrize("name,make", CIRCUITS[1:])
-def test_newton_dc_matches_oracle(cuda, name, make):
-    import torch
+def test_dc_operating_point_matches_oracle(cuda, name, make):
+    """Mid-rail start, plain Newton, then the gshunt / source-stepping homotopy."""
+    from oracle.dc import dc_operating_point
     from vajax_gb300.engine import CircuitEngine
     c = make()
     eng = CircuitEngine(c).parse()
     rc = eng.rc
-    _, dc, S = _pair(c)
+    eng.device = _pair(c)[1]
+    S = OracleSystem(rc, {g.model: load_model(g.model) for g in rc.groups})
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
     X0[: rc.n_nodes] = eng.init_mid_rail()
-    vs = rc.source_values(0.0)
-    r = dc.nr_solve(torch.as_tensor(X0.copy(), device=cuda), torch.as_tensor(vs, device=cuda), max_iter=20)
-    ro = nr_solve(S, X0.copy(), vs, max_iterations=20)
-    assert r["iterations"] == ro["iterations"]
-    assert r["converged"] == ro["converged"]
-    assert np.max(np.abs(r["X"].cpu().numpy()[: rc.n_nodes] - ro["X"][: rc.n_nodes])) < 1e-9
+    Xg, Qg, Ig, maxcg, ok = eng.initial_state()
+    ro = dc_operating_point(S, rc.source_values(0.0), X0)
+    assert ok and ro["converged"]
+    assert np.max(np.abs(Xg[: rc.n_nodes] - ro["X"][: rc.n_nodes])) < 1e-9
+    _close(Qg, ro["Q"], rel=1e-9)
 
 
 def _cfg(rc, fixed, t_stop, dt, max_steps, method=2):
@@ -189,7 +194,9 @@ def test_adaptive_network_matches_oracle(cuda):
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
     X0[: rc.n_nodes] = eng.init_mid_rail()
     vs = rc.source_values(0.0)
-    ro = nr_solve(S, X0.copy(), vs, max_iterations=20)
+    from oracle.dc import dc_operating_point
+    ro = dc_operating_point(S, vs, X0.copy())
+    assert ro["converged"]
     cfg = _cfg(rc, False, 2e-9, 0.25e-12, 61)
     cfg["max_dt"] = 2e-9 / 50
     o = run_transient(S, cfg, ro["X"], ro["Q"], ro["I_vsource"], ro["max_res_contrib"])

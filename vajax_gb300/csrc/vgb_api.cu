@@ -43,6 +43,10 @@ static void require_final(Circuit* c) {
     if (!c->finalized) throw Error(VGB_ERR_STATE, "circuit is not finalized");
 }
 
+static void require_analyzed(Circuit* c) {
+    if (!c->analyzed) throw Error(VGB_ERR_STATE, "circuit is not analyzed (call vgb_circuit_analyze)");
+}
+
 // ---------------------------------------------------------------------------
 // Core steps
 // ---------------------------------------------------------------------------
@@ -69,16 +73,35 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
     u.damping = o.damping;
     u.max_step = o.max_step;
     u.st = c.d_status.p;
+    const bool prof = c.profile;
     for (int it = 0; it < max_iter; ++it) {
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[0], s));
         launch_status_reset(c.d_status.p, s);
-        build_system(c, X, vs, is, Qp, dQp, Qp2, k, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p,
-                     c.d_maxc.p, c.d_fres.p, s);
+        eval_all(c, X, k.c0, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[1], s));
+        assemble(c, X, vs, is, Qp, dQp, Qp2, k, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p,
+                 c.d_maxc.p, c.d_fres.p, s);
         launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
-        linear_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[2], s));
+        const bool fp32 = c.solver_kind == 1;
+        lu_factor(c, c.d_csr_vals.p, fp32, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
+        lu_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, fp32, c.refine_sweeps, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[4], s));
         launch_nr_reduce(u, s);
         launch_nr_apply(u, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[5], s));
+        c.launches += 4 + solve_launches(c);  // status reset, negate, reduce, apply + solver kernels
         VGB_CUDA(cudaMemcpyAsync(c.h_status, c.d_status.p, sizeof(NRStatus), cudaMemcpyDeviceToHost, s));
         VGB_CUDA(cudaStreamSynchronize(s));
+        if (prof) {
+            for (int p = 0; p < 5; ++p) {
+                float ms = 0.f;
+                VGB_CUDA(cudaEventElapsedTime(&ms, c.ev[p], c.ev[p + 1]));
+                c.phase_ms[p] += ms;
+            }
+            c.phase_calls++;
+        }
         const NRStatus st = *c.h_status;
         r.iterations = it + 1;
         r.max_f = bits_to_double(st.max_f);
@@ -234,6 +257,56 @@ int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx) {
     });
 }
 
+int vgb_circuit_analyze(void* h) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        if (c->analyzed) return;
+        build_pattern(*c);
+        build_sparse_symbolic(*c);
+        c->analyzed = true;
+    });
+}
+
+int vgb_solver_info(void* h, int64_t* out) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(c->analyzed, "circuit is not analyzed");
+        const SparseLU& L = c->lu;
+        out[0] = c->n_aug;
+        out[1] = c->nnz;
+        out[2] = L.nnz_lu;
+        out[3] = L.flops;
+        out[4] = L.etree_height;
+        out[5] = L.max_col;
+        out[6] = L.crit_path;
+        out[7] = c->n_contrib;
+    });
+}
+
+int vgb_profile(void* h, int mode, double* out) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        if (out) {
+            for (int p = 0; p < 5; ++p) out[p] = c->phase_ms[p];
+            out[5] = (double)c->phase_calls;
+            out[6] = (double)c->launches;
+        }
+        if (mode == 1 || mode == 0) {
+            if (mode == 1 && !c->ev[0])
+                for (auto& e : c->ev) VGB_CUDA(cudaEventCreate(&e));
+            c->profile = mode == 1;
+        }
+        if (mode >= 0) {  // any explicit mode resets the counters
+            for (double& v : c->phase_ms) v = 0.0;
+            c->phase_calls = 0;
+            c->launches = 0;
+        }
+    });
+}
+
 int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
@@ -244,9 +317,16 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->gmin = gmin;
         c->solver_kind = precision;
         c->refine_sweeps = refine_sweeps;
-        build_pattern(*c);
-        build_sparse_symbolic(*c);
+        if (!c->analyzed) {
+            build_pattern(*c);
+            build_sparse_symbolic(*c);
+            c->analyzed = true;
+        }
         VGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->d_zeros.alloc(std::max({c->n_unk, c->n_vsrc, c->n_isrc, 1}));
+        c->d_zeros.zero(c->stream);
+        c->d_floor.alloc(std::max(c->n_unk, 1));
+        c->floor_value = -1.0;
         VGB_CUDA(cudaHostAlloc((void**)&c->h_status, sizeof(NRStatus), cudaHostAllocDefault));
         for (auto& g : c->groups) {
             g.d_node_map.upload(g.node_map);
@@ -269,6 +349,8 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->d_vsrc_p.upload(c->vsrc_p);
         c->d_vsrc_n.upload(c->vsrc_n);
         c->d_conv_mask.upload(c->conv_mask);
+        c->d_heavy_csr.upload(c->heavy_csr.empty() ? std::vector<int>{0} : c->heavy_csr);
+        c->d_heavy_row.upload(c->heavy_row.empty() ? std::vector<int>{0} : c->heavy_row);
         c->d_indptr.upload(c->indptr);
         c->d_indices.upload(c->indices);
         c->d_contrib.alloc(std::max<long long>(c->n_contrib, 1));
@@ -293,13 +375,27 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         L.d_urow_ptr.upload(L.urow_ptr);
         L.d_urow_pos.upload(L.urow_pos.empty() ? std::vector<long long>{0} : L.urow_pos);
         L.d_urow_col.upload(L.urow_col.empty() ? std::vector<int>{0} : L.urow_col);
-        std::vector<int> brow(L.n);
-        for (int i = 0; i < L.n; ++i) brow[i] = L.perm_r[L.q[i]];
+        L.d_ukl.upload(L.ukl);
+        std::vector<int> brow(std::max(L.nM, 1), 0);
+        for (int i = 0; i < L.nM; ++i) brow[i] = L.perm_r[L.q[i]];
         L.d_brow.upload(brow);
-        L.d_q.upload(L.q);
+        L.d_q.upload(L.q.empty() ? std::vector<int>{0} : L.q);
+        auto up = [](DevBuf<int>& d, const std::vector<int>& h) { d.upload(h.empty() ? std::vector<int>{0} : h); };
+        up(L.d_f_col, L.f_col);
+        up(L.d_f_arow, L.f_arow);
+        up(L.d_f_diag_e, L.f_diag_e);
+        up(L.d_l_col, L.l_col);
+        up(L.d_l_arow, L.l_arow);
+        up(L.d_l_diag_e, L.l_diag_e);
+        up(L.d_l_ptr, L.l_ptr);
+        up(L.d_l_e, L.l_e);
+        up(L.d_l_x, L.l_x);
+        up(L.d_pre_ptr, L.pre_ptr);
+        up(L.d_pre_e, L.pre_e);
+        up(L.d_pre_f, L.pre_f);
         if (precision == 1) L.d_vals32.alloc(std::max<long long>(L.nnz_lu, 1));
         else L.d_vals64.alloc(std::max<long long>(L.nnz_lu, 1));
-        L.d_done.alloc(3 * (size_t)std::max(L.n, 1));
+        L.d_done.alloc(3 * (size_t)std::max(L.nM, 1));
         L.d_done.zero(c->stream);
         L.d_counters.alloc(4);
         const size_t na = std::max(c->n_aug, 1), nu = std::max(c->n_unk, 1);
@@ -307,8 +403,8 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->d_f.alloc(na);
         c->d_delta.alloc(na);
         c->d_rhs.alloc(na);
-        c->d_work.alloc(na);
-        c->d_work2.alloc(2 * na);
+        c->d_work.alloc(3 * na);   // block right-hand side, forward and backward vectors
+        c->d_work2.alloc(2 * na);  // refinement residual and correction
         c->d_Q.alloc(nu);
         c->d_maxc.alloc(nu);
         c->d_fres.alloc(nu);
@@ -323,7 +419,7 @@ int vgb_pattern_info(void* h, int* n_aug, int* nnz, int64_t* nnz_lu, int64_t* lu
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
-        require_final(c);
+        require_analyzed(c);
         if (n_aug) *n_aug = c->n_aug;
         if (nnz) *nnz = c->nnz;
         if (nnz_lu) *nnz_lu = c->lu.nnz_lu;
@@ -335,7 +431,7 @@ int vgb_pattern_csr(void* h, int* indptr, int* indices) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
-        require_final(c);
+        require_analyzed(c);
         std::memcpy(indptr, c->indptr.data(), c->indptr.size() * sizeof(int));
         std::memcpy(indices, c->indices.data(), c->indices.size() * sizeof(int));
     });
@@ -345,7 +441,7 @@ int vgb_stamp_positions(void* h, int group, int* out) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
-        require_final(c);
+        require_analyzed(c);
         VGB_REQUIRE(group >= 0 && group < (int)c->groups.size(), "group out of range");
         const auto& p = c->groups[group].csr_pos;
         std::memcpy(out, p.data(), p.size() * sizeof(int));
@@ -356,7 +452,7 @@ int vgb_special_positions(void* h, int* diag, int* vsrc) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
-        require_final(c);
+        require_analyzed(c);
         if (diag) std::memcpy(diag, c->diag_pos.data(), c->diag_pos.size() * sizeof(int));
         if (vsrc)
             for (int q = 0; q < 4; ++q)
@@ -370,27 +466,15 @@ namespace vgb {
 
 
 
-DefaultVecs& defaults_for(Circuit& c, double abstol, cudaStream_t s) {
-    static thread_local std::vector<std::pair<Circuit*, DefaultVecs*>> cache;
-    for (auto& e : cache)
-        if (e.first == &c) {
-            if (e.second->floor_value != abstol) {
-                std::vector<double> fl(std::max(c.n_unk, 1), abstol);
-                e.second->floor_abstol.upload(fl);
-                e.second->floor_value = abstol;
-            }
-            return *e.second;
-        }
-    auto* d = new DefaultVecs();
-    const size_t m = std::max({c.n_unk, c.n_vsrc, c.n_isrc, 1});
-    d->zeros.alloc(m);
-    d->zeros.zero(s);
-    std::vector<double> fl(std::max(c.n_unk, 1), abstol);
-    d->floor_abstol.upload(fl);
-    d->floor_value = abstol;
-    VGB_CUDA(cudaStreamSynchronize(s));
-    cache.push_back({&c, d});
-    return *d;
+// Zero vector and abstol floor owned by the circuit (sized for it, allocated at finalize).
+DefaultVecs defaults_for(Circuit& c, double abstol, cudaStream_t s) {
+    if (c.floor_value != abstol) {
+        std::vector<double> fl(std::max(c.n_unk, 1), abstol);
+        VGB_CUDA(cudaMemcpyAsync(c.d_floor.p, fl.data(), fl.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        c.floor_value = abstol;
+    }
+    return DefaultVecs{c.d_zeros.p, c.d_floor.p};
 }
 
 } // namespace vgb
@@ -405,17 +489,17 @@ int vgb_build_system(void* h, const double* X, const double* vsrc_vals, const do
         c = as_circuit(h);
         require_final(c);
         cudaStream_t s = pick(c, stream);
-        DefaultVecs& dv = defaults_for(*c, 1e-12, s);
+        DefaultVecs dv = defaults_for(*c, 1e-12, s);
         Coeffs k;
         k.c0 = coeffs[0];
         k.c1 = coeffs[1];
         k.d1 = coeffs[2];
         k.c2 = coeffs[3];
         k.gshunt = coeffs[4];
-        const double* z = dv.zeros.p;
+        const double* z = dv.zeros;
         launch_status_reset(c->d_status.p, s);
         build_system(*c, X, vsrc_vals ? vsrc_vals : z, isrc_vals ? isrc_vals : z, Q_prev ? Q_prev : z,
-                     dQdt_prev ? dQdt_prev : z, Q_prev2 ? Q_prev2 : z, k, dv.floor_abstol.p, 1e-3, 1e-6,
+                     dQdt_prev ? dQdt_prev : z, Q_prev2 ? Q_prev2 : z, k, dv.floor_abstol, 1e-3, 1e-6,
                      csr_vals ? csr_vals : c->d_csr_vals.p, f ? f : c->d_f.p, Q ? Q : c->d_Q.p,
                      maxc ? maxc : c->d_maxc.p, fres ? fres : c->d_fres.p, s);
         VGB_CUDA(cudaGetLastError());
@@ -470,19 +554,19 @@ int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc
         o.vntol = opts[7];
         o.damping = opts[8];
         o.max_step = opts[9];
-        DefaultVecs& dv = defaults_for(*c, o.abstol, s);
-        const double* z = dv.zeros.p;
+        DefaultVecs dv = defaults_for(*c, o.abstol, s);
+        const double* z = dv.zeros;
         const double* vs = vsrc_vals ? vsrc_vals : z;
         const double* is = isrc_vals ? isrc_vals : z;
         const double* Qp = Q_prev ? Q_prev : z;
         const double* dQp = dQdt_prev ? dQdt_prev : z;
         const double* Qp2 = Q_prev2 ? Q_prev2 : z;
         VGB_CUDA(cudaMemsetAsync(&c->d_status.p->dev_err, 0, sizeof(int), s));
-        NRResult r = nr_loop(*c, X, vs, is, Qp, dQp, Qp2, res_tol_floor ? res_tol_floor : dv.floor_abstol.p, k, o,
+        NRResult r = nr_loop(*c, X, vs, is, Qp, dQp, Qp2, res_tol_floor ? res_tol_floor : dv.floor_abstol, k, o,
                              max_iter, s);
         // post-convergence rebuild for Q, I_vsource, max_res_contrib (solver_factories.py:689-713)
         launch_status_reset(c->d_status.p, s);
-        build_system(*c, X, vs, is, Qp, dQp, Qp2, k, dv.floor_abstol.p, o.reltol, o.vntol, c->d_csr_vals.p,
+        build_system(*c, X, vs, is, Qp, dQp, Qp2, k, dv.floor_abstol, o.reltol, o.vntol, c->d_csr_vals.p,
                      c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
         if (Q_out) VGB_CUDA(cudaMemcpyAsync(Q_out, c->d_Q.p, c->n_unk * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if (maxc_out)

@@ -10,6 +10,9 @@
 
 namespace vgb {
 
+// Gather lists longer than this are reduced by a whole block instead of one thread.
+constexpr int HEAVY_LIST = 64;
+
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -80,10 +83,17 @@ struct Sources {
 
 // Static-pivot sparse LU structures (host symbolic + device numeric).
 struct SparseLU {
-    int n = 0;
+    int n = 0;                   // n_aug
+    int nM = 0;                  // size of the factorised block M
     std::vector<int> perm_r;     // row r of B = row perm_r[r] of A (vsource transversal)
-    std::vector<int> q;          // column/row order: C = Q^T B Q, C(i,j) = B(q[i], q[j])
-    std::vector<int> qinv;
+    std::vector<int> q;          // [nM] block order: C = Q^T B_MM Q, C(i,j) = B(q[i], q[j])
+    std::vector<int> qinv;       // [n] B index -> position in M, -1 outside M
+    // singletons solved before M (row = diagonal only) and after M (column = diagonal only)
+    std::vector<int> f_col, f_arow, f_diag_e;          // B index, A row, A slot of the diagonal
+    std::vector<int> l_col, l_arow, l_diag_e;          // B index, A row, A slot of the diagonal
+    std::vector<int> l_ptr, l_e, l_x;                  // off-diagonal row entries: A slot, x index
+    std::vector<int> pre_ptr, pre_e, pre_f;            // per M row: A slot and F index of couplings
+    std::vector<long long> ukl;                        // per U slot: first L slot of the source column
     // factor storage, column-major with U part, diagonal, then L part per column
     std::vector<long long> col_ptr;   // [n+1]
     std::vector<int> nU;              // [n] entries above diagonal
@@ -102,9 +112,14 @@ struct SparseLU {
     std::vector<long long> urow_pos;  // positions of U(i,j), j > i
     std::vector<int> urow_col;        // j of each
     long long nnz_lu = 0, flops = 0;
+    long long etree_height = 0;   // levels of the elimination tree
+    long long max_col = 0;        // longest factor column (entries)
+    long long crit_path = 0;      // longest dependency chain, in sequential column steps
     // device
-    DevBuf<long long> d_col_ptr, d_ustart, d_umap_ptr, d_lrow_ptr, d_lrow_pos, d_urow_ptr, d_urow_pos;
-    DevBuf<int> d_nU, d_rows, d_f2a, d_umap, d_lrow_col, d_urow_col, d_brow;  // brow: B-row source of permuted row
+    DevBuf<long long> d_col_ptr, d_ustart, d_umap_ptr, d_lrow_ptr, d_lrow_pos, d_urow_ptr, d_urow_pos, d_ukl;
+    DevBuf<int> d_nU, d_rows, d_f2a, d_umap, d_lrow_col, d_urow_col, d_brow;  // brow: A row of permuted M row
+    DevBuf<int> d_f_col, d_f_arow, d_f_diag_e, d_l_col, d_l_arow, d_l_diag_e, d_l_ptr, d_l_e, d_l_x;
+    DevBuf<int> d_pre_ptr, d_pre_e, d_pre_f;
     DevBuf<int> d_q;
     DevBuf<double> d_vals64;
     DevBuf<float> d_vals32;
@@ -151,6 +166,8 @@ struct Circuit {
     std::vector<int> nb_ptr, nb_idx;   // node row -> vsource branch incidence (signed index: +k+1 / -(k+1))
     std::vector<int> ni_ptr, ni_idx;   // node row -> isource incidence (signed)
     std::vector<unsigned char> conv_mask;  // [n_aug] 1 = checked in the residual test
+    std::vector<int> heavy_csr, heavy_row; // items whose gather list is longer than HEAVY_LIST
+    DevBuf<int> d_heavy_csr, d_heavy_row;
     long long n_contrib = 0;
 
     DevBuf<int> d_csr_src_ptr, d_csr_src, d_res_src_ptr, d_res_src, d_rq_src;
@@ -165,8 +182,17 @@ struct Circuit {
     // work vectors (device)
     DevBuf<double> d_csr_vals, d_f, d_delta, d_Q, d_maxc, d_fres, d_rhs, d_work, d_work2;
     DevBuf<NRStatus> d_status;
-    NRStatus* h_status = nullptr;   // pinned, mapped
+    NRStatus* h_status = nullptr;   // pinned
     cudaStream_t stream = nullptr;
+    // per-phase device time (CUDA events on the circuit stream), enabled by vgb_profile_enable
+    bool profile = false;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double phase_ms[5] = {0, 0, 0, 0, 0};   // eval, assemble, factor, solve, update
+    long long phase_calls = 0;
+    long long launches = 0;                  // kernels launched by this handle
+    DevBuf<double> d_zeros, d_floor;  // defaults for omitted "previous state" vectors
+    double floor_value = -1.0;
+    bool analyzed = false;            // host-side pattern + symbolic built
 
     ~Circuit();
 };

@@ -10,8 +10,26 @@ struct Coeffs {
 };
 
 inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
-    for (auto& g : c.groups) g.me->launch(g.args(c.d_contrib.p), X, c0, s);
+    for (auto& g : c.groups)
+        if (g.n_dev) {
+            g.me->launch(g.args(c.d_contrib.p), X, c0, s);
+            c.launches++;
+        }
 }
+
+// Kernel launches of one linear solve (factor + triangular solves + refinement).
+inline long long solve_launches(const Circuit& c) {
+    const SparseLU& L = c.lu;
+    long long once = (L.nM + (long long)L.f_col.size() ? 1 : 0) + (L.nM ? 2 : 0) + (L.l_col.empty() ? 0 : 1);
+    long long n = (L.nM ? 1 : 0) + once;
+    if (c.solver_kind == 1) n += (long long)c.refine_sweeps * (once + 2);
+    return n;
+}
+
+inline void assemble(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
+                     const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
+                     double reltol, double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
+                     cudaStream_t s);
 
 // build_system: eval + assemble (+ residual check into d_status)
 inline void build_system(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
@@ -19,6 +37,14 @@ inline void build_system(Circuit& c, const double* X, const double* vs, const do
                          double reltol, double vntol, double* csr, double* f, double* Q, double* maxc,
                          double* fres, cudaStream_t s) {
     eval_all(c, X, k.c0, s);
+    assemble(c, X, vs, is, Qp, dQp, Qp2, k, res_tol_floor, reltol, vntol, csr, f, Q, maxc, fres, s);
+}
+
+inline void assemble(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
+                     const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
+                     double reltol, double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
+                     cudaStream_t s) {
+    c.launches += 1 + ((c.heavy_csr.size() + c.heavy_row.size()) ? 1 : 0);
     AssembleArgs a{};
     a.nnz = c.nnz;
     a.n_unk = c.n_unk;
@@ -59,6 +85,10 @@ inline void build_system(Circuit& c, const double* X, const double* vs, const do
     a.maxc = maxc;
     a.fres = fres;
     a.st = c.d_status.p;
+    a.heavy_csr = c.d_heavy_csr.p;
+    a.n_heavy_csr = (int)c.heavy_csr.size();
+    a.heavy_row = c.d_heavy_row.p;
+    a.n_heavy_row = (int)c.heavy_row.size();
     launch_assemble(a, s);
 }
 
@@ -81,13 +111,13 @@ struct NRResult {
 };
 
 struct DefaultVecs {
-    DevBuf<double> zeros, floor_abstol;
-    double floor_value = -1;
+    const double* zeros;          // [max(n_unk, n_vsrc, n_isrc)] zeros
+    const double* floor_abstol;   // [n_unk] residual tolerance floor = abstol
 };
 
 NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
                  const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
                  const NROpts& o, int max_iter, cudaStream_t s);
-DefaultVecs& defaults_for(Circuit& c, double abstol, cudaStream_t s);
+DefaultVecs defaults_for(Circuit& c, double abstol, cudaStream_t s);
 
 } // namespace vgb

@@ -44,8 +44,12 @@ struct ParamReader {
     }
 };
 
+// Device evaluation is FP64-pipe bound: small blocks spread the instances over
+// every SM instead of packing them onto a few.
+constexpr int EVAL_BLOCK = 64;
+
 template <class M>
-__global__ void __launch_bounds__(128) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
+__global__ void __launch_bounds__(EVAL_BLOCK) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n_dev) return;
@@ -106,7 +110,7 @@ template <class M>
 void launch_eval(const GroupArgs& g, const double* X, double c0, cudaStream_t s)
 {
     if (g.n_dev == 0) return;
-    eval_kernel<M><<<ceil_div(g.n_dev, 128), 128, 0, s>>>(g, X, c0);
+    eval_kernel<M><<<ceil_div(g.n_dev, EVAL_BLOCK), EVAL_BLOCK, 0, s>>>(g, X, c0);
 }
 
 template <class M>

@@ -160,6 +160,14 @@ void build_pattern(Circuit& c) {
     c.conv_mask.assign(n_aug, 1);
     for (int idx : c.internal_idx)
         if (idx > 0 && idx - 1 < n_unk) c.conv_mask[idx - 1] = 0;
+
+    // long gather lists (supply rails) are reduced by a block each
+    c.heavy_csr.clear();
+    c.heavy_row.clear();
+    for (int e = 0; e < c.nnz; ++e)
+        if (c.csr_src_ptr[e + 1] - c.csr_src_ptr[e] > HEAVY_LIST) c.heavy_csr.push_back(e);
+    for (int r = 0; r < n_unk; ++r)
+        if (c.res_src_ptr[r + 1] - c.res_src_ptr[r] > HEAVY_LIST) c.heavy_row.push_back(r);
 }
 
 // ---------------------------------------------------------------------------
@@ -231,44 +239,113 @@ void build_sparse_symbolic(Circuit& c) {
     std::vector<int> pinv_r(n);
     for (int r = 0; r < n; ++r) pinv_r[L.perm_r[r]] = r;
 
-    // 2. symmetric pattern of B = P_r A
-    std::vector<std::vector<int>> adj(n);
+    // 2. block-triangular singletons of B = P_r A.  A row whose only entry is
+    //    its diagonal (a node pinned by a grounded voltage source) is solved
+    //    first; a column whose only entry is its diagonal (that source's
+    //    branch current) is solved last from its row.  Neither enters the
+    //    factorised block M, which keeps the dense supply-rail row and column
+    //    out of the elimination.
+    std::vector<int> rowcnt(n, 0), colcnt(n, 0);
+    std::vector<char> rowdiag(n, 0), coldiag(n, 0);
     for (int ra = 0; ra < n; ++ra) {
-        int r = pinv_r[ra];
+        const int r = pinv_r[ra];
         for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
-            int col = c.indices[e];
-            if (col == r) continue;
-            adj[r].push_back(col);
-            adj[col].push_back(r);
+            const int col = c.indices[e];
+            rowcnt[r]++;
+            colcnt[col]++;
+            if (col == r) { rowdiag[r] = 1; coldiag[col] = 1; }
+        }
+    }
+    std::vector<int> kind(n, 0);  // 0 = M, 1 = F (first), 2 = L (last)
+    for (int i = 0; i < n; ++i) {
+        if (rowcnt[i] == 1 && rowdiag[i]) kind[i] = 1;
+        else if (colcnt[i] == 1 && coldiag[i]) kind[i] = 2;
+    }
+    L.f_col.clear(); L.f_arow.clear(); L.f_diag_e.clear();
+    L.l_col.clear(); L.l_arow.clear(); L.l_diag_e.clear();
+    std::vector<int> fidx(n, -1);
+    for (int i = 0; i < n; ++i) {
+        if (kind[i] == 1) {
+            fidx[i] = (int)L.f_col.size();
+            L.f_col.push_back(i);
+            L.f_arow.push_back(L.perm_r[i]);
+        } else if (kind[i] == 2) {
+            L.l_col.push_back(i);
+            L.l_arow.push_back(L.perm_r[i]);
+        }
+    }
+    auto diag_slot = [&](int i) {
+        const int ra = L.perm_r[i];
+        for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e)
+            if (c.indices[e] == i) return e;
+        return -1;
+    };
+    for (int i : L.f_col) L.f_diag_e.push_back(diag_slot(i));
+    L.l_ptr.assign(L.l_col.size() + 1, 0);
+    L.l_e.clear();
+    L.l_x.clear();
+    for (size_t t = 0; t < L.l_col.size(); ++t) {
+        const int i = L.l_col[t];
+        const int ra = L.perm_r[i];
+        L.l_diag_e.push_back(diag_slot(i));
+        for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
+            if (c.indices[e] == i) continue;
+            L.l_e.push_back(e);
+            L.l_x.push_back(c.indices[e]);
+        }
+        L.l_ptr[t + 1] = (int)L.l_e.size();
+    }
+
+    // 3. symmetric pattern of the block M
+    std::vector<int> mlist;
+    for (int i = 0; i < n; ++i)
+        if (kind[i] == 0) mlist.push_back(i);
+    const int nM = (int)mlist.size();
+    L.nM = nM;
+    std::vector<int> mloc(n, -1);
+    for (int t = 0; t < nM; ++t) mloc[mlist[t]] = t;
+    std::vector<std::vector<int>> adj(nM);
+    for (int ra = 0; ra < n; ++ra) {
+        const int r = pinv_r[ra];
+        if (kind[r] != 0) continue;
+        for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
+            const int col = c.indices[e];
+            if (col == r || kind[col] != 0) continue;
+            adj[mloc[r]].push_back(mloc[col]);
+            adj[mloc[col]].push_back(mloc[r]);
         }
     }
     for (auto& a : adj) { std::sort(a.begin(), a.end()); a.erase(std::unique(a.begin(), a.end()), a.end()); }
 
-    // 3. fill-reducing order
-    L.q = min_degree_order(n, adj);
-    L.qinv.resize(n);
-    for (int i = 0; i < n; ++i) L.qinv[L.q[i]] = i;
+    // 4. fill-reducing order of M
+    std::vector<int> qm = min_degree_order(nM, adj);
+    L.q.resize(nM);
+    L.qinv.assign(n, -1);
+    for (int i = 0; i < nM; ++i) {
+        L.q[i] = mlist[qm[i]];
+        L.qinv[L.q[i]] = i;
+    }
 
-    // 4. elimination tree and row structure of L on the permuted pattern
-    std::vector<std::vector<int>> low(n);  // permuted neighbours below the diagonal
-    for (int v = 0; v < n; ++v) {
-        int i = L.qinv[v];
+    // 5. elimination tree and row structure of L on the permuted pattern
+    std::vector<std::vector<int>> low(nM);
+    for (int v = 0; v < nM; ++v) {
+        const int i = L.qinv[mlist[v]];
         for (int u : adj[v]) {
-            int k = L.qinv[u];
+            const int k = L.qinv[mlist[u]];
             if (k < i) low[i].push_back(k);
         }
     }
-    std::vector<int> parent(n, -1), ancestor(n, -1);
-    for (int i = 0; i < n; ++i) {
+    std::vector<int> parent(nM, -1), ancestor(nM, -1);
+    for (int i = 0; i < nM; ++i) {
         for (int k : low[i]) {
             int r = k;
             while (ancestor[r] != -1 && ancestor[r] != i) { int t = ancestor[r]; ancestor[r] = i; r = t; }
             if (ancestor[r] == -1) { ancestor[r] = i; parent[r] = i; }
         }
     }
-    std::vector<std::vector<int>> rowstruct(n);
-    std::vector<int> mark(n, -1);
-    for (int i = 0; i < n; ++i) {
+    std::vector<std::vector<int>> rowstruct(nM);
+    std::vector<int> mark(nM, -1);
+    for (int i = 0; i < nM; ++i) {
         mark[i] = i;
         auto& rs = rowstruct[i];
         for (int k : low[i]) {
@@ -277,20 +354,20 @@ void build_sparse_symbolic(Circuit& c) {
         }
         std::sort(rs.begin(), rs.end());
     }
-    std::vector<std::vector<int>> lcol(n);
-    for (int i = 0; i < n; ++i)
-        for (int k : rowstruct[i]) lcol[k].push_back(i);  // ascending i
+    std::vector<std::vector<int>> lcol(nM);
+    for (int i = 0; i < nM; ++i)
+        for (int k : rowstruct[i]) lcol[k].push_back(i);
 
-    // 5. column storage: [U rows asc][diag][L rows asc]
-    L.col_ptr.assign(n + 1, 0);
-    L.nU.resize(n);
-    for (int j = 0; j < n; ++j) {
+    // 6. column storage: [U rows asc][diag][L rows asc]
+    L.col_ptr.assign(nM + 1, 0);
+    L.nU.resize(nM);
+    for (int j = 0; j < nM; ++j) {
         L.nU[j] = (int)rowstruct[j].size();
         L.col_ptr[j + 1] = L.col_ptr[j] + rowstruct[j].size() + 1 + lcol[j].size();
     }
-    L.nnz_lu = L.col_ptr[n];
+    L.nnz_lu = L.col_ptr[nM];
     L.rows.resize(L.nnz_lu);
-    for (int j = 0; j < n; ++j) {
+    for (int j = 0; j < nM; ++j) {
         long long s = L.col_ptr[j];
         for (int r : rowstruct[j]) L.rows[s++] = r;
         L.rows[s++] = j;
@@ -308,30 +385,48 @@ void build_sparse_symbolic(Circuit& c) {
         auto it = std::lower_bound(b, e, i);
         return (it != e && *it == i) ? (long long)(it - L.rows.begin()) : -1;
     };
-    // 6. A -> factor slot
+    // 7. A -> factor slot (M x M entries) and the F couplings of each M row
     L.f2a.assign(L.nnz_lu, -1);
+    L.pre_ptr.assign(nM + 1, 0);
+    std::vector<std::vector<std::pair<int, int>>> pre(nM);
     for (int ra = 0; ra < n; ++ra) {
-        int i = L.qinv[pinv_r[ra]];
+        const int r = pinv_r[ra];
+        if (kind[r] != 0) continue;
+        const int i = L.qinv[r];
         for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
-            int j = L.qinv[c.indices[e]];
-            long long s = slot_of(i, j);
-            VGB_REQUIRE(s >= 0, "symbolic factor misses an entry of A");
-            L.f2a[s] = e;
+            const int col = c.indices[e];
+            if (kind[col] == 0) {
+                long long s = slot_of(i, L.qinv[col]);
+                VGB_REQUIRE(s >= 0, "symbolic factor misses an entry of A");
+                L.f2a[s] = e;
+            } else if (kind[col] == 1) {
+                pre[i].push_back({e, fidx[col]});
+            } else {
+                VGB_REQUIRE(false, "a trivial column has an off-diagonal entry");
+            }
         }
     }
-    // 7. left-looking update maps
-    L.ustart.assign(n + 1, 0);
-    for (int j = 0; j < n; ++j) L.ustart[j + 1] = L.ustart[j] + L.nU[j];
-    long long nUtot = L.ustart[n];
+    L.pre_e.clear();
+    L.pre_f.clear();
+    for (int i = 0; i < nM; ++i) {
+        for (auto& pe : pre[i]) { L.pre_e.push_back(pe.first); L.pre_f.push_back(pe.second); }
+        L.pre_ptr[i + 1] = (int)L.pre_e.size();
+    }
+    // 8. left-looking update maps
+    L.ustart.assign(nM + 1, 0);
+    for (int j = 0; j < nM; ++j) L.ustart[j + 1] = L.ustart[j] + L.nU[j];
+    const long long nUtot = L.ustart[nM];
     L.umap_ptr.assign(nUtot + 1, 0);
+    L.ukl.assign(std::max<long long>(nUtot, 1), 0);
     L.umap.clear();
-    std::vector<int> lookup(n, -1);
+    std::vector<int> lookup(nM, -1);
     long long u = 0;
-    for (int j = 0; j < n; ++j) {
+    for (int j = 0; j < nM; ++j) {
         long long s0 = L.col_ptr[j], s1 = L.col_ptr[j + 1];
         for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = (int)(s - s0);
         for (int t = 0; t < L.nU[j]; ++t, ++u) {
             int k = rowstruct[j][t];
+            L.ukl[u] = L.col_ptr[k] + L.nU[k] + 1;
             for (int i : lcol[k]) {
                 int pos = lookup[i];
                 VGB_REQUIRE(pos >= 0, "fill pattern is not closed under elimination");
@@ -342,21 +437,36 @@ void build_sparse_symbolic(Circuit& c) {
         for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = -1;
     }
     L.flops = 2 * (long long)L.umap.size();
-    // 8. row access for the triangular solves
-    L.lrow_ptr.assign(n + 1, 0);
+    {
+        std::vector<long long> h(nM, 1), cp(nM, 0);
+        L.etree_height = nM ? 1 : 0;
+        L.max_col = 0;
+        L.crit_path = 0;
+        for (int j = 0; j < nM; ++j) {
+            long long best = 0;
+            for (int k : rowstruct[j]) best = std::max(best, cp[k]);
+            cp[j] = best + L.nU[j] + 1;
+            L.crit_path = std::max(L.crit_path, cp[j]);
+            L.max_col = std::max(L.max_col, L.col_ptr[j + 1] - L.col_ptr[j]);
+            if (parent[j] >= 0) h[parent[j]] = std::max(h[parent[j]], h[j] + 1);
+            L.etree_height = std::max(L.etree_height, h[j]);
+        }
+    }
+    // 9. row access for the triangular solves
+    L.lrow_ptr.assign(nM + 1, 0);
     L.lrow_pos.clear();
     L.lrow_col.clear();
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < nM; ++i) {
         for (int k : rowstruct[i]) {
             L.lrow_pos.push_back(slot_of(i, k));
             L.lrow_col.push_back(k);
         }
         L.lrow_ptr[i + 1] = (long long)L.lrow_pos.size();
     }
-    L.urow_ptr.assign(n + 1, 0);
+    L.urow_ptr.assign(nM + 1, 0);
     L.urow_pos.clear();
     L.urow_col.clear();
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < nM; ++i) {
         for (int j : lcol[i]) {
             L.urow_pos.push_back(slot_of(i, j));
             L.urow_col.push_back(j);

@@ -42,31 +42,11 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* abort
 // solver_factories.py:271-281 (VACASK-style residual check).
 // ---------------------------------------------------------------------------
 
-__global__ void assemble_kernel(AssembleArgs a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n_aug = a.n_unk + a.n_vsrc;
-    if (t < a.nnz) {
-        double s = 0.0;
-        const int e0 = a.csr_src_ptr[t], e1 = a.csr_src_ptr[t + 1];
-        for (int e = e0; e < e1; ++e) s += a.contrib[a.csr_src[e]];
-        if (a.csr_diag[t]) s += a.gdiag;
-        s += a.csr_const[t];
-        a.csr_vals[t] = s;
-        return;
-    }
-    const int r = t - a.nnz;
-    if (r >= n_aug) return;
+// Finish one node row or branch row from its gathered sums (shared by both assembly kernels).
+__device__ __forceinline__ void finish_row(const AssembleArgs& a, int r, double fr, double q, double mc) {
     double fn;
     double tol;
     if (r < a.n_unk) {
-        double fr = 0.0, q = 0.0, mc = 0.0;
-        const int e0 = a.res_src_ptr[r], e1 = a.res_src_ptr[r + 1];
-        for (int e = e0; e < e1; ++e) {
-            double v = nan0(a.contrib[a.res_src[e]]);
-            fr += v;
-            mc = fmax(mc, fabs(v));
-            q += nan0(a.contrib[a.rq_src[e]]);
-        }
         for (int e = a.ni_ptr[r]; e < a.ni_ptr[r + 1]; ++e) {
             int k = a.ni_idx[e];
             double v = k > 0 ? a.isrc_vals[k - 1] : -a.isrc_vals[-k - 1];
@@ -98,10 +78,85 @@ __global__ void assemble_kernel(AssembleArgs a) {
     }
 }
 
+// One thread per CSR entry / row with a short gather list.  Entries whose
+// list is long (the supply rails collect one term per connected device) are
+// skipped here and summed by assemble_heavy_kernel with a whole block each.
+__global__ void assemble_kernel(AssembleArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_aug = a.n_unk + a.n_vsrc;
+    if (t < a.nnz) {
+        const int e0 = a.csr_src_ptr[t], e1 = a.csr_src_ptr[t + 1];
+        if (e1 - e0 > HEAVY_LIST) return;
+        double s = 0.0;
+        for (int e = e0; e < e1; ++e) s += a.contrib[a.csr_src[e]];
+        if (a.csr_diag[t]) s += a.gdiag;
+        s += a.csr_const[t];
+        a.csr_vals[t] = s;
+        return;
+    }
+    const int r = t - a.nnz;
+    if (r >= n_aug) return;
+    double fr = 0.0, q = 0.0, mc = 0.0;
+    if (r < a.n_unk) {
+        const int e0 = a.res_src_ptr[r], e1 = a.res_src_ptr[r + 1];
+        if (e1 - e0 > HEAVY_LIST) return;
+        for (int e = e0; e < e1; ++e) {
+            double v = nan0(a.contrib[a.res_src[e]]);
+            fr += v;
+            mc = fmax(mc, fabs(v));
+            q += nan0(a.contrib[a.rq_src[e]]);
+        }
+    }
+    finish_row(a, r, fr, q, mc);
+}
+
+// One block per heavy CSR entry or heavy node row; fixed-order block reduction.
+__global__ void __launch_bounds__(256) assemble_heavy_kernel(AssembleArgs a) {
+    __shared__ double s_sum[256], s_q[256], s_max[256];
+    const int b = blockIdx.x;
+    const bool is_csr = b < a.n_heavy_csr;
+    const int item = is_csr ? a.heavy_csr[b] : a.heavy_row[b - a.n_heavy_csr];
+    const int e0 = is_csr ? a.csr_src_ptr[item] : a.res_src_ptr[item];
+    const int e1 = is_csr ? a.csr_src_ptr[item + 1] : a.res_src_ptr[item + 1];
+    double s = 0.0, q = 0.0, m = 0.0;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        if (is_csr) {
+            s += a.contrib[a.csr_src[e]];
+        } else {
+            double v = nan0(a.contrib[a.res_src[e]]);
+            s += v;
+            m = fmax(m, fabs(v));
+            q += nan0(a.contrib[a.rq_src[e]]);
+        }
+    }
+    s_sum[threadIdx.x] = s;
+    s_q[threadIdx.x] = q;
+    s_max[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s_sum[threadIdx.x] += s_sum[threadIdx.x + o];
+            s_q[threadIdx.x] += s_q[threadIdx.x + o];
+            s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    if (is_csr) {
+        double v = s_sum[0];
+        if (a.csr_diag[item]) v += a.gdiag;
+        v += a.csr_const[item];
+        a.csr_vals[item] = v;
+    } else {
+        finish_row(a, item, s_sum[0], s_q[0], s_max[0]);
+    }
+}
+
 void launch_assemble(const AssembleArgs& a, cudaStream_t s) {
     const long long total = (long long)a.nnz + a.n_unk + a.n_vsrc;
     if (total == 0) return;
     assemble_kernel<<<ceil_div(total, 256), 256, 0, s>>>(a);
+    if (a.n_heavy_csr + a.n_heavy_row) assemble_heavy_kernel<<<a.n_heavy_csr + a.n_heavy_row, 256, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -154,15 +209,17 @@ void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// Static-pivot sparse LU: sync-free left-looking factorisation.
+// Static-pivot sparse LU of the block M: sync-free left-looking factorisation.
 //
-// Column j (in elimination order) is owned by one warp.  Its values start as
-// the permuted A entries; for each k in the U pattern of column j (ascending)
-// the warp waits until column k is final, reads u = U(k, j) and applies
-// x(i) -= L(i, k) * u for every row i of L(:, k) through a precomputed map of
-// positions inside column j.  Columns are claimed in increasing order from a
-// global counter, so every dependency (k < j) is already owned by a running
-// warp and the waits always end; each wait is bounded anyway.
+// Column j (in elimination order) is owned by one warp.  The warp first waits,
+// lanes in parallel, until every column k in the U pattern of column j is
+// final; it then stages the column (the permuted A entries) and every update
+// operand L(i, k) with its target position in shared memory in one bulk
+// load, and runs the sequential part, x(i) -= L(i, k) * x(k) for k ascending,
+// entirely on chip.  Columns are claimed in increasing order from a global
+// counter, so every dependency (k < j) is owned by a warp that is already
+// running and the waits always end; each wait is bounded anyway.  Columns too
+// large for the shared-memory stage run the same loop on global memory.
 // ---------------------------------------------------------------------------
 
 struct LUArgs {
@@ -174,6 +231,7 @@ struct LUArgs {
     const long long* ustart;
     const long long* umap_ptr;
     const int* umap;
+    const long long* ukl;
     const double* A;
     int* done;
     int* counter;
@@ -183,44 +241,102 @@ struct LUArgs {
     unsigned spin_limit;
 };
 
+constexpr int LU_WARPS = 4;
+constexpr int CAP_X = 256;   // column entries staged per warp
+constexpr int CAP_U = 512;   // update operands staged per warp
+constexpr int CAP_T = 128;   // U entries staged per warp
+
 template <typename T>
-__global__ void __launch_bounds__(256) lu_factor_kernel(LUArgs a, T* vals) {
+struct LUSmem {
+    T x[LU_WARPS][CAP_X];
+    T lv[LU_WARPS][CAP_U];
+    int um[LU_WARPS][CAP_U];
+    int uptr[LU_WARPS][CAP_T + 1];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(LU_WARPS * 32) lu_factor_kernel(LUArgs a, T* vals) {
+    __shared__ LUSmem<T> sm;
     const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    T* x = sm.x[w];
+    T* lv = sm.lv[w];
+    int* um = sm.um[w];
+    int* uptr = sm.uptr[w];
     while (true) {
         int j = 0;
         if (lane == 0) j = atomicAdd(a.counter, 1);
         j = __shfl_sync(0xffffffffu, j, 0);
         if (j >= a.n) return;
         const long long s0 = a.col_ptr[j], s1 = a.col_ptr[j + 1];
+        const int len = (int)(s1 - s0);
         const int nu = a.nU[j];
-        for (long long s = s0 + lane; s < s1; s += 32) {
-            const int e = a.f2a[s];
-            vals[s] = e >= 0 ? (T)a.A[e] : (T)0;
-        }
-        __syncwarp();
         const long long ub = a.ustart[j];
+        const long long M0 = a.umap_ptr[ub], M1 = a.umap_ptr[ub + nu];
+        const long long nupd = M1 - M0;
+        // 1. dependencies, waited for in parallel
         bool ok = true;
-        for (int t = 0; t < nu; ++t) {
-            const int k = a.rows[s0 + t];
-            if (lane == 0) ok = wait_flag(a.done + k, a.epoch, a.abort_flag, a.err, a.spin_limit);
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (!ok) break;
+        for (int t = lane; t < nu; t += 32)
+            ok = ok && wait_flag(a.done + a.rows[s0 + t], a.epoch, a.abort_flag, a.err, a.spin_limit);
+        ok = __all_sync(0xffffffffu, ok);
+        const bool fits = len <= CAP_X && nupd <= CAP_U && nu <= CAP_T;
+        if (ok && fits) {
+            // 2. bulk stage: column values, update pointers, update operands
+            for (int s = lane; s < len; s += 32) {
+                const int e = a.f2a[s0 + s];
+                x[s] = e >= 0 ? (T)a.A[e] : (T)0;
+            }
+            for (int t = lane; t <= nu; t += 32) uptr[t] = (int)(a.umap_ptr[ub + t] - M0);
             __syncwarp();
-            const T u = vals[s0 + t];
-            const long long kL = a.col_ptr[k] + a.nU[k] + 1;
-            const long long m0 = a.umap_ptr[ub + t], m1 = a.umap_ptr[ub + t + 1];
-            if (u != (T)0) {
-                for (long long m = m0 + lane; m < m1; m += 32) vals[s0 + a.umap[m]] -= vals[kL + (m - m0)] * u;
+            for (int m = lane; m < (int)nupd; m += 32) {
+                int lo = 0, hi = nu;  // largest t with uptr[t] <= m
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (uptr[mid] <= m) lo = mid; else hi = mid;
+                }
+                lv[m] = vals[a.ukl[ub + lo] + (m - uptr[lo])];
+                um[m] = a.umap[M0 + m];
             }
             __syncwarp();
+            // 3. sequential elimination on chip
+            for (int t = 0; t < nu; ++t) {
+                const T u = x[t];
+                if (u != (T)0)
+                    for (int m = uptr[t] + lane; m < uptr[t + 1]; m += 32) x[um[m]] -= lv[m] * u;
+                __syncwarp();
+            }
+            T piv = x[nu];
+            if (piv == (T)0 || !isfinite((double)piv)) {
+                if (lane == 0) atomicOr(a.err, DEV_ERR_PIVOT);
+                piv = (T)1e-30;
+                if (lane == 0) x[nu] = piv;
+                __syncwarp();
+            }
+            for (int s = lane; s < len; s += 32) vals[s0 + s] = s > nu ? x[s] / piv : x[s];
+        } else if (ok) {
+            // large column: same elimination on global memory
+            for (int s = lane; s < len; s += 32) {
+                const int e = a.f2a[s0 + s];
+                vals[s0 + s] = e >= 0 ? (T)a.A[e] : (T)0;
+            }
+            __syncwarp();
+            for (int t = 0; t < nu; ++t) {
+                const T u = vals[s0 + t];
+                const long long m0 = a.umap_ptr[ub + t], m1 = a.umap_ptr[ub + t + 1];
+                const long long kL = a.ukl[ub + t];
+                if (u != (T)0)
+                    for (long long m = m0 + lane; m < m1; m += 32) vals[s0 + a.umap[m]] -= vals[kL + (m - m0)] * u;
+                __syncwarp();
+            }
+            T piv = vals[s0 + nu];
+            if (piv == (T)0 || !isfinite((double)piv)) {
+                if (lane == 0) atomicOr(a.err, DEV_ERR_PIVOT);
+                piv = (T)1e-30;
+                if (lane == 0) vals[s0 + nu] = piv;
+            }
+            __syncwarp();
+            for (long long s = s0 + nu + 1 + lane; s < s1; s += 32) vals[s] = vals[s] / piv;
         }
-        T piv = vals[s0 + nu];
-        if (piv == (T)0 || !isfinite((double)piv)) {
-            if (lane == 0) atomicOr(a.err, DEV_ERR_PIVOT);
-            piv = (T)1e-30;
-            if (lane == 0) vals[s0 + nu] = piv;
-        }
-        for (long long s = s0 + nu + 1 + lane; s < s1; s += 32) vals[s] = vals[s] / piv;
         __syncwarp();
         __threadfence();
         if (lane == 0) st_release(a.done + j, a.epoch);
@@ -234,8 +350,7 @@ struct SolveArgs {
     const int* col;          // dependency index of each entry
     const long long* col_ptr;
     const int* nU;
-    const int* brow;         // forward: A-row of permuted row
-    const int* q;            // backward: original column of permuted column
+    const int* q;            // backward: B index of permuted column
     int* done;
     int* counter;
     int* abort_flag;
@@ -244,10 +359,30 @@ struct SolveArgs {
     unsigned spin_limit;
 };
 
-// L y = P b (unit lower triangular), row-oriented, one warp per row.
+// Right-hand side of the block M: b restricted to M minus the couplings to the
+// singletons solved first (x_F = b_F / diag).  Also writes x_F.
+template <typename T>
+__global__ void lu_pre_kernel(int nM, int nF, const int* brow, const int* pre_ptr, const int* pre_e,
+                              const int* pre_f, const int* f_col, const int* f_arow, const int* f_diag_e,
+                              const double* A, const double* b, T* rhsM, double* xout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nM) {
+        double v = b[brow[i]];
+        for (int e = pre_ptr[i]; e < pre_ptr[i + 1]; ++e) {
+            const int f = pre_f[e];
+            v -= A[pre_e[e]] * (b[f_arow[f]] / A[f_diag_e[f]]);
+        }
+        rhsM[i] = (T)v;
+    } else if (i < nM + nF) {
+        const int f = i - nM;
+        xout[f_col[f]] = b[f_arow[f]] / A[f_diag_e[f]];
+    }
+}
+
+// L y = rhs (unit lower triangular), row-oriented, one warp per row.
 template <typename T>
 __global__ void __launch_bounds__(256) lu_fwd_kernel(SolveArgs a, const T* __restrict__ vals,
-                                                     const double* __restrict__ b, T* y) {
+                                                     const T* __restrict__ rhs, T* y) {
     const int lane = threadIdx.x & 31;
     while (true) {
         int i = 0;
@@ -262,7 +397,7 @@ __global__ void __launch_bounds__(256) lu_fwd_kernel(SolveArgs a, const T* __res
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) {
-            y[i] = (T)b[a.brow[i]] - acc;
+            y[i] = rhs[i] - acc;
             __threadfence();
             st_release(a.done + i, a.epoch);
         }
@@ -298,26 +433,38 @@ __global__ void __launch_bounds__(256) lu_bwd_kernel(SolveArgs a, const T* __res
     }
 }
 
-static int persistent_blocks() {
-    static int blocks = 0;
-    if (!blocks) {
-        int dev = 0, sms = 0;
+// Singletons solved last: x_c = (b_c - sum_j B(c, j) x_j) / B(c, c), one warp per row.
+__global__ void lu_post_kernel(int nL, const int* l_col, const int* l_arow, const int* l_diag_e, const int* l_ptr,
+                               const int* l_e, const int* l_x, const double* A, const double* b, double* xout) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nL) return;
+    double acc = 0.0;
+    for (int e = l_ptr[warp] + lane; e < l_ptr[warp + 1]; e += 32) acc += A[l_e[e]] * xout[l_x[e]];
+    for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) xout[l_col[warp]] = (b[l_arow[warp]] - acc) / A[l_diag_e[warp]];
+}
+
+static int persistent_blocks(int per_sm) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        blocks = std::max(1, sms) * 4;
+        sms = std::max(1, sms);
     }
-    return blocks;
+    return sms * per_sm;
 }
 
 static unsigned spin_limit_default() { return 1u << 24; }
 
 void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
     SparseLU& L = c.lu;
-    if (L.n == 0) return;
+    if (L.nM == 0) return;
     L.epoch++;
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
     LUArgs a{};
-    a.n = L.n;
+    a.n = L.nM;
     a.col_ptr = L.d_col_ptr.p;
     a.nU = L.d_nU.p;
     a.rows = L.d_rows.p;
@@ -325,6 +472,7 @@ void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
     a.ustart = L.d_ustart.p;
     a.umap_ptr = L.d_umap_ptr.p;
     a.umap = L.d_umap.p;
+    a.ukl = L.d_ukl.p;
     a.A = A;
     a.done = L.d_done.p;
     a.counter = L.d_counters.p;
@@ -332,41 +480,53 @@ void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
     a.err = &c.d_status.p->dev_err;
     a.epoch = L.epoch;
     a.spin_limit = spin_limit_default();
-    const int blocks = std::min(persistent_blocks(), ceil_div((long long)L.n * 32, 256));
-    if (fp32) lu_factor_kernel<float><<<blocks, 256, 0, s>>>(a, L.d_vals32.p);
-    else lu_factor_kernel<double><<<blocks, 256, 0, s>>>(a, L.d_vals64.p);
+    const int threads = LU_WARPS * 32;
+    const int blocks = std::min(persistent_blocks(fp32 ? 8 : 5), ceil_div((long long)L.nM * 32, threads));
+    if (fp32) lu_factor_kernel<float><<<blocks, threads, 0, s>>>(a, L.d_vals32.p);
+    else lu_factor_kernel<double><<<blocks, threads, 0, s>>>(a, L.d_vals64.p);
     VGB_CUDA(cudaGetLastError());
 }
 
 template <typename T>
-static void lu_solve_once(Circuit& c, const T* vals, const double* rhs, double* x, T* ybuf, T* xbuf, cudaStream_t s) {
+static void lu_solve_once(Circuit& c, const T* vals, const double* A, const double* rhs, double* x, T* rhsM, T* ybuf,
+                          T* xbuf, cudaStream_t s) {
     SparseLU& L = c.lu;
-    L.epoch++;
-    VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
-    const int blocks = std::min(persistent_blocks(), ceil_div((long long)L.n * 32, 256));
-    SolveArgs f{};
-    f.n = L.n;
-    f.ptr = L.d_lrow_ptr.p;
-    f.pos = L.d_lrow_pos.p;
-    f.col = L.d_lrow_col.p;
-    f.col_ptr = L.d_col_ptr.p;
-    f.nU = L.d_nU.p;
-    f.brow = L.d_brow.p;
-    f.q = L.d_q.p;
-    f.done = L.d_done.p + L.n;
-    f.counter = L.d_counters.p + 1;
-    f.abort_flag = L.d_counters.p + 3;
-    f.err = &c.d_status.p->dev_err;
-    f.epoch = L.epoch;
-    f.spin_limit = spin_limit_default();
-    lu_fwd_kernel<T><<<blocks, 256, 0, s>>>(f, vals, rhs, ybuf);
-    SolveArgs b = f;
-    b.ptr = L.d_urow_ptr.p;
-    b.pos = L.d_urow_pos.p;
-    b.col = L.d_urow_col.p;
-    b.done = L.d_done.p + 2 * (size_t)L.n;
-    b.counter = L.d_counters.p + 2;
-    lu_bwd_kernel<T><<<blocks, 256, 0, s>>>(b, vals, ybuf, xbuf, x);
+    const int nM = L.nM, nF = (int)L.f_col.size(), nL = (int)L.l_col.size();
+    if (nM + nF)
+        lu_pre_kernel<T><<<ceil_div(nM + nF, 256), 256, 0, s>>>(nM, nF, L.d_brow.p, L.d_pre_ptr.p, L.d_pre_e.p,
+                                                                L.d_pre_f.p, L.d_f_col.p, L.d_f_arow.p,
+                                                                L.d_f_diag_e.p, A, rhs, rhsM, x);
+    if (nM) {
+        L.epoch++;
+        VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
+        const int blocks = std::min(persistent_blocks(8), ceil_div((long long)nM * 32, 256));
+        SolveArgs f{};
+        f.n = nM;
+        f.ptr = L.d_lrow_ptr.p;
+        f.pos = L.d_lrow_pos.p;
+        f.col = L.d_lrow_col.p;
+        f.col_ptr = L.d_col_ptr.p;
+        f.nU = L.d_nU.p;
+        f.q = L.d_q.p;
+        f.done = L.d_done.p + nM;
+        f.counter = L.d_counters.p + 1;
+        f.abort_flag = L.d_counters.p + 3;
+        f.err = &c.d_status.p->dev_err;
+        f.epoch = L.epoch;
+        f.spin_limit = spin_limit_default();
+        lu_fwd_kernel<T><<<blocks, 256, 0, s>>>(f, vals, rhsM, ybuf);
+        SolveArgs b = f;
+        b.ptr = L.d_urow_ptr.p;
+        b.pos = L.d_urow_pos.p;
+        b.col = L.d_urow_col.p;
+        b.done = L.d_done.p + 2 * (size_t)nM;
+        b.counter = L.d_counters.p + 2;
+        lu_bwd_kernel<T><<<blocks, 256, 0, s>>>(b, vals, ybuf, xbuf, x);
+    }
+    if (nL)
+        lu_post_kernel<<<ceil_div((long long)nL * 32, 256), 256, 0, s>>>(nL, L.d_l_col.p, L.d_l_arow.p,
+                                                                        L.d_l_diag_e.p, L.d_l_ptr.p, L.d_l_e.p,
+                                                                        L.d_l_x.p, A, rhs, x);
     VGB_CUDA(cudaGetLastError());
 }
 
@@ -391,18 +551,23 @@ void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp
     SparseLU& L = c.lu;
     const int n = L.n;
     if (n == 0) return;
+    const int nM = std::max(L.nM, 1);
     if (!fp32) {
-        lu_solve_once<double>(c, L.d_vals64.p, rhs, x, (double*)c.d_work.p, (double*)c.d_work2.p, s);
+        double* rhsM = c.d_work.p;
+        double* ybuf = c.d_work.p + nM;
+        double* xbuf = c.d_work.p + 2 * (size_t)nM;
+        lu_solve_once<double>(c, L.d_vals64.p, A, rhs, x, rhsM, ybuf, xbuf, s);
         return;
     }
-    float* ybuf = (float*)c.d_work.p;
-    float* xbuf = ybuf + n;
-    lu_solve_once<float>(c, L.d_vals32.p, rhs, x, ybuf, xbuf, s);
+    float* rhsM = (float*)c.d_work.p;
+    float* ybuf = rhsM + nM;
+    float* xbuf = ybuf + nM;
+    lu_solve_once<float>(c, L.d_vals32.p, A, rhs, x, rhsM, ybuf, xbuf, s);
     double* r = c.d_work2.p;
     double* d = c.d_work2.p + n;
     for (int k = 0; k < sweeps; ++k) {
         residual_kernel<<<ceil_div((long long)n * 32, 256), 256, 0, s>>>(n, c.d_indptr.p, c.d_indices.p, A, rhs, x, r);
-        lu_solve_once<float>(c, L.d_vals32.p, r, d, ybuf, xbuf, s);
+        lu_solve_once<float>(c, L.d_vals32.p, A, r, d, rhsM, ybuf, xbuf, s);
         axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, x);
     }
 }

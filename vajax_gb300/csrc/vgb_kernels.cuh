@@ -20,6 +20,8 @@ struct AssembleArgs {
     const unsigned char* conv_mask;
     double* csr_vals; double* f; double* Q; double* maxc; double* fres;
     NRStatus* st;
+    const int* heavy_csr; int n_heavy_csr;   // CSR entries with gather lists longer than HEAVY_LIST
+    const int* heavy_row; int n_heavy_row;   // node rows with gather lists longer than HEAVY_LIST
 };
 
 void launch_assemble(const AssembleArgs& a, cudaStream_t s);

@@ -225,17 +225,17 @@ extern "C" int vgb_transient(void* h, const double* cfg, const double* X0, const
             k.c0 = inv; k.c1 = -inv;
             if (method == 1) { k.c0 = 2 * inv; k.c1 = -2 * inv; k.d1 = -1.0; }
             else if (method == 2) { k.c0 = 1.5 * inv; k.c1 = -2.0 * inv; k.c2 = 0.5 * inv; }
-            DefaultVecs& dv = defaults_for(*c, abstol, s);
+            DefaultVecs dv = defaults_for(*c, abstol, s);
             for (int i = 0; i < n_steps; ++i) {
                 const double t_next = ((double)i + 1.0) * dt;
                 launch_eval_sources(c->vsrc_wave, n_vsrc, t_next, vs.p, s);
                 launch_eval_sources(c->isrc_wave, c->n_isrc, t_next, is.p, s);
                 VGB_CUDA(cudaMemcpyAsync(Xc.p, X.p, n_x * sizeof(double), cudaMemcpyDeviceToDevice, s));
-                NRResult r = nr_loop(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, dv.floor_abstol.p, k, o, tran_itl, s);
+                NRResult r = nr_loop(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, dv.floor_abstol, k, o, tran_itl, s);
                 total_nr += r.iterations;
                 if (!r.converged) nr_fail_count++;
                 launch_status_reset(c->d_status.p, s);
-                build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, k, dv.floor_abstol.p, reltol, vntol,
+                build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, k, dv.floor_abstol, reltol, vntol,
                              c->d_csr_vals.p, c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
                 launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
                 launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, k.c0, k.c1, k.d1, k.c2, dQn.p, n_unk, s);
@@ -245,6 +245,8 @@ extern "C" int vgb_transient(void* h, const double* cfg, const double* X0, const
                                                      Vmax.p, c->d_maxc.p, hmaxc.p, Ivs.p,
                                                      Vout.p + (size_t)(i + 1) * n_ext, Iout.p + (size_t)(i + 1) * nvo);
                 tout[i + 1] = t_next;
+                // sources (2), status reset, vsource current, dQ/dt, commit
+                c->launches += (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0) + 4;
             }
             step_idx = n_steps + 1;
         } else {
@@ -328,6 +330,8 @@ extern "C" int vgb_transient(void* h, const double* cfg, const double* X0, const
                     n_nodes, n_x, n_unk, n_ext, n_vsrc, use_new ? 1 : 0, accept ? 1 : 0, nr_failed_at_min ? 1 : 0,
                     Xc.p, X.p, c->d_Q.p, Qp.p, dQn.p, dQp.p, Qp2.p, hist.p + (size_t)new_head * n_nodes, Vmax.p,
                     c->d_maxc.p, hmaxc.p, Ivs.p, Vout.p + (size_t)step_idx * n_ext, Iout.p + (size_t)step_idx * nvo);
+                // sources, predictor, status reset, vsource current, dQ/dt, LTE, commit
+                c->launches += (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0) + 6;
                 if (use_new) {
                     head = new_head;
                     for (int q = 3; q > 0; --q) dt_hist[q] = dt_hist[q - 1];

@@ -103,6 +103,8 @@ class CircuitEngine:
         self.device = None
         self._prepared = False
         self.analysis_params: Dict[str, float] = {}
+        self.homotopy = True
+        self.dc_method = ""
 
     # parse: resolve node numbering and device groups (engine.py:421-486)
     def parse(self):
@@ -181,12 +183,26 @@ class CircuitEngine:
             return X0, Q.cpu().numpy(), I0, np.zeros(rc.n_nodes - 1), True
         X0 = np.zeros(n_x)
         X0[: rc.n_nodes] = self.init_mid_rail()
-        Xd = torch.as_tensor(X0, device="cuda")
-        r = dev.nr_solve(Xd, vs0 if len(rc.vsources) else None, is0, c0=0.0, reltol=self.options.reltol,
-                         abstol=self.options.abstol, vntol=self.options.vntol, damping=self.options.nr_damping,
-                         max_iter=self.options.tran_itl)
-        return (r["X"].cpu().numpy(), r["Q"].cpu().numpy(), r["I_vsource"].cpu().numpy(),
-                r["max_res_contrib"].cpu().numpy(), r["converged"])
+        o = self.options
+
+        def solve(X, gshunt=0.0, sf=1.0):
+            Xd = torch.as_tensor(np.array(X, np.float64), device="cuda")
+            r = dev.nr_solve(Xd, vs0 * sf if len(rc.vsources) else None, is0 * sf if is0 is not None else None,
+                             c0=0.0, gshunt=gshunt, reltol=o.reltol, abstol=o.abstol, vntol=o.vntol,
+                             damping=o.nr_damping, max_iter=o.tran_itl)
+            Xn = r["X"].cpu().numpy()
+            return Xn, r["iterations"], bool(r["converged"] and np.all(np.isfinite(Xn))), r
+
+        # plain Newton from mid-rail first (full_mna.py:922-957) ...
+        Xn, _, ok, r = solve(X0)
+        self.dc_method = "newton"
+        if not ok and self.homotopy:
+            # ... then the homotopy chain when it does not converge (homotopy.py:470-567)
+            from vajax_gb300.dc import homotopy_chain
+            Xh, ok, self.dc_method, _, _ = homotopy_chain(lambda X, g, s: solve(X, g, s)[:3], X0)
+            if ok:
+                Xn, _, ok, r = solve(Xh)
+        return (Xn, r["Q"].cpu().numpy(), r["I_vsource"].cpu().numpy(), r["max_res_contrib"].cpu().numpy(), ok)
 
     def transient_cfg(self) -> Dict[str, float]:
         cfg = self.config

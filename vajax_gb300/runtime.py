@@ -34,7 +34,11 @@ def _ptr(t) -> Optional[int]:
 
 
 class DeviceCircuit:
-    def __init__(self, rc: ResolvedCircuit, precision: int = 0, refine_sweeps: int = 3, gmin: float = 1e-12):
+    """``device=False`` stops after the host-side analysis (pattern, maps,
+    symbolic factorisation), which needs no GPU."""
+
+    def __init__(self, rc: ResolvedCircuit, precision: int = 0, refine_sweeps: int = 3, gmin: float = 1e-12,
+                 device: bool = True):
         self.rc = rc
         self.lib = _lib.load()
         h = C.c_void_p()
@@ -65,7 +69,9 @@ class DeviceCircuit:
             if rc.internal_nodes:
                 inn = np.asarray(rc.internal_nodes, np.int32)
                 self._check(self.lib.vgb_circuit_set_internal_nodes(h, len(inn), _ip(inn)))
-            self._check(self.lib.vgb_circuit_finalize(h, gmin, precision, refine_sweeps))
+            self._check(self.lib.vgb_circuit_analyze(h))
+            if device:
+                self._check(self.lib.vgb_circuit_finalize(h, gmin, precision, refine_sweeps))
         except Exception:
             self.lib.vgb_circuit_destroy(h)
             self.h = None
@@ -92,7 +98,20 @@ class DeviceCircuit:
         except Exception:
             pass
 
+    def profile(self, mode: int = -1) -> Dict[str, float]:
+        """mode 1: enable + reset, 0: disable + reset, -1: read."""
+        out = np.zeros(7)
+        self._check(self.lib.vgb_profile(self.h, mode, _dp(out)))
+        keys = ["eval_ms", "assemble_ms", "factor_ms", "solve_ms", "update_ms", "iterations", "launches"]
+        return dict(zip(keys, out.tolist()))
+
     # ---- pattern and maps -------------------------------------------------
+    def solver_info(self) -> Dict[str, int]:
+        out = np.zeros(8, np.int64)
+        self._check(self.lib.vgb_solver_info(self.h, out.ctypes.data_as(_lib.i64p)))
+        keys = ["n_aug", "nnz", "nnz_lu", "lu_flops", "etree_height", "max_col", "crit_path", "contrib_slots"]
+        return dict(zip(keys, map(int, out)))
+
     def pattern(self):
         indptr = np.zeros(self.n_aug + 1, np.int32)
         indices = np.zeros(max(self.nnz, 1), np.int32)
