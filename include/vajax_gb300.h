@@ -80,9 +80,17 @@ int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx);
  * symbolic factorisation.  Touches no GPU; the pattern getters below work
  * after this call.  finalize() runs it when it has not been run. */
 int vgb_circuit_analyze(void* h);
-/* Solver statistics after analysis, out[8] = {n_aug, nnz, nnz_lu, lu_flops,
- * etree_height, max_factor_column, critical_path_steps, contribution_slots}. */
+/* Solver statistics after analysis, out[16] = {n_aug, nnz, nnz_lu, lu_flops,
+ * etree_height, max_factor_column, critical_path_steps, contribution_slots,
+ * supernodes, max_front, front_storage, front_flops, front_tree_depth, 0, 0, 0}. */
 int vgb_solver_info(void* h, int64_t* out);
+
+/* Static-pivot ordering: perm_r[n_aug] (row r of the factorised matrix is row
+ * perm_r[r] of the Jacobian) and order[n_aug] (elimination order of the
+ * columns: pinned singletons, the multifrontal block, trailing singletons).
+ * Replaces the symbolic data the reference caches inside UMFPACK/cuDSS
+ * (vajax/sparse/umfpack_ffi.cpp:140-185). */
+int vgb_solver_order(void* h, int* perm_r, int* order);
 
 /* Per-phase device timing of the Newton loop (CUDA events on the handle's
  * stream).  mode 1 enables and resets, 0 disables and resets, -1 only reads.

@@ -68,6 +68,6 @@ def test_empty_circuit_rejected_cleanly():
     h = ctypes.c_void_p()
     assert lib.vgb_circuit_create(1, 0, None, None, 0, None, None, ctypes.byref(h)) == 0
     assert lib.vgb_circuit_analyze(h) == 0
-    out = (ctypes.c_int64 * 8)()
+    out = (ctypes.c_int64 * 16)()
     assert lib.vgb_solver_info(h, out) == 0 and out[0] == 0
     assert lib.vgb_circuit_destroy(h) == 0

@@ -33,6 +33,7 @@ SIGNATURES = {
     "vgb_circuit_set_internal_nodes": (C.c_int, [vp, C.c_int, i32p]),
     "vgb_circuit_analyze": (C.c_int, [vp]),
     "vgb_profile": (C.c_int, [vp, C.c_int, f64p]),
+    "vgb_solver_order": (C.c_int, [vp, i32p, i32p]),
     "vgb_solver_info": (C.c_int, [vp, i64p]),
     "vgb_circuit_finalize": (C.c_int, [vp, C.c_double, C.c_int, C.c_int]),
     "vgb_pattern_info": (C.c_int, [vp, i32p, i32p, i64p, i64p]),

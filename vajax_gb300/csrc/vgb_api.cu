@@ -282,6 +282,27 @@ int vgb_solver_info(void* h, int64_t* out) {
         out[5] = L.max_col;
         out[6] = L.crit_path;
         out[7] = c->n_contrib;
+        out[8] = L.nsn;
+        out[9] = L.mf_max_m;
+        out[10] = L.fr_off.empty() ? 0 : L.fr_off.back();
+        out[11] = L.mf_flops;
+        out[12] = L.mf_depth;
+    });
+}
+
+int vgb_solver_order(void* h, int* perm_r, int* order) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(c->analyzed, "circuit is not analyzed");
+        const SparseLU& L = c->lu;
+        if (perm_r) std::memcpy(perm_r, L.perm_r.data(), L.perm_r.size() * sizeof(int));
+        if (order) {
+            int k = 0;
+            for (int i : L.f_col) order[k++] = i;
+            for (int i : L.q) order[k++] = i;
+            for (int i : L.l_col) order[k++] = i;
+        }
     });
 }
 
@@ -393,10 +414,45 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         up(L.d_pre_ptr, L.pre_ptr);
         up(L.d_pre_e, L.pre_e);
         up(L.d_pre_f, L.pre_f);
-        if (precision == 1) L.d_vals32.alloc(std::max<long long>(L.nnz_lu, 1));
-        else L.d_vals64.alloc(std::max<long long>(L.nnz_lu, 1));
-        L.d_done.alloc(3 * (size_t)std::max(L.nM, 1));
-        L.d_done.zero(c->stream);
+        // multifrontal structure
+        auto up64 = [](DevBuf<long long>& d, const std::vector<long long>& h) {
+            d.upload(h.empty() ? std::vector<long long>{0} : h);
+        };
+        up64(L.d_fr_ptr, L.fr_ptr);
+        up64(L.d_fr_off, L.fr_off);
+        up64(L.d_em_ptr, L.em_ptr);
+        up64(L.d_asm_ptr, L.asm_ptr);
+        up64(L.d_cv_off, L.fr_cv_off);
+        up(L.d_fr_idx, L.fr_idx);
+        up(L.d_fr_w, L.fr_w);
+        up(L.d_sn_first, L.sn_first);
+        up(L.d_sn_parent, L.sn_parent);
+        up(L.d_ch_ptr, L.ch_ptr);
+        up(L.d_ch_idx, L.ch_idx);
+        up(L.d_em_idx, L.em_idx);
+        up(L.d_asm_e, L.asm_e);
+        up(L.d_asm_pos, L.asm_pos);
+        up(L.d_fr_task0, L.fr_task0);
+        up(L.d_fr_nb, L.fr_nb);
+        up(L.d_task_type, L.task_type);
+        up(L.d_task_front, L.task_front);
+        up(L.d_task_b0, L.task_b0);
+        up(L.d_task_b1, L.task_b1);
+        up(L.d_fr_big, L.fr_big);
+        up(L.d_big_asm_e, L.big_asm_e);
+        up64(L.d_big_asm_pos, L.big_asm_pos);
+        const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
+        const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
+        if (precision == 1) {
+            L.d_pool32.alloc(pool);
+            L.d_cv32.alloc(cvn);
+        } else {
+            L.d_pool64.alloc(pool);
+            L.d_cv64.alloc(cvn);
+        }
+        L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1) + std::max<size_t>(L.task_type.size(), 1));
+        L.d_mf_flags.zero(c->stream);
+        L.d_mf_count.alloc(std::max(L.nsn, 1));
         L.d_counters.alloc(4);
         const size_t na = std::max(c->n_aug, 1), nu = std::max(c->n_unk, 1);
         c->d_csr_vals.alloc(std::max(c->nnz, 1));

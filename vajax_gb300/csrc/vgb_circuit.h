@@ -81,6 +81,19 @@ struct Sources {
     DevBuf<double> d_data;
 };
 
+// An A entry inside the factorised block: CSR slot and permuted row/column.
+struct MEntry {
+    int e, i, j;
+};
+
+// Widest supernode (number of pivots eliminated by one front).
+constexpr int FRONT_WMAX = 64;
+// Fronts up to SMALL_FRONT wide are factorised by one CTA in shared memory;
+// larger ones are split into diagonal, panel and Schur-complement tile tasks.
+constexpr int SMALL_FRONT = 64;
+constexpr int FRONT_TILE = 32;
+enum TaskType : int { TASK_SMALL = 0, TASK_DIAG = 1, TASK_PANEL = 2, TASK_SCHUR = 3 };
+
 // Static-pivot sparse LU structures (host symbolic + device numeric).
 struct SparseLU {
     int n = 0;                   // n_aug
@@ -112,6 +125,34 @@ struct SparseLU {
     std::vector<long long> urow_pos;  // positions of U(i,j), j > i
     std::vector<int> urow_col;        // j of each
     long long nnz_lu = 0, flops = 0;
+    // multifrontal structure of M (supernodes numbered by first column: children before parents)
+    int nsn = 0;
+    std::vector<int> sn_first, sn_of, sn_parent, fr_w;
+    std::vector<long long> fr_ptr, fr_off;            // front index lists, dense front storage offsets
+    std::vector<int> fr_idx;                          // global (permuted M) index of each front row/column
+    std::vector<int> ch_ptr, ch_idx;                  // children of each supernode
+    std::vector<long long> em_ptr;                    // extend-add map of each supernode into its parent
+    std::vector<int> em_idx;
+    std::vector<long long> asm_ptr;                   // A entries assembled into each front
+    std::vector<int> asm_e, asm_pos;                  // A slot, position r + c*m inside the front
+    long long mf_max_m = 0, mf_flops = 0, mf_depth = 0;
+    std::vector<long long> fr_cv_off;                 // forward-solve contribution vector offsets
+    std::vector<int> fr_task0, fr_nb;                 // first task of each front, tiles per dimension
+    std::vector<int> task_type, task_front, task_b0, task_b1;
+    std::vector<int> fr_big;                          // 1 = front handled by tile tasks
+    std::vector<int> big_asm_e;                       // A entries of large fronts ...
+    std::vector<long long> big_asm_pos;               // ... and their absolute pool positions
+    long long big_lo = 0, big_hi = 0;                 // pool span holding the large fronts
+    DevBuf<int> d_fr_big, d_big_asm_e;
+    DevBuf<long long> d_big_asm_pos;
+    // device mirrors of the multifrontal structure
+    DevBuf<long long> d_fr_ptr, d_fr_off, d_em_ptr, d_asm_ptr, d_cv_off;
+    DevBuf<int> d_fr_idx, d_fr_w, d_sn_first, d_sn_parent, d_ch_ptr, d_ch_idx, d_em_idx, d_asm_e, d_asm_pos;
+    DevBuf<int> d_fr_task0, d_fr_nb, d_task_type, d_task_front, d_task_b0, d_task_b1;
+    DevBuf<int> d_mf_flags;                            // done, diag_done, fwd_done, bwd_done [4 ns] + panel flags
+    DevBuf<int> d_mf_count;                            // completed Schur tiles per front [ns]
+    DevBuf<double> d_pool64, d_cv64, d_y64;
+    DevBuf<float> d_pool32, d_cv32, d_y32;
     long long etree_height = 0;   // levels of the elimination tree
     long long max_col = 0;        // longest factor column (entries)
     long long crit_path = 0;      // longest dependency chain, in sequential column steps

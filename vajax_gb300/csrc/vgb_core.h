@@ -20,8 +20,8 @@ inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
 // Kernel launches of one linear solve (factor + triangular solves + refinement).
 inline long long solve_launches(const Circuit& c) {
     const SparseLU& L = c.lu;
-    long long once = (L.nM + (long long)L.f_col.size() ? 1 : 0) + (L.nM ? 2 : 0) + (L.l_col.empty() ? 0 : 1);
-    long long n = (L.nM ? 1 : 0) + once;
+    long long once = (L.nM + (long long)L.f_col.size() ? 1 : 0) + (L.nsn ? 2 : 0) + (L.l_col.empty() ? 0 : 1);
+    long long n = (L.nsn ? 1 : 0) + (L.big_asm_e.empty() ? 0 : 1) + once;
     if (c.solver_kind == 1) n += (long long)c.refine_sweeps * (once + 2);
     return n;
 }

@@ -216,6 +216,213 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
     return order;
 }
 
+// ---------------------------------------------------------------------------
+// Multifrontal structure of the block M
+//
+// Fundamental supernodes: column j+1 joins the supernode of column j when j is
+// its only child in the elimination tree and the structure of L(:, j) is
+// {j+1} plus the structure of L(:, j+1); widths are capped at FRONT_WMAX.
+// The front of supernode S = [f, l] is the dense matrix on the index set
+// I_S = {f..l} U struct(L(:, l)); its trailing block (rows/columns past the
+// pivots) is the contribution block that the parent adds into its own front.
+// Supernodes are numbered by first column, which lists children before
+// parents.
+// ---------------------------------------------------------------------------
+
+void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector<std::vector<int>>& lcol,
+                  const std::vector<MEntry>& entries) {
+    const int nM = L.nM;
+    std::vector<int> nchild(nM, 0);
+    for (int j = 0; j < nM; ++j)
+        if (parent[j] >= 0) nchild[parent[j]]++;
+    std::vector<int> fund;  // first column of each fundamental supernode
+    for (int j = 0; j < nM; ++j) {
+        bool merge = false;
+        if (j > 0 && parent[j - 1] == j && nchild[j] == 1 && lcol[j - 1].size() == lcol[j].size() + 1)
+            merge = (j - fund.back()) < FRONT_WMAX;
+        if (!merge) fund.push_back(j);
+    }
+    // Relaxed amalgamation: fold a child supernode that ends right before its
+    // parent into the parent when the merged front stays narrow and gains few
+    // explicit zeros (thresholds in the spirit of CHOLMOD's nrelax/zrelax).
+    // This shortens the chains of tiny fronts that make up the tree depth.
+    struct Sn { int f, l; long long nnz; };
+    std::vector<Sn> sn;
+    for (size_t k = 0; k < fund.size(); ++k) {
+        const int f = fund[k], l = (k + 1 < fund.size() ? fund[k + 1] : nM) - 1;
+        long long nnz = 0;
+        for (int j = f; j <= l; ++j) nnz += (long long)lcol[j].size();
+        Sn cur{f, l, nnz};
+        while (!sn.empty()) {
+            const Sn& ch = sn.back();
+            const int pc = parent[ch.l];
+            if (ch.l + 1 != cur.f || pc < cur.f || pc > cur.l) break;
+            const long long w = cur.l - ch.f + 1;
+            const long long t = (long long)lcol[cur.l].size();
+            const long long dense = w * (w - 1) / 2 + w * t;
+            const long long actual = ch.nnz + cur.nnz;
+            const double z = dense > 0 ? (double)(dense - actual) / (double)dense : 0.0;
+            const bool ok = w <= FRONT_WMAX &&
+                            (w <= 4 || (w <= 16 && z < 0.8) || (w <= 48 && z < 0.1) || z < 0.05);
+            if (!ok) break;
+            cur = Sn{ch.f, cur.l, actual};
+            sn.pop_back();
+        }
+        sn.push_back(cur);
+    }
+    L.sn_first.clear();
+    L.sn_of.assign(nM, -1);
+    for (size_t s = 0; s < sn.size(); ++s) {
+        L.sn_first.push_back(sn[s].f);
+        for (int j = sn[s].f; j <= sn[s].l; ++j) L.sn_of[j] = (int)s;
+    }
+    const int ns = (int)L.sn_first.size();
+    L.nsn = ns;
+    L.sn_first.push_back(nM);
+    L.sn_parent.assign(ns, -1);
+    L.fr_ptr.assign(ns + 1, 0);
+    L.fr_idx.clear();
+    L.fr_w.assign(ns, 0);
+    L.fr_off.assign(ns + 1, 0);
+    for (int s = 0; s < ns; ++s) {
+        const int f = L.sn_first[s], l = L.sn_first[s + 1] - 1;
+        L.fr_w[s] = l - f + 1;
+        for (int j = f; j <= l; ++j) L.fr_idx.push_back(j);
+        for (int r : lcol[l]) L.fr_idx.push_back(r);
+        L.fr_ptr[s + 1] = (long long)L.fr_idx.size();
+        const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s];
+        L.fr_off[s + 1] = L.fr_off[s] + m * m;
+        if (parent[l] >= 0) L.sn_parent[s] = L.sn_of[parent[l]];
+    }
+    // children and extend-add maps (positions of the child's contribution rows in the parent front)
+    L.ch_ptr.assign(ns + 1, 0);
+    for (int s = 0; s < ns; ++s)
+        if (L.sn_parent[s] >= 0) L.ch_ptr[L.sn_parent[s] + 1]++;
+    for (int s = 0; s < ns; ++s) L.ch_ptr[s + 1] += L.ch_ptr[s];
+    L.ch_idx.assign(L.ch_ptr[ns], 0);
+    {
+        std::vector<int> fill(L.ch_ptr.begin(), L.ch_ptr.end() - 1);
+        for (int s = 0; s < ns; ++s)
+            if (L.sn_parent[s] >= 0) L.ch_idx[fill[L.sn_parent[s]]++] = s;
+    }
+    std::vector<int> local(nM, -1);
+    L.em_ptr.assign(ns + 1, 0);
+    L.em_idx.clear();
+    std::vector<std::vector<int>> em(ns);
+    for (int p = 0; p < ns; ++p) {
+        for (long long t = L.fr_ptr[p]; t < L.fr_ptr[p + 1]; ++t) local[L.fr_idx[t]] = (int)(t - L.fr_ptr[p]);
+        for (int q = L.ch_ptr[p]; q < L.ch_ptr[p + 1]; ++q) {
+            const int c = L.ch_idx[q];
+            for (long long t = L.fr_ptr[c] + L.fr_w[c]; t < L.fr_ptr[c + 1]; ++t) {
+                const int pos = local[L.fr_idx[t]];
+                VGB_REQUIRE(pos >= 0, "child contribution row missing from the parent front");
+                em[c].push_back(pos);
+            }
+        }
+        for (long long t = L.fr_ptr[p]; t < L.fr_ptr[p + 1]; ++t) local[L.fr_idx[t]] = -1;
+    }
+    for (int s = 0; s < ns; ++s) {
+        L.em_idx.insert(L.em_idx.end(), em[s].begin(), em[s].end());
+        L.em_ptr[s + 1] = (long long)L.em_idx.size();
+    }
+    // A entries of M -> (front, position): the front owning min(i, j)
+    std::vector<std::vector<std::pair<int, int>>> asmv(ns);
+    {
+        // local index of a global index inside a front: binary search in the sorted tail
+        for (const auto& me : entries) {
+            const int piv = std::min(me.i, me.j);
+            const int s = L.sn_of[piv];
+            const long long b = L.fr_ptr[s], e = L.fr_ptr[s + 1];
+            auto loc = [&](int g) -> int {
+                const int f = L.sn_first[s];
+                if (g >= f && g < f + L.fr_w[s]) return g - f;
+                auto it = std::lower_bound(L.fr_idx.begin() + b + L.fr_w[s], L.fr_idx.begin() + e, g);
+                VGB_REQUIRE(it != L.fr_idx.begin() + e && *it == g, "A entry outside its front");
+                return (int)(it - (L.fr_idx.begin() + b));
+            };
+            const long long m = e - b;
+            asmv[s].push_back({me.e, (int)(loc(me.i) + (long long)loc(me.j) * m)});
+        }
+    }
+    L.asm_ptr.assign(ns + 1, 0);
+    L.asm_e.clear();
+    L.asm_pos.clear();
+    for (int s = 0; s < ns; ++s) {
+        for (auto& pr : asmv[s]) { L.asm_e.push_back(pr.first); L.asm_pos.push_back(pr.second); }
+        L.asm_ptr[s + 1] = (long long)L.asm_e.size();
+    }
+    // task list for the numeric factorisation, in topological order
+    L.fr_cv_off.assign(ns + 1, 0);
+    L.task_type.clear();
+    L.task_front.clear();
+    L.task_b0.clear();
+    L.task_b1.clear();
+    L.fr_task0.assign(ns, 0);
+    L.fr_nb.assign(ns, 0);
+    for (int s = 0; s < ns; ++s) {
+        const int m = (int)(L.fr_ptr[s + 1] - L.fr_ptr[s]);
+        const int w = L.fr_w[s], r = m - w;
+        L.fr_cv_off[s + 1] = L.fr_cv_off[s] + r;
+        L.fr_task0[s] = (int)L.task_type.size();
+        if (m <= SMALL_FRONT) {
+            L.task_type.push_back(TASK_SMALL);
+            L.task_front.push_back(s);
+            L.task_b0.push_back(0);
+            L.task_b1.push_back(0);
+            continue;
+        }
+        const int nb = (r + FRONT_TILE - 1) / FRONT_TILE;
+        L.fr_nb[s] = nb;
+        L.task_type.push_back(TASK_DIAG);
+        L.task_front.push_back(s);
+        L.task_b0.push_back(0);
+        L.task_b1.push_back(0);
+        for (int b = 0; b < nb; ++b) {
+            L.task_type.push_back(TASK_PANEL);
+            L.task_front.push_back(s);
+            L.task_b0.push_back(b);
+            L.task_b1.push_back(0);
+        }
+        for (int bj = 0; bj < nb; ++bj)
+            for (int bi = 0; bi < nb; ++bi) {
+                L.task_type.push_back(TASK_SCHUR);
+                L.task_front.push_back(s);
+                L.task_b0.push_back(bi);
+                L.task_b1.push_back(bj);
+            }
+    }
+    // large fronts: zeroed and A-assembled before the factor kernel, filled by their children
+    L.fr_big.assign(ns, 0);
+    L.big_asm_e.clear();
+    L.big_asm_pos.clear();
+    L.big_lo = L.fr_off.empty() ? 0 : L.fr_off.back();
+    L.big_hi = 0;
+    for (int s = 0; s < ns; ++s) {
+        const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s];
+        if (m <= SMALL_FRONT) continue;
+        L.fr_big[s] = 1;
+        L.big_lo = std::min(L.big_lo, L.fr_off[s]);
+        L.big_hi = std::max(L.big_hi, L.fr_off[s + 1]);
+        for (long long t = L.asm_ptr[s]; t < L.asm_ptr[s + 1]; ++t) {
+            L.big_asm_e.push_back(L.asm_e[t]);
+            L.big_asm_pos.push_back(L.fr_off[s] + L.asm_pos[t]);
+        }
+    }
+    if (L.big_hi < L.big_lo) L.big_lo = L.big_hi = 0;
+    // statistics
+    L.mf_max_m = 0;
+    L.mf_flops = 0;
+    L.mf_depth = 0;
+    std::vector<long long> depth(ns, 1);
+    for (int s = 0; s < ns; ++s) {
+        const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s], w = L.fr_w[s];
+        L.mf_max_m = std::max(L.mf_max_m, m);
+        for (long long p = 0; p < w; ++p) L.mf_flops += 2 * (m - p - 1) * (m - p - 1) + (m - p - 1);
+        if (L.sn_parent[s] >= 0) depth[L.sn_parent[s]] = std::max(depth[L.sn_parent[s]], depth[s] + 1);
+        L.mf_depth = std::max(L.mf_depth, depth[s]);
+    }
+}
+
 void build_sparse_symbolic(Circuit& c) {
     SparseLU& L = c.lu;
     const int n = c.n_aug;
@@ -326,23 +533,58 @@ void build_sparse_symbolic(Circuit& c) {
         L.qinv[L.q[i]] = i;
     }
 
-    // 5. elimination tree and row structure of L on the permuted pattern
+    // 5. elimination tree; renumber by its postorder (same fill, contiguous
+    //    subtrees, so supernodes and their chains line up), then the row
+    //    structure of L on the permuted pattern
     std::vector<std::vector<int>> low(nM);
-    for (int v = 0; v < nM; ++v) {
-        const int i = L.qinv[mlist[v]];
-        for (int u : adj[v]) {
-            const int k = L.qinv[mlist[u]];
-            if (k < i) low[i].push_back(k);
-        }
-    }
     std::vector<int> parent(nM, -1), ancestor(nM, -1);
-    for (int i = 0; i < nM; ++i) {
-        for (int k : low[i]) {
-            int r = k;
-            while (ancestor[r] != -1 && ancestor[r] != i) { int t = ancestor[r]; ancestor[r] = i; r = t; }
-            if (ancestor[r] == -1) { ancestor[r] = i; parent[r] = i; }
+    auto etree = [&]() {
+        for (auto& v : low) v.clear();
+        for (int v = 0; v < nM; ++v) {
+            const int i = L.qinv[mlist[v]];
+            for (int u : adj[v]) {
+                const int k = L.qinv[mlist[u]];
+                if (k < i) low[i].push_back(k);
+            }
         }
+        std::fill(parent.begin(), parent.end(), -1);
+        std::fill(ancestor.begin(), ancestor.end(), -1);
+        for (int i = 0; i < nM; ++i) {
+            for (int k : low[i]) {
+                int r = k;
+                while (ancestor[r] != -1 && ancestor[r] != i) { int t = ancestor[r]; ancestor[r] = i; r = t; }
+                if (ancestor[r] == -1) { ancestor[r] = i; parent[r] = i; }
+            }
+        }
+    };
+    etree();
+    {
+        std::vector<int> head(nM, -1), next(nM, -1), post;
+        post.reserve(nM);
+        for (int j = nM - 1; j >= 0; --j)
+            if (parent[j] >= 0) { next[j] = head[parent[j]]; head[parent[j]] = j; }
+        std::vector<int> stack;
+        for (int root = 0; root < nM; ++root) {
+            if (parent[root] >= 0) continue;
+            stack.push_back(root);
+            while (!stack.empty()) {
+                const int v = stack.back();
+                if (head[v] >= 0) {
+                    const int c = head[v];
+                    head[v] = next[c];
+                    stack.push_back(c);
+                } else {
+                    post.push_back(v);
+                    stack.pop_back();
+                }
+            }
+        }
+        std::vector<int> q2(nM);
+        for (int k = 0; k < nM; ++k) q2[k] = L.q[post[k]];
+        L.q = q2;
+        for (int i = 0; i < nM; ++i) L.qinv[L.q[i]] = i;
     }
+    etree();
     std::vector<std::vector<int>> rowstruct(nM);
     std::vector<int> mark(nM, -1);
     for (int i = 0; i < nM; ++i) {
@@ -389,6 +631,7 @@ void build_sparse_symbolic(Circuit& c) {
     L.f2a.assign(L.nnz_lu, -1);
     L.pre_ptr.assign(nM + 1, 0);
     std::vector<std::vector<std::pair<int, int>>> pre(nM);
+    std::vector<MEntry> m_entries;
     for (int ra = 0; ra < n; ++ra) {
         const int r = pinv_r[ra];
         if (kind[r] != 0) continue;
@@ -399,6 +642,7 @@ void build_sparse_symbolic(Circuit& c) {
                 long long s = slot_of(i, L.qinv[col]);
                 VGB_REQUIRE(s >= 0, "symbolic factor misses an entry of A");
                 L.f2a[s] = e;
+                m_entries.push_back({e, i, L.qinv[col]});
             } else if (kind[col] == 1) {
                 pre[i].push_back({e, fidx[col]});
             } else {
@@ -452,6 +696,7 @@ void build_sparse_symbolic(Circuit& c) {
             L.etree_height = std::max(L.etree_height, h[j]);
         }
     }
+    build_fronts(L, parent, lcol, m_entries);
     // 9. row access for the triangular solves
     L.lrow_ptr.assign(nM + 1, 0);
     L.lrow_pos.clear();

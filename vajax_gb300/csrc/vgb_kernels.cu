@@ -209,155 +209,13 @@ void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// Static-pivot sparse LU of the block M: sync-free left-looking factorisation.
+// Static-pivot sparse LU: singletons around the multifrontal block M.
 //
-// Column j (in elimination order) is owned by one warp.  The warp first waits,
-// lanes in parallel, until every column k in the U pattern of column j is
-// final; it then stages the column (the permuted A entries) and every update
-// operand L(i, k) with its target position in shared memory in one bulk
-// load, and runs the sequential part, x(i) -= L(i, k) * x(k) for k ascending,
-// entirely on chip.  Columns are claimed in increasing order from a global
-// counter, so every dependency (k < j) is owned by a warp that is already
-// running and the waits always end; each wait is bounded anyway.  Columns too
-// large for the shared-memory stage run the same loop on global memory.
+// B = P_r A (voltage-source transversal).  Rows of B that hold only their
+// diagonal are solved first (x_F = b_F / diag), the block M is factorised by
+// the multifrontal kernels (vgb_frontal.cu), and rows whose column holds only
+// the diagonal are solved last from their own row.
 // ---------------------------------------------------------------------------
-
-struct LUArgs {
-    int n;
-    const long long* col_ptr;
-    const int* nU;
-    const int* rows;
-    const int* f2a;
-    const long long* ustart;
-    const long long* umap_ptr;
-    const int* umap;
-    const long long* ukl;
-    const double* A;
-    int* done;
-    int* counter;
-    int* abort_flag;
-    int* err;
-    int epoch;
-    unsigned spin_limit;
-};
-
-constexpr int LU_WARPS = 4;
-constexpr int CAP_X = 256;   // column entries staged per warp
-constexpr int CAP_U = 512;   // update operands staged per warp
-constexpr int CAP_T = 128;   // U entries staged per warp
-
-template <typename T>
-struct LUSmem {
-    T x[LU_WARPS][CAP_X];
-    T lv[LU_WARPS][CAP_U];
-    int um[LU_WARPS][CAP_U];
-    int uptr[LU_WARPS][CAP_T + 1];
-};
-
-template <typename T>
-__global__ void __launch_bounds__(LU_WARPS * 32) lu_factor_kernel(LUArgs a, T* vals) {
-    __shared__ LUSmem<T> sm;
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    T* x = sm.x[w];
-    T* lv = sm.lv[w];
-    int* um = sm.um[w];
-    int* uptr = sm.uptr[w];
-    while (true) {
-        int j = 0;
-        if (lane == 0) j = atomicAdd(a.counter, 1);
-        j = __shfl_sync(0xffffffffu, j, 0);
-        if (j >= a.n) return;
-        const long long s0 = a.col_ptr[j], s1 = a.col_ptr[j + 1];
-        const int len = (int)(s1 - s0);
-        const int nu = a.nU[j];
-        const long long ub = a.ustart[j];
-        const long long M0 = a.umap_ptr[ub], M1 = a.umap_ptr[ub + nu];
-        const long long nupd = M1 - M0;
-        // 1. dependencies, waited for in parallel
-        bool ok = true;
-        for (int t = lane; t < nu; t += 32)
-            ok = ok && wait_flag(a.done + a.rows[s0 + t], a.epoch, a.abort_flag, a.err, a.spin_limit);
-        ok = __all_sync(0xffffffffu, ok);
-        const bool fits = len <= CAP_X && nupd <= CAP_U && nu <= CAP_T;
-        if (ok && fits) {
-            // 2. bulk stage: column values, update pointers, update operands
-            for (int s = lane; s < len; s += 32) {
-                const int e = a.f2a[s0 + s];
-                x[s] = e >= 0 ? (T)a.A[e] : (T)0;
-            }
-            for (int t = lane; t <= nu; t += 32) uptr[t] = (int)(a.umap_ptr[ub + t] - M0);
-            __syncwarp();
-            for (int m = lane; m < (int)nupd; m += 32) {
-                int lo = 0, hi = nu;  // largest t with uptr[t] <= m
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (uptr[mid] <= m) lo = mid; else hi = mid;
-                }
-                lv[m] = vals[a.ukl[ub + lo] + (m - uptr[lo])];
-                um[m] = a.umap[M0 + m];
-            }
-            __syncwarp();
-            // 3. sequential elimination on chip
-            for (int t = 0; t < nu; ++t) {
-                const T u = x[t];
-                if (u != (T)0)
-                    for (int m = uptr[t] + lane; m < uptr[t + 1]; m += 32) x[um[m]] -= lv[m] * u;
-                __syncwarp();
-            }
-            T piv = x[nu];
-            if (piv == (T)0 || !isfinite((double)piv)) {
-                if (lane == 0) atomicOr(a.err, DEV_ERR_PIVOT);
-                piv = (T)1e-30;
-                if (lane == 0) x[nu] = piv;
-                __syncwarp();
-            }
-            for (int s = lane; s < len; s += 32) vals[s0 + s] = s > nu ? x[s] / piv : x[s];
-        } else if (ok) {
-            // large column: same elimination on global memory
-            for (int s = lane; s < len; s += 32) {
-                const int e = a.f2a[s0 + s];
-                vals[s0 + s] = e >= 0 ? (T)a.A[e] : (T)0;
-            }
-            __syncwarp();
-            for (int t = 0; t < nu; ++t) {
-                const T u = vals[s0 + t];
-                const long long m0 = a.umap_ptr[ub + t], m1 = a.umap_ptr[ub + t + 1];
-                const long long kL = a.ukl[ub + t];
-                if (u != (T)0)
-                    for (long long m = m0 + lane; m < m1; m += 32) vals[s0 + a.umap[m]] -= vals[kL + (m - m0)] * u;
-                __syncwarp();
-            }
-            T piv = vals[s0 + nu];
-            if (piv == (T)0 || !isfinite((double)piv)) {
-                if (lane == 0) atomicOr(a.err, DEV_ERR_PIVOT);
-                piv = (T)1e-30;
-                if (lane == 0) vals[s0 + nu] = piv;
-            }
-            __syncwarp();
-            for (long long s = s0 + nu + 1 + lane; s < s1; s += 32) vals[s] = vals[s] / piv;
-        }
-        __syncwarp();
-        __threadfence();
-        if (lane == 0) st_release(a.done + j, a.epoch);
-    }
-}
-
-struct SolveArgs {
-    int n;
-    const long long* ptr;    // row access pointers
-    const long long* pos;    // slot of each entry
-    const int* col;          // dependency index of each entry
-    const long long* col_ptr;
-    const int* nU;
-    const int* q;            // backward: B index of permuted column
-    int* done;
-    int* counter;
-    int* abort_flag;
-    int* err;
-    int epoch;
-    unsigned spin_limit;
-};
 
 // Right-hand side of the block M: b restricted to M minus the couplings to the
 // singletons solved first (x_F = b_F / diag).  Also writes x_F.
@@ -379,59 +237,6 @@ __global__ void lu_pre_kernel(int nM, int nF, const int* brow, const int* pre_pt
     }
 }
 
-// L y = rhs (unit lower triangular), row-oriented, one warp per row.
-template <typename T>
-__global__ void __launch_bounds__(256) lu_fwd_kernel(SolveArgs a, const T* __restrict__ vals,
-                                                     const T* __restrict__ rhs, T* y) {
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(a.counter, 1);
-        i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= a.n) return;
-        T acc = 0;
-        for (long long e = a.ptr[i] + lane; e < a.ptr[i + 1]; e += 32) {
-            const int k = a.col[e];
-            if (!wait_flag(a.done + k, a.epoch, a.abort_flag, a.err, a.spin_limit)) break;
-            acc += vals[a.pos[e]] * ((volatile T*)y)[k];
-        }
-        for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            y[i] = rhs[i] - acc;
-            __threadfence();
-            st_release(a.done + i, a.epoch);
-        }
-    }
-}
-
-// U x = y, rows processed from the last one upwards.
-template <typename T>
-__global__ void __launch_bounds__(256) lu_bwd_kernel(SolveArgs a, const T* __restrict__ vals,
-                                                     const T* __restrict__ y, T* xs, double* xout) {
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(a.counter, 1);
-        c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= a.n) return;
-        const int i = a.n - 1 - c;
-        T acc = 0;
-        for (long long e = a.ptr[i] + lane; e < a.ptr[i + 1]; e += 32) {
-            const int j = a.col[e];
-            if (!wait_flag(a.done + j, a.epoch, a.abort_flag, a.err, a.spin_limit)) break;
-            acc += vals[a.pos[e]] * ((volatile T*)xs)[j];
-        }
-        for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            const T d = vals[a.col_ptr[i] + a.nU[i]];
-            const T xi = (y[i] - acc) / d;
-            xs[i] = xi;
-            xout[a.q[i]] = (double)xi;
-            __threadfence();
-            st_release(a.done + i, a.epoch);
-        }
-    }
-}
 
 // Singletons solved last: x_c = (b_c - sum_j B(c, j) x_j) / B(c, c), one warp per row.
 __global__ void lu_post_kernel(int nL, const int* l_col, const int* l_arow, const int* l_diag_e, const int* l_ptr,
@@ -445,84 +250,19 @@ __global__ void lu_post_kernel(int nL, const int* l_col, const int* l_arow, cons
     if (lane == 0) xout[l_col[warp]] = (b[l_arow[warp]] - acc) / A[l_diag_e[warp]];
 }
 
-static int persistent_blocks(int per_sm) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        sms = std::max(1, sms);
-    }
-    return sms * per_sm;
-}
 
-static unsigned spin_limit_default() { return 1u << 24; }
-
-void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
-    SparseLU& L = c.lu;
-    if (L.nM == 0) return;
-    L.epoch++;
-    VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
-    LUArgs a{};
-    a.n = L.nM;
-    a.col_ptr = L.d_col_ptr.p;
-    a.nU = L.d_nU.p;
-    a.rows = L.d_rows.p;
-    a.f2a = L.d_f2a.p;
-    a.ustart = L.d_ustart.p;
-    a.umap_ptr = L.d_umap_ptr.p;
-    a.umap = L.d_umap.p;
-    a.ukl = L.d_ukl.p;
-    a.A = A;
-    a.done = L.d_done.p;
-    a.counter = L.d_counters.p;
-    a.abort_flag = L.d_counters.p + 3;
-    a.err = &c.d_status.p->dev_err;
-    a.epoch = L.epoch;
-    a.spin_limit = spin_limit_default();
-    const int threads = LU_WARPS * 32;
-    const int blocks = std::min(persistent_blocks(fp32 ? 8 : 5), ceil_div((long long)L.nM * 32, threads));
-    if (fp32) lu_factor_kernel<float><<<blocks, threads, 0, s>>>(a, L.d_vals32.p);
-    else lu_factor_kernel<double><<<blocks, threads, 0, s>>>(a, L.d_vals64.p);
-    VGB_CUDA(cudaGetLastError());
-}
+void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) { mf_factor(c, A, fp32, s); }
 
 template <typename T>
-static void lu_solve_once(Circuit& c, const T* vals, const double* A, const double* rhs, double* x, T* rhsM, T* ybuf,
-                          T* xbuf, cudaStream_t s) {
+static void lu_solve_once(Circuit& c, const double* A, const double* rhs, double* x, T* rhsM, T* ybuf, T* xbuf,
+                          cudaStream_t s) {
     SparseLU& L = c.lu;
     const int nM = L.nM, nF = (int)L.f_col.size(), nL = (int)L.l_col.size();
     if (nM + nF)
         lu_pre_kernel<T><<<ceil_div(nM + nF, 256), 256, 0, s>>>(nM, nF, L.d_brow.p, L.d_pre_ptr.p, L.d_pre_e.p,
                                                                 L.d_pre_f.p, L.d_f_col.p, L.d_f_arow.p,
                                                                 L.d_f_diag_e.p, A, rhs, rhsM, x);
-    if (nM) {
-        L.epoch++;
-        VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
-        const int blocks = std::min(persistent_blocks(8), ceil_div((long long)nM * 32, 256));
-        SolveArgs f{};
-        f.n = nM;
-        f.ptr = L.d_lrow_ptr.p;
-        f.pos = L.d_lrow_pos.p;
-        f.col = L.d_lrow_col.p;
-        f.col_ptr = L.d_col_ptr.p;
-        f.nU = L.d_nU.p;
-        f.q = L.d_q.p;
-        f.done = L.d_done.p + nM;
-        f.counter = L.d_counters.p + 1;
-        f.abort_flag = L.d_counters.p + 3;
-        f.err = &c.d_status.p->dev_err;
-        f.epoch = L.epoch;
-        f.spin_limit = spin_limit_default();
-        lu_fwd_kernel<T><<<blocks, 256, 0, s>>>(f, vals, rhsM, ybuf);
-        SolveArgs b = f;
-        b.ptr = L.d_urow_ptr.p;
-        b.pos = L.d_urow_pos.p;
-        b.col = L.d_urow_col.p;
-        b.done = L.d_done.p + 2 * (size_t)nM;
-        b.counter = L.d_counters.p + 2;
-        lu_bwd_kernel<T><<<blocks, 256, 0, s>>>(b, vals, ybuf, xbuf, x);
-    }
+    if (nM) mf_solve_t<T>(c, rhsM, ybuf, xbuf, x, s);
     if (nL)
         lu_post_kernel<<<ceil_div((long long)nL * 32, 256), 256, 0, s>>>(nL, L.d_l_col.p, L.d_l_arow.p,
                                                                         L.d_l_diag_e.p, L.d_l_ptr.p, L.d_l_e.p,
@@ -554,20 +294,18 @@ void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp
     const int nM = std::max(L.nM, 1);
     if (!fp32) {
         double* rhsM = c.d_work.p;
-        double* ybuf = c.d_work.p + nM;
-        double* xbuf = c.d_work.p + 2 * (size_t)nM;
-        lu_solve_once<double>(c, L.d_vals64.p, A, rhs, x, rhsM, ybuf, xbuf, s);
+        lu_solve_once<double>(c, A, rhs, x, rhsM, c.d_work.p + nM, c.d_work.p + 2 * (size_t)nM, s);
         return;
     }
     float* rhsM = (float*)c.d_work.p;
     float* ybuf = rhsM + nM;
     float* xbuf = ybuf + nM;
-    lu_solve_once<float>(c, L.d_vals32.p, A, rhs, x, rhsM, ybuf, xbuf, s);
+    lu_solve_once<float>(c, A, rhs, x, rhsM, ybuf, xbuf, s);
     double* r = c.d_work2.p;
     double* d = c.d_work2.p + n;
     for (int k = 0; k < sweeps; ++k) {
         residual_kernel<<<ceil_div((long long)n * 32, 256), 256, 0, s>>>(n, c.d_indptr.p, c.d_indices.p, A, rhs, x, r);
-        lu_solve_once<float>(c, L.d_vals32.p, A, r, d, rhsM, ybuf, xbuf, s);
+        lu_solve_once<float>(c, A, r, d, rhsM, ybuf, xbuf, s);
         axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, x);
     }
 }

@@ -37,7 +37,12 @@ void launch_nr_reduce(const NRUpdateArgs& a, cudaStream_t s);
 void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s);
 void launch_status_reset(NRStatus* st, cudaStream_t s);
 
-// Sparse LU (static pivoting, sync-free left-looking)
+// Multifrontal factorisation and solves of the block M (vgb_frontal.cu)
+void mf_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s);
+template <typename T>
+void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream_t s);
+
+// Sparse LU (static pivoting): singletons + multifrontal block
 void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s);
 // Solve J x = rhs for x (all double, device); fp32 uses FP32 factors with
 // FP64-residual refinement sweeps.

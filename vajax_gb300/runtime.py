@@ -107,10 +107,17 @@ class DeviceCircuit:
 
     # ---- pattern and maps -------------------------------------------------
     def solver_info(self) -> Dict[str, int]:
-        out = np.zeros(8, np.int64)
+        out = np.zeros(16, np.int64)
         self._check(self.lib.vgb_solver_info(self.h, out.ctypes.data_as(_lib.i64p)))
-        keys = ["n_aug", "nnz", "nnz_lu", "lu_flops", "etree_height", "max_col", "crit_path", "contrib_slots"]
+        keys = ["n_aug", "nnz", "nnz_lu", "lu_flops", "etree_height", "max_col", "crit_path", "contrib_slots",
+                "supernodes", "max_front", "front_storage", "front_flops", "front_depth"]
         return dict(zip(keys, map(int, out)))
+
+    def solver_order(self):
+        perm_r = np.zeros(max(self.n_aug, 1), np.int32)
+        order = np.zeros(max(self.n_aug, 1), np.int32)
+        self._check(self.lib.vgb_solver_order(self.h, _ip(perm_r), _ip(order)))
+        return perm_r[: self.n_aug], order[: self.n_aug]
 
     def pattern(self):
         indptr = np.zeros(self.n_aug + 1, np.int32)
