@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Transient ms/step of the ~80k-transistor random gate network on one GB300.
+
+Workload: seeded random static-CMOS network, 23,530 gates (inverter / NAND2 /
+NOR2 / NAND3 = 40/30/20/10 %, 79,960 EKV transistors), logic depth 60, 32
+primary inputs driven by PWL sources with seeded random bits, 50 ps edges,
+0.5 ns period, 5 fF per net; adaptive BDF2 (gear2) from the DC operating
+point, reltol 1e-3, abstol 1e-12, FP64 throughout.
+
+A bench step is one accepted adaptive transient step: device evaluation,
+stamping, sparse LU refactorisation and solve for every Newton iteration of
+the step, plus the predictor, LTE and step control.  ms/step is the
+reference's metric (wall time / accepted steps, full_mna.py:1142-1176).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference path (the oracle; the reference's JAX path cannot be installed
+here) on the host cores.  Under torchrun each rank runs an independent
+replica (the path does not shard within one circuit); rank 0 prints.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(workload="random_gate_network_80k_transistors_adaptive_bdf2", gates=23530, depth=60, n_inputs=32,
+                seed=1, c_wire=5e-15, period=0.5e-9, edge=50e-12, t_stop=20e-9, dt0=1e-12, method="gear2",
+                model="ekv")
+L2_BYTES = 129 * 2 ** 20
+STATUS_BYTES = 48  # NRStatus read back per Newton iteration
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_engine_host(gates: int):
+    """Engine over the seeded network, parsed and configured, no GPU touched."""
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions
+    from vajax_gb300.generators import random_gate_network
+    w = WORKLOAD
+    depth = w["depth"] if gates >= 20 * w["depth"] else max(4, gates // 20)
+    c, stats = random_gate_network(n_gates=gates, depth=depth, n_inputs=w["n_inputs"], seed=w["seed"],
+                                   c_wire=w["c_wire"], period=w["period"], edge=w["edge"])
+    eng = CircuitEngine(c, SimulationOptions(tran_method=w["method"]))
+    eng.parse()
+    eng.t_stop, eng.dt = w["t_stop"], w["dt0"]
+    eng.config = eng._config(w["t_stop"], w["dt0"], None)
+    eng.max_steps = 2
+    return eng, stats, depth
+
+
+def make_engine(gates: int, max_steps: int):
+    eng, stats, depth = make_engine_host(gates)
+    w = WORKLOAD
+    eng.prepare(t_stop=w["t_stop"], dt=w["dt0"], max_steps=max_steps)
+    return eng, stats, depth
+
+
+# ---------------------------------------------------------------------------
+# clocks (nvidia-smi sampled during the timed region)
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.2)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t is not None:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gpu_index(local_rank: int) -> int:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if local_rank < len(ids) and ids[local_rank].isdigit():
+            return int(ids[local_rank])
+    return local_rank
+
+
+# ---------------------------------------------------------------------------
+# roofline inputs
+# ---------------------------------------------------------------------------
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    p = ROOT / "profiles" / "dram_traffic.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        f = ln.split()
+        if len(f) >= 3 and not ln.startswith("#") and f[0] == kernel and f[1] == workload:
+            return float(f[2])
+    return None
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_gb300(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    K, W = args.steps, args.warmup
+    prof_steps = 2
+    eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4)
+    dev = eng.device
+    info = dev.solver_info()
+    t0 = time.perf_counter()
+    X0, Q0, I0, maxc0, dc_ok = eng.initial_state()
+    dc_s = time.perf_counter() - t0
+    if not dc_ok:
+        raise RuntimeError(f"DC operating point did not converge ({eng.dc_method})")
+    cfg = eng.transient_cfg()
+    sess = dev.session(cfg, X0, Q0, I0, maxc0)
+    for _ in range(W):
+        sess.advance(1)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    sampler = ClockSampler(gpu_index(local))
+    sampler.start()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    st0 = sess.stats()
+    dev_ms = 0.0
+    wall0 = time.perf_counter()
+    for _ in range(K):
+        flush.zero_()  # L2 flush between timed steps (outside the step's device time)
+        torch.cuda.synchronize()
+        a = sess.stats()[5]
+        got = sess.advance(1)
+        if got != 1:
+            raise RuntimeError("transient ended before the timed steps finished")
+        dev_ms += sess.stats()[5] - a
+    torch.cuda.synchronize()
+    wall_s = time.perf_counter() - wall0
+    if pg:
+        pg.barrier()
+    clocks = sampler.stop()
+    st1 = sess.stats()
+    nr_iters = int(st1[2] - st0[2])
+    launches = int(st1[7] - st0[7])
+    rejected = int(st1[1] - st0[1])
+    if pg:
+        t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_per_step = dev_ms / K
+    value = dev_ms / (K * world)  # whole-job: all replicas' steps over the slowest rank's time
+
+    # per-phase split on two more steps (CUDA events on the library's stream)
+    dev.profile(1)
+    sess.advance(prof_steps)
+    prof = dev.profile(-1)
+    dev.profile(0)
+    its = max(prof["iterations"], 1)
+    phase = {k: prof[k] / its for k in ("eval_ms", "assemble_ms", "factor_ms", "solve_ms", "update_ms")}
+    sess.close()
+
+    # roofline of the dominant kernel: the multifrontal refactorisation
+    # (mf_factor_kernel); algorithmic bytes = nnz(L+U) x (8 B value read +
+    # 8 B value write + 4 B index)
+    peak, peak_kind = measured_peaks()
+    fac_bytes = info["nnz_lu"] * 20
+    fac_ms = phase["factor_ms"]
+    achieved = fac_bytes / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0
+    work = f"gates{args.gates}"
+    roofline = {"kernel": "mf_factor_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic("mf_factor_kernel", work),
+                "algorithmic_bytes_per_launch": fac_bytes,
+                "fp64_gflops": info["front_flops"] / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0}
+
+    # end to end through the public API: CircuitEngine.run_transient (host
+    # buffers in and out, wall time / accepted steps of the transient call)
+    e2e = None
+    if rank == 0 or world > 1:
+        eng.max_steps = K + 1
+        r = eng.run_transient()
+        acc = max(r.stats["n_steps"] - 1, 1)  # row 0 is the initial point
+        n_x = len(X0)
+        h2d = (n_x + 3 * dev.n_unk + dev.n_vsrc + 22) * 8
+        d2h = r.stats["n_steps"] * (8 + 8 * eng.rc.n_external + 8 * max(dev.n_vsrc, 1)) + \
+            STATUS_BYTES * r.stats["total_nr_iterations"]
+        e2e = {"value": r.stats["wall_time"] * 1e3 / acc, "unit": "ms/step", "h2d_bytes_per_step": h2d / acc,
+               "d2h_bytes_per_step": d2h / acc, "steps": acc}
+
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu = cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg)
+
+    out = {"metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world, "steps": K,
+           "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "config": {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors,
+                      "depth": depth, "n_unknowns": info["n_aug"], "nnz": info["nnz"], "nnz_lu": info["nnz_lu"],
+                      "front_flops": info["front_flops"], "seed": WORKLOAD["seed"],
+                      "parallelism": f"replicas{world}", "l2": "flushed (2x L2 write) before every timed step",
+                      "dc_seconds": dc_s, "dc_method": eng.dc_method},
+           "newton_iters_per_s": nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
+           "newton_iters": nr_iters, "rejected_steps": rejected, "host_wall_ms_per_step": wall_s * 1e3 / K,
+           "phase_ms_per_newton_iter": phase, "gpu_launches": launches, "roofline": roofline,
+           "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def _oracle_system(eng, threads=1):
+    from oracle.mna import OracleSystem
+    from vajax_gb300.devices import load_model
+    rc = eng.rc
+    return OracleSystem(rc, {g.model: load_model(g.model) for g in rc.groups}, gmin=eng.options.gmin,
+                        threads=threads)
+
+
+def cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg, steps=1):
+    """The oracle (CPU restatement of the reference path) timed on the host
+    on the first `steps` accepted steps from the same DC state."""
+    from oracle.transient import run_transient
+    S = _oracle_system(eng)
+    c = dict(cfg)
+    c["max_steps"] = steps + 1
+    t0 = time.perf_counter()
+    o = run_transient(S, c, X0, Q0, I0, maxc0)
+    wall = time.perf_counter() - t0
+    acc = max(o["n_steps"] - 1, 1)
+    return {"value": wall * 1e3 / acc, "unit": "ms/step", "cores": 1, "kind": "port",
+            "sample": f"first {acc} accepted adaptive step(s) from the DC point, full network, numpy + SuperLU"}
+
+
+def run_reference(args):
+    """CPU arm: the oracle restatement of the reference's transient path on
+    the host cores, same workload and metric.  Each step is one accepted
+    adaptive step; the count is capped so that the run stays within a few
+    minutes (a step of the full network takes tens of seconds on the CPU)."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    from oracle.dc import dc_operating_point
+    from oracle.transient import run_transient
+    K, W = args.steps, args.warmup
+    eng, nstats, depth = make_engine_host(args.gates)
+    S = _oracle_system(eng, threads=threads)
+    rc = eng.rc
+    X0 = np.zeros(rc.n_nodes + len(rc.vsources))
+    X0[: rc.n_nodes] = eng.initial_guess()
+    r = dc_operating_point(S, rc.source_values(0.0), X0)
+    if not r["converged"]:
+        print(json.dumps({"impl": "reference", "unavailable": "oracle DC operating point did not converge"}))
+        return
+    cfg = eng.transient_cfg()
+    budget_s = args.reference_budget
+    # one untimed warm-up step, then timed steps until K or the time budget
+    c = dict(cfg)
+    steps_done = 0
+    t_first = time.perf_counter()
+    c["max_steps"] = 2
+    run_transient(S, c, r["X"], r["Q"], r["I_vsource"], r["max_res_contrib"])
+    est = time.perf_counter() - t_first
+    k_run = int(max(1, min(K, budget_s // max(est, 1e-3))))
+    c["max_steps"] = k_run + 1
+    t0 = time.perf_counter()
+    o = run_transient(S, c, r["X"], r["Q"], r["I_vsource"], r["max_res_contrib"])
+    wall = time.perf_counter() - t0
+    steps_done = max(o["n_steps"] - 1, 1)
+    value = wall * 1e3 / steps_done
+    sample = (f"{steps_done} accepted adaptive steps from the DC point (cap {budget_s:.0f} s), full network, "
+              f"oracle numpy + SuperLU, {min(1, W)} warm-up step")
+    out = {"impl": "reference", "metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world,
+           "steps": steps_done, "warmup": min(1, W), "ms_per_step": value, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "config": {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors,
+                      "depth": depth, "seed": WORKLOAD["seed"], "parallelism": "host"},
+           "cpu_baseline": {"value": value, "unit": "ms/step", "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
+    ap.add_argument("--reference-budget", type=float, default=150.0, help="seconds of timed CPU work, reference arm")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -141,7 +141,11 @@ int vgb_eval_group(void* h, int group, const double* X, double* out, vgb_stream_
 int vgb_linear_solve(void* h, const double* csr_vals, const double* rhs, double* x, vgb_stream_t stream);
 
 /* Newton solve from X (device, updated in place).  opts = {c0, c1, d1, c2,
- * gshunt, reltol, abstol, vntol, damping, max_step}; res_tol_floor (device,
+ * gshunt, reltol, abstol, vntol, damping, max_step, node_limit}: max_step
+ * scales the whole node update down to at most max_step volts (reference
+ * semantics); node_limit > 0 (extension, 0 = off) clips each node's update to
+ * +-node_limit volts, the SPICE node-voltage limiting used by the DC
+ * operating-point solve of circuits without model $limit; res_tol_floor (device,
  * n_unknowns) may be NULL for abstol.  Outputs (host): iterations,
  * converged, max_f.  Q_out/dQdt_out/I_vsrc/maxc_out are device pointers
  * (may be NULL) filled from the post-convergence rebuild, as nr_solve does
@@ -166,6 +170,31 @@ int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc
  *             device_ms, nr_failures, kernel_launches}. */
 int vgb_transient(void* h, const double* cfg, const double* X0, const double* Q0, const double* I0,
                   const double* maxc0, double* times, double* V_out, double* I_out, double* stats);
+
+/* Resumable transient session on circuit h: vgb_transient split into
+ * create / advance / read / destroy, so that a caller can run a transient in
+ * slices (a step-timed benchmark, a serving loop that interleaves jobs).
+ * vgb_transient(...) equals create + advance(0) + read + destroy.  The state
+ * (solution, charge history, predictor history, step controller) lives in the
+ * session; the circuit's Newton scratch is shared, so calls on sessions of
+ * one circuit must not overlap.  Errors are reported on the circuit handle
+ * (vgb_last_error(h)).  No counterpart in the reference, whose run() is one
+ * call (full_mna.py:1792-2196).
+ *   create:  cfg/X0/Q0/I0/maxc0 as vgb_transient (host memory, copied).
+ *   advance: run until max_accepted more steps are accepted (0 = to the end);
+ *            *accepted = steps accepted in this call, *done = 1 once the run
+ *            reached t_stop or max_steps (either may be NULL).
+ *   read:    times[n], V_out[n][n_external], I_out[n][max(n_vsrc,1)] for the
+ *            n = stats[0] output rows so far (any may be NULL); stats[8] as
+ *            vgb_transient, device_ms and kernel_launches summed over advances.
+ *   state:   current solution X[n_nodes+n_vsrc] and charges Q[n_nodes-1]
+ *            (host memory, either may be NULL). */
+int vgb_tran_create(void* h, const double* cfg, const double* X0, const double* Q0, const double* I0,
+                    const double* maxc0, void** out_session);
+int vgb_tran_advance(void* session, int max_accepted, int* accepted, int* done);
+int vgb_tran_read(void* session, double* times, double* V_out, double* I_out, double* stats);
+int vgb_tran_state(void* session, double* X, double* Q);
+int vgb_tran_destroy(void* session);
 
 #ifdef __cplusplus
 }

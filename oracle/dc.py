@@ -76,11 +76,17 @@ def source_stepping(S, vs, X0, itl=20, step=0.1, step_min=0.001, scale=2.0, max_
     return X_good, False
 
 
-def dc_operating_point(S, vs, X0, itl=20):
-    """Plain Newton, then gshunt stepping, then source stepping; final Newton at the result."""
+def dc_operating_point(S, vs, X0, itl=20, node_limit=0.3, node_limit_itl=100):
+    """Plain Newton, then Newton with a per-node step clip (the product's
+    extension, skipped when node_limit is 0), then gshunt stepping, then source
+    stepping; final plain Newton at the result."""
     r = nr_solve(S, np.array(X0, np.float64), vs, max_iterations=itl)
     if r["converged"] and np.all(np.isfinite(r["X"])):
         return r
+    if node_limit > 0:
+        r = nr_solve(S, np.array(X0, np.float64), vs, max_iterations=node_limit_itl, node_limit=node_limit)
+        if r["converged"] and np.all(np.isfinite(r["X"])):
+            return nr_solve(S, r["X"], vs, max_iterations=itl)
     X, ok = gshunt_stepping(S, vs, X0, itl=itl)
     if not ok:
         X, ok = source_stepping(S, vs, X0, itl=itl)

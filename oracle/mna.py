@@ -65,9 +65,13 @@ class OracleModel:
 class OracleSystem:
     """build_system of the reference for one resolved circuit."""
 
-    def __init__(self, rc, models: Dict[str, dict], gmin: float = 1e-12):
+    def __init__(self, rc, models: Dict[str, dict], gmin: float = 1e-12, threads: int = 1):
         self.rc = rc
         self.gmin = gmin
+        # device evaluation splits the instances of a group over this many
+        # threads (numpy releases the GIL inside its array loops)
+        self.threads = max(1, int(threads))
+        self._pool = None
         self.n_nodes = rc.n_nodes
         self.n_unk = rc.n_nodes - 1
         self.n_vsrc = len(rc.vsrc_p)
@@ -149,7 +153,18 @@ class OracleSystem:
     def eval_group(self, gi: int, X: np.ndarray):
         g = self.groups[gi]
         V_nodes = X[g["node_map"]]
-        return g["model"].eval(g["params"], g["temps"], V_nodes)
+        n = V_nodes.shape[1]
+        if self.threads == 1 or n < 4096:
+            return g["model"].eval(g["params"], g["temps"], V_nodes)
+        if self._pool is None:
+            from concurrent.futures import ThreadPoolExecutor
+            self._pool = ThreadPoolExecutor(self.threads)
+        cuts = np.linspace(0, n, self.threads + 1).astype(int)
+        temps = np.broadcast_to(np.asarray(g["temps"], np.float64), (n,))
+        parts = list(self._pool.map(
+            lambda ab: g["model"].eval(g["params"][:, ab[0]:ab[1]], temps[ab[0]:ab[1]], V_nodes[:, ab[0]:ab[1]]),
+            zip(cuts[:-1], cuts[1:])))
+        return tuple(np.concatenate([p[k] for p in parts], 0) for k in range(4))
 
     # ---- build_system (mna_builder.py:759-1076) ----------------------------
     def build_system(self, X, vsrc_vals, isrc_vals=None, Q_prev=None, c0=0.0, gshunt=0.0, c1=0.0, d1=0.0,
@@ -228,12 +243,15 @@ class OracleSystem:
         import scipy.sparse as sp
         import scipy.sparse.linalg as spl
         A = sp.csr_matrix((csr, self.indices, self.indptr), shape=(self.n_aug, self.n_aug)).tocsc()
-        return spl.splu(A).solve(rhs)
+        # minimum degree on A^T + A: circuit matrices are nearly structurally
+        # symmetric, and COLAMD fills far more on the large gate networks
+        return spl.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.01).solve(rhs)
 
 
 def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None, c0=0.0, gshunt=0.0, c1=0.0,
              d1=0.0, dQdt_prev=None, c2=0.0, Q_prev2=None, res_tol_floor=None, max_iterations=20, reltol=1e-3,
-             abstol=1e-12, vntol=1e-6, nr_damping=1.0, max_step=1e30, conv_mask: Optional[np.ndarray] = None):
+             abstol=1e-12, vntol=1e-6, nr_damping=1.0, max_step=1e30, conv_mask: Optional[np.ndarray] = None,
+             node_limit: float = 0.0):
     """solver_factories.py:140-325 + while-loop nr_solve (:526-725)."""
     n_unk, n_v = sys_.n_unk, sys_.n_vsrc
     X = np.array(X_init, dtype=np.float64)
@@ -257,7 +275,10 @@ def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None,
         dV = delta[:n_unk]
         max_dv = float(np.max(np.abs(dV))) if n_unk else 0.0
         scale = min(1.0, max_step / max(max_dv, 1e-30))
-        X[1:sys_.n_nodes] += dV * scale * nr_damping
+        step = dV * scale * nr_damping
+        if node_limit > 0.0:  # per-node clip (extension; the reference has only max_step)
+            step = np.clip(step, -node_limit, node_limit)
+        X[1:sys_.n_nodes] += step
         X[sys_.n_nodes:] += delta[n_unk:]
         converged = residual_converged and delta_converged
         it += 1

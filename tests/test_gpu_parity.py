@@ -166,7 +166,8 @@ def test_newton_divider(cuda):
 
 @pytest.mark.parametrize("name,make", CIRCUITS[1:])
 def test_dc_operating_point_matches_oracle(cuda, name, make):
-    """Mid-rail start, plain Newton, then the gshunt / source-stepping homotopy."""
+    """Mid-rail / nodeset start, plain Newton, node-limited Newton, then the
+    gshunt / source-stepping homotopy."""
     from oracle.dc import dc_operating_point
     from vajax_gb300.engine import CircuitEngine
     c = make()
@@ -175,12 +176,31 @@ def test_dc_operating_point_matches_oracle(cuda, name, make):
     eng.device = _pair(c)[1]
     S = OracleSystem(rc, {g.model: load_model(g.model) for g in rc.groups})
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
-    X0[: rc.n_nodes] = eng.init_mid_rail()
+    X0[: rc.n_nodes] = eng.initial_guess()
     Xg, Qg, Ig, maxcg, ok = eng.initial_state()
     ro = dc_operating_point(S, rc.source_values(0.0), X0)
     assert ok and ro["converged"]
     assert np.max(np.abs(Xg[: rc.n_nodes] - ro["X"][: rc.n_nodes])) < 1e-9
     _close(Qg, ro["Q"], rel=1e-9)
+
+
+def test_node_limited_newton_matches_oracle(cuda):
+    """Newton with the per-node step clip from the logic nodeset of a 500-gate
+    network: same iteration count and operating point as the oracle."""
+    import torch
+    from vajax_gb300.engine import CircuitEngine
+    c, _ = random_gate_network(n_gates=500, depth=12, n_inputs=32, seed=1)
+    rc, dc, S = _pair(c)
+    eng = CircuitEngine(c).parse()
+    X0 = np.zeros(rc.n_nodes + len(rc.vsources))
+    X0[: rc.n_nodes] = eng.initial_guess()
+    vs = rc.source_values(0.0)
+    ro = nr_solve(S, X0.copy(), vs, max_iterations=100, node_limit=0.3)
+    r = dc.nr_solve(torch.as_tensor(X0.copy(), device=cuda), torch.as_tensor(vs, device=cuda), max_iter=100,
+                    node_limit=0.3)
+    assert ro["converged"] and r["converged"]
+    assert r["iterations"] == ro["iterations"]
+    assert np.max(np.abs(r["X"].cpu().numpy() - ro["X"])) < 1e-9
 
 
 def _cfg(rc, fixed, t_stop, dt, max_steps, method=2):
@@ -232,3 +252,29 @@ def test_adaptive_network_matches_oracle(cuda):
     assert g["rejected"] == o["rejected"]
     np.testing.assert_allclose(g["times"], o["times"], rtol=1e-9)
     assert np.max(np.abs(g["V"] - o["V"])) < 1e-6
+
+
+def test_transient_session_slices_match_one_call(cuda):
+    """vgb_tran_* in slices of 7 accepted steps reproduces vgb_transient bit for bit."""
+    rc, dc, S = _pair(_small_network(seed=7, gates=60))
+    from vajax_gb300.engine import CircuitEngine
+    eng = CircuitEngine(_small_network(seed=7, gates=60)).parse()
+    X0 = np.zeros(rc.n_nodes + len(rc.vsources))
+    X0[: rc.n_nodes] = eng.initial_guess()
+    from oracle.dc import dc_operating_point
+    ro = dc_operating_point(S, rc.source_values(0.0), X0.copy())
+    cfg = _cfg(rc, False, 2e-9, 0.25e-12, 41)
+    cfg["max_dt"] = 2e-9 / 50
+    args = (ro["X"], ro["Q"], ro["I_vsource"], ro["max_res_contrib"])
+    one = dc.transient(cfg, *args)
+    sess = dc.session(cfg, *args)
+    total = 0
+    while not sess.done:
+        total += sess.advance(7)
+    sl = sess.read()
+    sess.close()
+    assert sl["n_steps"] == one["n_steps"] == 41
+    assert total == 40
+    assert np.array_equal(sl["times"], one["times"]) and np.array_equal(sl["V"], one["V"])
+    assert np.array_equal(sl["I"], one["I"])
+    assert sl["rejected"] == one["rejected"] and sl["total_nr_iters"] == one["total_nr_iters"]

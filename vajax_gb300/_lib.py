@@ -46,6 +46,11 @@ SIGNATURES = {
     "vgb_nr_solve": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, f64p, C.c_int, i32p, i32p, f64p,
                                vp, vp, vp, vp, vp]),
     "vgb_transient": (C.c_int, [vp, f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p]),
+    "vgb_tran_create": (C.c_int, [vp, f64p, f64p, f64p, f64p, f64p, C.POINTER(vp)]),
+    "vgb_tran_advance": (C.c_int, [vp, C.c_int, i32p, i32p]),
+    "vgb_tran_read": (C.c_int, [vp, f64p, f64p, f64p, f64p]),
+    "vgb_tran_state": (C.c_int, [vp, f64p, f64p]),
+    "vgb_tran_destroy": (C.c_int, [vp]),
 }
 
 

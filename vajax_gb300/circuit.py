@@ -168,6 +168,8 @@ class Circuit:
         self.isources: List[Source] = []
         self.temperature = temperature
         self.ground = "0"
+        # SPICE-style .nodeset: initial guesses (volts) for the DC Newton solve
+        self.nodeset: Dict[str, float] = {}
 
     def add(self, name: str, model: str, nodes: Sequence[str], temperature: Optional[float] = None, **params):
         info = model_info(model)

@@ -72,6 +72,7 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
     u.abstol = o.abstol;
     u.damping = o.damping;
     u.max_step = o.max_step;
+    u.node_limit = o.node_limit;
     u.st = c.d_status.p;
     const bool prof = c.profile;
     for (int it = 0; it < max_iter; ++it) {
@@ -610,6 +611,7 @@ int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc
         o.vntol = opts[7];
         o.damping = opts[8];
         o.max_step = opts[9];
+        o.node_limit = opts[10];
         DefaultVecs dv = defaults_for(*c, o.abstol, s);
         const double* z = dv.zeros;
         const double* vs = vsrc_vals ? vsrc_vals : z;

@@ -100,6 +100,7 @@ inline void linear_solve(Circuit& c, const double* csr, const double* rhs, doubl
 
 struct NROpts {
     double reltol = 1e-3, abstol = 1e-12, vntol = 1e-6, damping = 1.0, max_step = 1e30;
+    double node_limit = 0.0;
 };
 
 struct NRResult {

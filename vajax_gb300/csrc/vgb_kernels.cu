@@ -195,7 +195,9 @@ __global__ void nr_apply_kernel(NRUpdateArgs a) {
     if (i < a.n_unk) {
         const double max_dv = __longlong_as_double((long long)a.st->max_dv);
         const double scale = fmin(1.0, a.max_step / fmax(max_dv, 1e-30));
-        a.X[i + 1] += d * scale * a.damping;
+        double dv = d * scale * a.damping;
+        if (a.node_limit > 0.0) dv = fmin(fmax(dv, -a.node_limit), a.node_limit);
+        a.X[i + 1] += dv;
     } else {
         a.X[i + 1] += d;
     }

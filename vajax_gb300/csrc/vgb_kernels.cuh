@@ -31,6 +31,7 @@ struct NRUpdateArgs {
     const double* delta;
     double* X;
     double reltol, vntol, abstol, damping, max_step;
+    double node_limit;  // > 0: clip each node's update to +-node_limit volts
     NRStatus* st;
 };
 void launch_nr_reduce(const NRUpdateArgs& a, cudaStream_t s);

@@ -44,6 +44,10 @@ class SimulationOptions:
     icmode: str = "op"
     fixed_step_transient: bool = False
     maxstep: Optional[float] = None
+    # extension: per-node Newton step clip (volts) for the DC retry when plain
+    # Newton fails; 0 disables the retry
+    dc_node_limit: float = 0.3
+    dc_node_limit_itl: int = 100
     # extension: per-node initial conditions used with icmode='uic'
     ic: Dict[str, float] = field(default_factory=dict)
 
@@ -166,6 +170,20 @@ class CircuitEngine:
                 V[p] = s.dc_value()
         return V
 
+    def initial_guess(self) -> np.ndarray:
+        """Mid-rail start overridden by the circuit's ``.nodeset`` guesses
+        (extension: the reference has no nodeset and always starts DC from
+        mid-rail, full_mna.py:694-745)."""
+        V = self.init_mid_rail()
+        for node, v in self.circuit.nodeset.items():
+            idx = self.rc.node_names.get(node)
+            if idx is not None and idx > 0:
+                V[idx] = v
+        for s, p, n in zip(self.rc.vsources, self.rc.vsrc_p, self.rc.vsrc_n):
+            if n == 0 and p > 0:
+                V[p] = s.value(0.0)
+        return V
+
     def initial_state(self):
         import torch
         rc = self.rc
@@ -182,20 +200,26 @@ class CircuitEngine:
             I0 = np.where(rc.vsrc_p > 0, -fres.cpu().numpy()[np.maximum(rc.vsrc_p - 1, 0)], 0.0)
             return X0, Q.cpu().numpy(), I0, np.zeros(rc.n_nodes - 1), True
         X0 = np.zeros(n_x)
-        X0[: rc.n_nodes] = self.init_mid_rail()
+        X0[: rc.n_nodes] = self.initial_guess()
         o = self.options
 
-        def solve(X, gshunt=0.0, sf=1.0):
+        def solve(X, gshunt=0.0, sf=1.0, node_limit=0.0, itl=None):
             Xd = torch.as_tensor(np.array(X, np.float64), device="cuda")
             r = dev.nr_solve(Xd, vs0 * sf if len(rc.vsources) else None, is0 * sf if is0 is not None else None,
                              c0=0.0, gshunt=gshunt, reltol=o.reltol, abstol=o.abstol, vntol=o.vntol,
-                             damping=o.nr_damping, max_iter=o.tran_itl)
+                             damping=o.nr_damping, max_iter=itl or o.tran_itl, node_limit=node_limit)
             Xn = r["X"].cpu().numpy()
             return Xn, r["iterations"], bool(r["converged"] and np.all(np.isfinite(Xn))), r
 
-        # plain Newton from mid-rail first (full_mna.py:922-957) ...
+        # plain Newton from the initial guess first (full_mna.py:922-957) ...
         Xn, _, ok, r = solve(X0)
         self.dc_method = "newton"
+        if not ok and o.dc_node_limit > 0:
+            # ... then Newton with per-node voltage limiting (extension) ...
+            Xn, _, ok, r = solve(X0, node_limit=o.dc_node_limit, itl=o.dc_node_limit_itl)
+            self.dc_method = "newton_limited"
+            if ok:
+                Xn, _, ok, r = solve(Xn)
         if not ok and self.homotopy:
             # ... then the homotopy chain when it does not converge (homotopy.py:470-567)
             from vajax_gb300.dc import homotopy_chain

@@ -50,6 +50,33 @@ def ring_oscillator(stages: int = 7, vdd: float = 1.2, c_load: float = 10e-15, m
     return c
 
 
+def _nodeset_gate(c: Circuit, logic: Dict[str, int], g: str, kind: int, ins: List[str], out: str, vdd: float):
+    """Static logic value of the gate output and its stack nodes at t = 0.
+
+    The values seed the DC Newton solve like a SPICE ``.nodeset``: settled
+    gates put every on transistor in its linear region with Vds near 0,
+    so Newton converges in a few iterations where mid-rail starts diverge.
+    Stack nodes that no on transistor ties to a rail get a threshold drop
+    below (NMOS stacks) or above (PMOS stacks) the rail they float towards.
+    """
+    a = [logic[n] for n in ins]
+    vt = 0.4
+    if kind == 0:
+        y = 1 - a[0]
+    elif kind == 1:
+        y = 1 - (a[0] & a[1])
+        c.nodeset[f"{g}.x"] = 0.0 if a[1] else (vdd - vt if a[0] else vt)
+    elif kind == 2:
+        y = 1 - (a[0] | a[1])
+        c.nodeset[f"{g}.x"] = vdd if not a[0] else (vt if not a[1] else vdd - vt)
+    else:
+        y = 1 - (a[0] & a[1] & a[2])
+        c.nodeset[f"{g}.x2"] = 0.0 if a[2] else (vdd - vt if a[1] else vt)
+        c.nodeset[f"{g}.x1"] = 0.0 if (a[1] and a[2]) else (vdd - vt if a[0] else vt)
+    logic[out] = y
+    c.nodeset[out] = vdd * y
+
+
 @dataclass
 class NetworkStats:
     gates: int
@@ -70,6 +97,7 @@ def random_gate_network(n_gates: int = 23530, depth: int = 60, n_inputs: int = 3
     c.vsource("vdd", "vdd", "0", "dc", dc=vdd)
     # primary inputs: PWL with seeded random bits, 50 ps edges, 0.5 ns period
     levels: List[List[str]] = [[f"pi{k}" for k in range(n_inputs)]]
+    logic: Dict[str, int] = {}  # t = 0 logic value of every net, for the DC nodeset
     for k in range(n_inputs):
         bits = rng.integers(0, 2, n_periods + 1)
         wave = [0.0, vdd * bits[0]]
@@ -77,6 +105,7 @@ def random_gate_network(n_gates: int = 23530, depth: int = 60, n_inputs: int = 3
             t = p * period
             wave += [t, vdd * bits[p - 1], t + edge, vdd * bits[p]]
         c.vsource(f"vpi{k}", f"pi{k}", "0", "pwl", wave=wave)
+        logic[f"pi{k}"] = int(bits[0])
         c.add(f"cw_pi{k}", "capacitor", [f"pi{k}", "0"], c=c_wire)
     counts = per_level or [n_gates // depth + (1 if l < n_gates % depth else 0) for l in range(depth)]
     kinds = rng.choice(4, size=sum(counts), p=np.asarray(mix) / np.sum(mix))
@@ -141,6 +170,7 @@ def random_gate_network(n_gates: int = 23530, depth: int = 60, n_inputs: int = 3
                 ntrans += 6
             c.add(f"cw_{out}", "capacitor", [out, "0"], c=c_wire)
             outs.append(out)
+            _nodeset_gate(c, logic, g, kind, ins, out, vdd)
         levels.append(outs)
         keep = np.sort(rng.permutation(m)[: max(1, int(round(0.75 * m)))])
         eligible.append(keep)

@@ -174,7 +174,7 @@ class DeviceCircuit:
 
     def nr_solve(self, X, vsrc_vals=None, isrc_vals=None, Q_prev=None, dQdt_prev=None, Q_prev2=None,
                  res_tol_floor=None, c0=0.0, c1=0.0, d1=0.0, c2=0.0, gshunt=0.0, reltol=1e-3, abstol=1e-12,
-                 vntol=1e-6, damping=1.0, max_step=1e30, max_iter=20):
+                 vntol=1e-6, damping=1.0, max_step=1e30, max_iter=20, node_limit=0.0):
         import torch
         dev = X.device
         nu = max(self.n_unk, 1)
@@ -182,7 +182,8 @@ class DeviceCircuit:
         dQ = torch.empty(nu, dtype=torch.float64, device=dev)
         maxc = torch.empty(nu, dtype=torch.float64, device=dev)
         I = torch.empty(max(self.n_vsrc, 1), dtype=torch.float64, device=dev)
-        opts = np.asarray([c0, c1, d1, c2, gshunt, reltol, abstol, vntol, damping, max_step], np.float64)
+        opts = np.asarray([c0, c1, d1, c2, gshunt, reltol, abstol, vntol, damping, max_step, node_limit],
+                          np.float64)
         it, conv, mf = C.c_int(), C.c_int(), C.c_double()
         self._check(self.lib.vgb_nr_solve(self.h, _ptr(X), _ptr(vsrc_vals), _ptr(isrc_vals), _ptr(Q_prev),
                                           _ptr(dQdt_prev), _ptr(Q_prev2), _ptr(res_tol_floor), _dp(opts), max_iter,
@@ -193,11 +194,7 @@ class DeviceCircuit:
                 "max_res_contrib": maxc[: self.n_unk]}
 
     def transient(self, cfg: Dict[str, float], X0: np.ndarray, Q0=None, I0=None, maxc0=None):
-        keys = ["t_stop", "dt", "max_dt", "min_dt", "reltol", "abstol", "vntol", "lte_ratio", "redo_factor",
-                "grow_factor", "tran_ft", "nr_damping", "gshunt_init", "gshunt_target", "gshunt_steps",
-                "warmup_steps", "max_consecutive_rejects", "fixed_step", "method", "n_external", "max_steps",
-                "tran_itl"]
-        c = np.asarray([float(cfg[k]) for k in keys], np.float64)
+        c = tran_cfg_array(cfg)
         max_steps = int(cfg["max_steps"])
         n_ext = int(cfg["n_external"])
         times = np.zeros(max_steps)
@@ -210,6 +207,78 @@ class DeviceCircuit:
         self._check(self.lib.vgb_transient(self.h, _dp(c), _dp(X0), opt(keep[0]), opt(keep[1]), opt(keep[2]),
                                            _dp(times), _dp(V), _dp(I), _dp(stats)))
         n = int(stats[0])
-        return {"times": times[:n], "V": V[:n], "I": I[:n, : self.n_vsrc], "n_steps": n,
-                "rejected": int(stats[1]), "total_nr_iters": int(stats[2]), "min_dt_used": stats[3],
-                "max_dt_used": stats[4], "device_ms": stats[5], "nr_failures": int(stats[6])}
+        return _tran_result(times, V, I, stats, self.n_vsrc)
+
+    def session(self, cfg: Dict[str, float], X0: np.ndarray, Q0=None, I0=None, maxc0=None) -> "TransientSession":
+        return TransientSession(self, cfg, X0, Q0, I0, maxc0)
+
+
+TRAN_KEYS = ["t_stop", "dt", "max_dt", "min_dt", "reltol", "abstol", "vntol", "lte_ratio", "redo_factor",
+             "grow_factor", "tran_ft", "nr_damping", "gshunt_init", "gshunt_target", "gshunt_steps",
+             "warmup_steps", "max_consecutive_rejects", "fixed_step", "method", "n_external", "max_steps", "tran_itl"]
+
+
+def tran_cfg_array(cfg: Dict[str, float]) -> np.ndarray:
+    return np.asarray([float(cfg[k]) for k in TRAN_KEYS], np.float64)
+
+
+def _tran_result(times, V, I, stats, n_vsrc):
+    n = int(stats[0])
+    return {"times": times[:n], "V": V[:n], "I": I[:n, :n_vsrc], "n_steps": n,
+            "rejected": int(stats[1]), "total_nr_iters": int(stats[2]), "min_dt_used": stats[3],
+            "max_dt_used": stats[4], "device_ms": stats[5], "nr_failures": int(stats[6]),
+            "kernel_launches": int(stats[7])}
+
+
+class TransientSession:
+    """A transient run that advances in slices (``vgb_tran_*``)."""
+
+    def __init__(self, dc: DeviceCircuit, cfg: Dict[str, float], X0, Q0=None, I0=None, maxc0=None):
+        self.dc = dc
+        self.cfg = dict(cfg)
+        self.max_steps = int(cfg["max_steps"])
+        self.n_ext = int(cfg["n_external"])
+        c = tran_cfg_array(cfg)
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (X0, Q0, I0, maxc0)]
+        h = C.c_void_p()
+        dc._check(dc.lib.vgb_tran_create(dc.h, _dp(c), *[None if a is None else _dp(a) for a in arrs],
+                                         C.byref(h)))
+        self.h = h
+        self.done = False
+
+    def advance(self, max_accepted: int = 0) -> int:
+        acc, done = C.c_int(), C.c_int()
+        self.dc._check(self.dc.lib.vgb_tran_advance(self.h, int(max_accepted), C.byref(acc), C.byref(done)))
+        self.done = bool(done.value)
+        return acc.value
+
+    def stats(self) -> np.ndarray:
+        st = np.zeros(8)
+        self.dc._check(self.dc.lib.vgb_tran_read(self.h, None, None, None, _dp(st)))
+        return st
+
+    def read(self):
+        st = self.stats()
+        n = int(st[0])
+        times = np.zeros(max(n, 1))
+        V = np.zeros((max(n, 1), self.n_ext))
+        I = np.zeros((max(n, 1), max(self.dc.n_vsrc, 1)))
+        self.dc._check(self.dc.lib.vgb_tran_read(self.h, _dp(times), _dp(V), _dp(I), _dp(st)))
+        return _tran_result(times, V, I, st, self.dc.n_vsrc)
+
+    def state(self):
+        X = np.zeros(self.dc.n_nodes + self.dc.n_vsrc)
+        Q = np.zeros(max(self.dc.n_unk, 1))
+        self.dc._check(self.dc.lib.vgb_tran_state(self.h, _dp(X), _dp(Q)))
+        return X, Q[: self.dc.n_unk]
+
+    def close(self):
+        if self.h is not None:
+            self.dc.lib.vgb_tran_destroy(self.h)  # frees only the session's own buffers
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
