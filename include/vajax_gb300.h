@@ -81,8 +81,9 @@ int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx);
  * after this call.  finalize() runs it when it has not been run. */
 int vgb_circuit_analyze(void* h);
 /* Solver statistics after analysis, out[16] = {n_aug, nnz, nnz_lu, lu_flops,
- * etree_height, max_factor_column, critical_path_steps, contribution_slots,
- * supernodes, max_front, front_storage, front_flops, front_tree_depth, 0, 0, 0}. */
+ * etree_height, max_factor_column, critical_path_tasks, contribution_slots,
+ * supernodes, max_front, front_storage, front_flops, front_tree_depth,
+ * schedule_makespan_ns (simulated), factorisation_tasks, 0}. */
 int vgb_solver_info(void* h, int64_t* out);
 
 /* Static-pivot ordering: perm_r[n_aug] (row r of the factorised matrix is row

@@ -288,6 +288,8 @@ int vgb_solver_info(void* h, int64_t* out) {
         out[10] = L.fr_off.empty() ? 0 : L.fr_off.back();
         out[11] = L.mf_flops;
         out[12] = L.mf_depth;
+        out[13] = (int64_t)L.sched_makespan_ns;
+        out[14] = (int64_t)L.task_type.size();
     });
 }
 
@@ -373,6 +375,14 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->d_conv_mask.upload(c->conv_mask);
         c->d_heavy_csr.upload(c->heavy_csr.empty() ? std::vector<int>{0} : c->heavy_csr);
         c->d_heavy_row.upload(c->heavy_row.empty() ? std::vector<int>{0} : c->heavy_row);
+        {
+            auto up1 = [](DevBuf<int>& d, const std::vector<int>& h) { d.upload(h.empty() ? std::vector<int>{0} : h); };
+            up1(c->d_hchunk_item, c->hchunk_item);
+            up1(c->d_hchunk_lo, c->hchunk_lo);
+            up1(c->d_hchunk_hi, c->hchunk_hi);
+            up1(c->d_hitem_ptr, c->hitem_ptr);
+            c->d_hpart.alloc(3 * std::max<size_t>(c->hchunk_item.size(), 1));
+        }
         c->d_indptr.upload(c->indptr);
         c->d_indices.upload(c->indices);
         c->d_contrib.alloc(std::max<long long>(c->n_contrib, 1));
@@ -384,20 +394,6 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
             s->d_data.upload(s->data);
         }
         SparseLU& L = c->lu;
-        L.d_col_ptr.upload(L.col_ptr);
-        L.d_nU.upload(L.nU);
-        L.d_rows.upload(L.rows);
-        L.d_f2a.upload(L.f2a);
-        L.d_ustart.upload(L.ustart);
-        L.d_umap_ptr.upload(L.umap_ptr);
-        L.d_umap.upload(L.umap.empty() ? std::vector<int>{0} : L.umap);
-        L.d_lrow_ptr.upload(L.lrow_ptr);
-        L.d_lrow_pos.upload(L.lrow_pos.empty() ? std::vector<long long>{0} : L.lrow_pos);
-        L.d_lrow_col.upload(L.lrow_col.empty() ? std::vector<int>{0} : L.lrow_col);
-        L.d_urow_ptr.upload(L.urow_ptr);
-        L.d_urow_pos.upload(L.urow_pos.empty() ? std::vector<long long>{0} : L.urow_pos);
-        L.d_urow_col.upload(L.urow_col.empty() ? std::vector<int>{0} : L.urow_col);
-        L.d_ukl.upload(L.ukl);
         std::vector<int> brow(std::max(L.nM, 1), 0);
         for (int i = 0; i < L.nM; ++i) brow[i] = L.perm_r[L.q[i]];
         L.d_brow.upload(brow);
@@ -424,24 +420,29 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         up64(L.d_em_ptr, L.em_ptr);
         up64(L.d_asm_ptr, L.asm_ptr);
         up64(L.d_cv_off, L.fr_cv_off);
+        up64(L.d_tasm_ptr, L.tasm_ptr);
+        up64(L.d_tch_ptr, L.tch_ptr);
         up(L.d_fr_idx, L.fr_idx);
         up(L.d_fr_w, L.fr_w);
-        up(L.d_sn_first, L.sn_first);
         up(L.d_sn_parent, L.sn_parent);
         up(L.d_ch_ptr, L.ch_ptr);
         up(L.d_ch_idx, L.ch_idx);
         up(L.d_em_idx, L.em_idx);
         up(L.d_asm_e, L.asm_e);
         up(L.d_asm_pos, L.asm_pos);
-        up(L.d_fr_task0, L.fr_task0);
-        up(L.d_fr_nb, L.fr_nb);
         up(L.d_task_type, L.task_type);
         up(L.d_task_front, L.task_front);
-        up(L.d_task_b0, L.task_b0);
-        up(L.d_task_b1, L.task_b1);
+        up(L.d_task_i, L.task_i);
+        up(L.d_task_j, L.task_j);
+        up(L.d_task_k, L.task_k);
         up(L.d_fr_big, L.fr_big);
-        up(L.d_big_asm_e, L.big_asm_e);
-        up64(L.d_big_asm_pos, L.big_asm_pos);
+        up(L.d_fr_kb, L.fr_kb);
+        up(L.d_fr_nb, L.fr_nb);
+        up(L.d_fr_tile0, L.fr_tile0);
+        up(L.d_tasm_e, L.tasm_e);
+        up(L.d_tasm_pos, L.tasm_pos);
+        up(L.d_tch, L.tch);
+        L.d_tver.alloc(std::max<long long>(L.n_tiles, 1));
         const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
         const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
         if (precision == 1) {
@@ -451,7 +452,7 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
             L.d_pool64.alloc(pool);
             L.d_cv64.alloc(cvn);
         }
-        L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1) + std::max<size_t>(L.task_type.size(), 1));
+        L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
         L.d_mf_flags.zero(c->stream);
         L.d_mf_count.alloc(std::max(L.nsn, 1));
         L.d_counters.alloc(4);

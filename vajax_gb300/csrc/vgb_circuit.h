@@ -12,6 +12,7 @@ namespace vgb {
 
 // Gather lists longer than this are reduced by a whole block instead of one thread.
 constexpr int HEAVY_LIST = 64;
+constexpr int HEAVY_CHUNK = 2048;
 
 template <class T>
 struct DevBuf {
@@ -86,13 +87,17 @@ struct MEntry {
     int e, i, j;
 };
 
-// Widest supernode (number of pivots eliminated by one front).
-constexpr int FRONT_WMAX = 64;
-// Fronts up to SMALL_FRONT wide are factorised by one CTA in shared memory;
-// larger ones are split into diagonal, panel and Schur-complement tile tasks.
+// Widest supernode (number of pivots eliminated by one front).  Separators
+// stay whole: a wide front is factorised as a DAG of 32 x 32 tile tasks.
+constexpr int FRONT_WMAX = 4096;
+// Fronts of order m <= SMALL_FRONT are factorised by one CTA in shared memory;
+// larger ones by tile tasks (right-looking tiled LU: GETRF of a diagonal tile,
+// TRSM of the tiles below and right of it, GEMM updates of the trailing tiles).
 constexpr int SMALL_FRONT = 64;
 constexpr int FRONT_TILE = 32;
-enum TaskType : int { TASK_SMALL = 0, TASK_DIAG = 1, TASK_PANEL = 2, TASK_SCHUR = 3 };
+constexpr int FRONT_TILE_LD = 33;          // shared-memory leading dimension of a tile (no bank conflicts)
+constexpr int TILE_FINAL = 1 << 20;        // tile version of a finished L / U / diagonal tile
+enum TaskType : int { TASK_SMALL = 0, TASK_GETRF = 1, TASK_TRSM_L = 2, TASK_TRSM_U = 3, TASK_GEMM = 4 };
 
 // Static-pivot sparse LU structures (host symbolic + device numeric).
 struct SparseLU {
@@ -106,25 +111,10 @@ struct SparseLU {
     std::vector<int> l_col, l_arow, l_diag_e;          // B index, A row, A slot of the diagonal
     std::vector<int> l_ptr, l_e, l_x;                  // off-diagonal row entries: A slot, x index
     std::vector<int> pre_ptr, pre_e, pre_f;            // per M row: A slot and F index of couplings
-    std::vector<long long> ukl;                        // per U slot: first L slot of the source column
-    // factor storage, column-major with U part, diagonal, then L part per column
-    std::vector<long long> col_ptr;   // [n+1]
-    std::vector<int> nU;              // [n] entries above diagonal
-    std::vector<int> rows;            // [nnzLU] row index of each slot (permuted indexing)
-    std::vector<int> f2a;             // [nnzLU] CSR index of A feeding this slot or -1
-    // left-looking update schedule: for column j, the U entries k (rows[] of U part)
-    // each with a run of map offsets (positions inside column j) for L(:,k)
-    std::vector<long long> ustart;    // [n+1] prefix of nU (global U-slot numbering)
-    std::vector<long long> umap_ptr;  // [nnzU + 1] prefix over U slots
-    std::vector<int> umap;            // relative position inside column j per L(i,k)
-    // row access for triangular solves
-    std::vector<long long> lrow_ptr;  // [n+1]
-    std::vector<long long> lrow_pos;  // positions of L(i,k), k < i (global slot)
-    std::vector<int> lrow_col;        // k of each
-    std::vector<long long> urow_ptr;  // [n+1]
-    std::vector<long long> urow_pos;  // positions of U(i,j), j > i
-    std::vector<int> urow_col;        // j of each
-    long long nnz_lu = 0, flops = 0;
+    long long nnz_lu = 0, flops = 0;                   // exact nnz(L+U) and 2 x multiply-adds of M
+    long long etree_height = 0;   // levels of the elimination tree
+    long long max_col = 0;        // longest column of L+U
+    long long crit_path = 0;      // longest chain of dependent factorisation tasks
     // multifrontal structure of M (supernodes numbered by first column: children before parents)
     int nsn = 0;
     std::vector<int> sn_first, sn_of, sn_parent, fr_w;
@@ -133,38 +123,34 @@ struct SparseLU {
     std::vector<int> ch_ptr, ch_idx;                  // children of each supernode
     std::vector<long long> em_ptr;                    // extend-add map of each supernode into its parent
     std::vector<int> em_idx;
-    std::vector<long long> asm_ptr;                   // A entries assembled into each front
+    std::vector<long long> asm_ptr;                   // A entries assembled into each (small) front
     std::vector<int> asm_e, asm_pos;                  // A slot, position r + c*m inside the front
     long long mf_max_m = 0, mf_flops = 0, mf_depth = 0;
     std::vector<long long> fr_cv_off;                 // forward-solve contribution vector offsets
-    std::vector<int> fr_task0, fr_nb;                 // first task of each front, tiles per dimension
-    std::vector<int> task_type, task_front, task_b0, task_b1;
+    // task list and tiles of the large fronts
+    std::vector<int> task_type, task_front, task_i, task_j, task_k;
     std::vector<int> fr_big;                          // 1 = front handled by tile tasks
-    std::vector<int> big_asm_e;                       // A entries of large fronts ...
-    std::vector<long long> big_asm_pos;               // ... and their absolute pool positions
-    long long big_lo = 0, big_hi = 0;                 // pool span holding the large fronts
-    DevBuf<int> d_fr_big, d_big_asm_e;
-    DevBuf<long long> d_big_asm_pos;
-    // device mirrors of the multifrontal structure
-    DevBuf<long long> d_fr_ptr, d_fr_off, d_em_ptr, d_asm_ptr, d_cv_off;
-    DevBuf<int> d_fr_idx, d_fr_w, d_sn_first, d_sn_parent, d_ch_ptr, d_ch_idx, d_em_idx, d_asm_e, d_asm_pos;
-    DevBuf<int> d_fr_task0, d_fr_nb, d_task_type, d_task_front, d_task_b0, d_task_b1;
-    DevBuf<int> d_mf_flags;                            // done, diag_done, fwd_done, bwd_done [4 ns] + panel flags
-    DevBuf<int> d_mf_count;                            // completed Schur tiles per front [ns]
-    DevBuf<double> d_pool64, d_cv64, d_y64;
-    DevBuf<float> d_pool32, d_cv32, d_y32;
-    long long etree_height = 0;   // levels of the elimination tree
-    long long max_col = 0;        // longest factor column (entries)
-    long long crit_path = 0;      // longest dependency chain, in sequential column steps
-    // device
-    DevBuf<long long> d_col_ptr, d_ustart, d_umap_ptr, d_lrow_ptr, d_lrow_pos, d_urow_ptr, d_urow_pos, d_ukl;
-    DevBuf<int> d_nU, d_rows, d_f2a, d_umap, d_lrow_col, d_urow_col, d_brow;  // brow: A row of permuted M row
+    std::vector<int> fr_kb, fr_nb;                    // pivot tiles, all tiles per dimension
+    std::vector<int> fr_tile0;                        // first tile of the front in the tile arrays
+    long long n_tiles = 0;
+    double sched_makespan_ns = 0;                     // simulated factorisation time of the task schedule
+    std::vector<long long> tasm_ptr;                  // per tile: A entries (slot, tile-local position)
+    std::vector<int> tasm_e, tasm_pos;
+    std::vector<long long> tch_ptr;                   // per tile: child blocks {child, r0, r1, c0, c1}
+    std::vector<int> tch;
+    // device mirrors
+    DevBuf<long long> d_fr_ptr, d_fr_off, d_em_ptr, d_asm_ptr, d_cv_off, d_tasm_ptr, d_tch_ptr;
+    DevBuf<int> d_fr_idx, d_fr_w, d_sn_parent, d_ch_ptr, d_ch_idx, d_em_idx, d_asm_e, d_asm_pos;
+    DevBuf<int> d_task_type, d_task_front, d_task_i, d_task_j, d_task_k;
+    DevBuf<int> d_fr_big, d_fr_kb, d_fr_nb, d_fr_tile0, d_tasm_e, d_tasm_pos, d_tch;
+    DevBuf<int> d_mf_flags;                            // done, -, fwd_done, bwd_done [4 ns]
+    DevBuf<int> d_mf_count;                            // final contribution tiles per front [ns]
+    DevBuf<int> d_tver;                                // per tile: updates applied, or TILE_FINAL
+    DevBuf<double> d_pool64, d_cv64;
+    DevBuf<float> d_pool32, d_cv32;
+    DevBuf<int> d_brow, d_q;
     DevBuf<int> d_f_col, d_f_arow, d_f_diag_e, d_l_col, d_l_arow, d_l_diag_e, d_l_ptr, d_l_e, d_l_x;
     DevBuf<int> d_pre_ptr, d_pre_e, d_pre_f;
-    DevBuf<int> d_q;
-    DevBuf<double> d_vals64;
-    DevBuf<float> d_vals32;
-    DevBuf<int> d_done;      // per column/row epoch flags (factor, fwd, bwd: 3n)
     DevBuf<int> d_counters;  // work counters
     int epoch = 0;
 };
@@ -209,6 +195,10 @@ struct Circuit {
     std::vector<unsigned char> conv_mask;  // [n_aug] 1 = checked in the residual test
     std::vector<int> heavy_csr, heavy_row; // items whose gather list is longer than HEAVY_LIST
     DevBuf<int> d_heavy_csr, d_heavy_row;
+    // chunks of the heavy lists (HEAVY_CHUNK entries each, in list order) and each item's chunk range
+    std::vector<int> hchunk_item, hchunk_lo, hchunk_hi, hitem_ptr;
+    DevBuf<int> d_hchunk_item, d_hchunk_lo, d_hchunk_hi, d_hitem_ptr;
+    DevBuf<double> d_hpart;                // [3][n_chunks] partial sum, charge sum, max
     long long n_contrib = 0;
 
     DevBuf<int> d_csr_src_ptr, d_csr_src, d_res_src_ptr, d_res_src, d_rq_src;

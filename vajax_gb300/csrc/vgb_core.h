@@ -21,7 +21,7 @@ inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
 inline long long solve_launches(const Circuit& c) {
     const SparseLU& L = c.lu;
     long long once = (L.nM + (long long)L.f_col.size() ? 1 : 0) + (L.nsn ? 2 : 0) + (L.l_col.empty() ? 0 : 1);
-    long long n = (L.nsn ? 1 : 0) + (L.big_asm_e.empty() ? 0 : 1) + once;
+    long long n = (L.nsn ? 1 : 0) + once;
     if (c.solver_kind == 1) n += (long long)c.refine_sweeps * (once + 2);
     return n;
 }
@@ -44,7 +44,7 @@ inline void assemble(Circuit& c, const double* X, const double* vs, const double
                      const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
                      double reltol, double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
                      cudaStream_t s) {
-    c.launches += 1 + ((c.heavy_csr.size() + c.heavy_row.size()) ? 1 : 0);
+    c.launches += 1 + ((c.heavy_csr.size() + c.heavy_row.size()) ? 2 : 0);
     AssembleArgs a{};
     a.nnz = c.nnz;
     a.n_unk = c.n_unk;
@@ -89,6 +89,12 @@ inline void assemble(Circuit& c, const double* X, const double* vs, const double
     a.n_heavy_csr = (int)c.heavy_csr.size();
     a.heavy_row = c.d_heavy_row.p;
     a.n_heavy_row = (int)c.heavy_row.size();
+    a.hchunk_item = c.d_hchunk_item.p;
+    a.hchunk_lo = c.d_hchunk_lo.p;
+    a.hchunk_hi = c.d_hchunk_hi.p;
+    a.hitem_ptr = c.d_hitem_ptr.p;
+    a.n_hchunk = (int)c.hchunk_item.size();
+    a.hpart = c.d_hpart.p;
     launch_assemble(a, s);
 }
 

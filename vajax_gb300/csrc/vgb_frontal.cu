@@ -3,19 +3,25 @@
 // Numeric factorisation is one persistent, sync-free kernel over a task list
 // in topological order of the assembly tree (built by the host symbolic phase):
 //
-//   TASK_SMALL  front of order m <= SMALL_FRONT: one CTA assembles it in shared
-//               memory (A entries + children's contribution blocks), eliminates
-//               its w pivots and writes the front back;
-//   TASK_DIAG   large front: assemble in global memory, factor the w x w
-//               diagonal block on chip;
-//   TASK_PANEL  one row tile of L21 = A21 U11^-1 and one column tile of
-//               U12 = L11^-1 A12;
-//   TASK_SCHUR  one tile of the contribution block, C -= L21 U12.
+//   TASK_SMALL   front of order m <= SMALL_FRONT: one CTA assembles it in shared
+//                memory (A entries, then the children's contribution blocks in
+//                child order), eliminates its w pivots and stores it;
+//   TASK_GETRF   large front, diagonal tile k: LU of a 32 x 32 tile in registers
+//                of one warp;
+//   TASK_TRSM_L  tile (i, k) below it: L(i,k) = A(i,k) U(k,k)^-1;
+//   TASK_TRSM_U  tile (k, j) right of it: U(k,j) = L(k,k)^-1 A(k,j);
+//   TASK_GEMM    trailing tile (i, j): A(i,j) -= L(i,k) U(k,j).
 //
-// CTAs claim tasks in list order from a global counter and wait (bounded) on
-// flags of earlier tasks only, so every wait ends.  Extend-add is a pull by
-// the parent, one child at a time, so sums are deterministic.  Front storage
-// is dense column-major: F[i + j*m].
+// Large fronts are never assembled as a whole: the first task that touches a
+// tile (the k = 0 task of that tile) builds it in shared memory from its A
+// entries and the blocks of the children's contribution blocks that land in
+// it, in child order, so every sum has a fixed order and the factorisation is
+// deterministic.  A per-tile version counter orders the updates of a tile
+// (GEMM k waits for version k) and marks finished L / U / diagonal tiles
+// (TILE_FINAL).  CTAs claim tasks in list order from a global counter and wait
+// (bounded) only on tasks earlier in the list, so every wait ends.
+//
+// Front storage is dense column-major, F[i + j * m], in one pool.
 #include <cuda/atomic>
 
 #include "vgb_kernels.cuh"
@@ -31,9 +37,11 @@ __device__ __forceinline__ void st_rel(int* p, int v) {
     cuda::atomic_ref<int, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_release);
 }
 
-__device__ bool wait_eq(const int* flag, int epoch, int* abort_flag, int* err, unsigned limit) {
+// Spin until *flag == value; gives up after `limit` polls (sets the timeout
+// error bit and the abort flag) or when another CTA has aborted.
+__device__ bool wait_eq(const int* flag, int value, int* abort_flag, int* err, unsigned limit) {
     unsigned it = 0;
-    while (ld_acq(flag) != epoch) {
+    while (ld_acq(flag) != value) {
         if (++it > limit) {
             atomicOr(err, DEV_ERR_TIMEOUT);
             atomicExch(abort_flag, 1);
@@ -61,18 +69,24 @@ struct MFArgs {
     const long long* asm_ptr;
     const int* asm_e;
     const int* asm_pos;
-    const int* fr_task0;
+    const int* fr_kb;
     const int* fr_nb;
+    const int* fr_tile0;
+    const long long* tasm_ptr;
+    const int* tasm_e;
+    const int* tasm_pos;
+    const long long* tch_ptr;
+    const int* tch;
     const int* task_type;
     const int* task_front;
-    const int* task_b0;
-    const int* task_b1;
-    const int* sn_parent;
-    const int* fr_big;
+    const int* task_i;
+    const int* task_j;
+    const int* task_k;
     int n_tasks;
     const double* A;
-    int* flags;       // done [ns], diag [ns], fwd [ns], bwd [ns], panel [n_tasks]
-    int* count;       // per front
+    int* done;        // [ns] epoch flag: front factorised (contribution block final)
+    int* count;       // [ns] final contribution tiles of a large front
+    int* tver;        // [n_tiles] updates applied to a tile, or TILE_FINAL
     int* counter;
     int* abort_flag;
     int* err;
@@ -81,20 +95,54 @@ struct MFArgs {
 };
 
 constexpr int MF_THREADS = 128;
-constexpr int MF_SMEM_DOUBLES = 8192;  // 64 KB
+constexpr int MF_CTAS_PER_SM = 4;
+constexpr int LD = FRONT_TILE_LD;
+constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
+// shared memory of a factorisation CTA: one small front, or three tiles
+constexpr int MF_SMEM_ELEMS = SMALL_FRONT * SMALL_FRONT;
+static_assert(3 * TILE_ELEMS <= MF_SMEM_ELEMS, "three tiles must fit in the small-front buffer");
 
-// wait for every child front of S to be complete
-__device__ bool wait_children(const MFArgs& a, int S, const int* flag_base) {
+__device__ __forceinline__ int tile_lo(int t, int kb, int w) {
+    return t < kb ? t * FRONT_TILE : w + (t - kb) * FRONT_TILE;
+}
+__device__ __forceinline__ int tile_hi(int t, int kb, int nb, int w, int m) {
+    return t + 1 < nb ? tile_lo(t + 1, kb, w) : m;
+}
+
+// wait until every child front of S is factorised
+__device__ bool wait_children(const MFArgs& a, int S) {
     bool ok = true;
     for (int q = a.ch_ptr[S] + threadIdx.x; q < a.ch_ptr[S + 1]; q += blockDim.x)
-        ok = ok && wait_eq(flag_base + a.ch_idx[q], a.epoch, a.abort_flag, a.err, a.spin_limit);
+        ok = ok && wait_eq(a.done + a.ch_idx[q], a.epoch, a.abort_flag, a.err, a.spin_limit);
     return __syncthreads_and(ok);
 }
 
+// thread 0 waits on up to three flags; the whole CTA learns the outcome
+__device__ bool wait3(const MFArgs& a, const int* f0, int v0, const int* f1, int v1, const int* f2, int v2) {
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        if (f0) ok = wait_eq(f0, v0, a.abort_flag, a.err, a.spin_limit);
+        if (ok && f1) ok = wait_eq(f1, v1, a.abort_flag, a.err, a.spin_limit);
+        if (ok && f2) ok = wait_eq(f2, v2, a.abort_flag, a.err, a.spin_limit);
+    }
+    return !__syncthreads_or(!ok);
+}
+
+// publish a flag after the CTA's global stores
+__device__ __forceinline__ void publish(int* flag, int value) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        st_rel(flag, value);
+    }
+}
+
+// ---- small fronts ------------------------------------------------------------
+
 template <typename T>
-__device__ void assemble_front(const MFArgs& a, int S, T* F, int m, const T* pool, bool zero_first) {
-    if (zero_first)
-        for (long long t = threadIdx.x; t < (long long)m * m; t += blockDim.x) F[t] = (T)0;
+__device__ void assemble_small(const MFArgs& a, int S, T* F, int m, const T* pool) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) F[t] = (T)0;
     __syncthreads();
     for (long long t = a.asm_ptr[S] + threadIdx.x; t < a.asm_ptr[S + 1]; t += blockDim.x)
         F[a.asm_pos[t]] = (T)a.A[a.asm_e[t]];
@@ -106,49 +154,187 @@ __device__ void assemble_front(const MFArgs& a, int S, T* F, int m, const T* poo
         const int rc = mc - wc;
         const T* FC = pool + a.fr_off[C];
         const int* em = a.em_idx + a.em_ptr[C];
-        for (int idx = threadIdx.x; idx < rc * rc; idx += blockDim.x) {
-            const int i = idx % rc, j = idx / rc;
-            F[em[i] + (long long)em[j] * m] += __ldcg(FC + (wc + i) + (long long)(wc + j) * mc);
+        for (int cj = warp; cj < rc; cj += nw) {
+            const int dj = em[cj] * m;
+            const T* src = FC + (long long)(wc + cj) * mc + wc;
+            for (int ci = lane; ci < rc; ci += 32) F[em[ci] + dj] += __ldcg(src + ci);
         }
         __syncthreads();
     }
 }
 
-// Eliminate w pivots of an m x m column-major matrix held by the CTA (shared or global).
+// Eliminate the first w pivots of an m x m column-major front in shared memory.
 template <typename T>
-__device__ void partial_lu(T* F, int ld, int m, int w, int* err) {
+__device__ void partial_lu_small(T* F, int m, int w, int* err) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int p = 0; p < w; ++p) {
-        T piv = F[p + (long long)p * ld];
-        if (piv == (T)0 || !isfinite((double)piv)) {
-            piv = (T)1e-30;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                F[p + (long long)p * ld] = piv;
-                atomicOr(err, DEV_ERR_PIVOT);
+        T piv = F[p + p * m];
+        if (piv == (T)0 || !isfinite((double)piv)) piv = (T)1e-30;
+        __syncthreads();
+        if (threadIdx.x == 0 && piv != F[p + p * m]) {
+            F[p + p * m] = piv;
+            atomicOr(err, DEV_ERR_PIVOT);
+        }
+        for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) F[i + p * m] /= piv;
+        __syncthreads();
+        for (int j = p + 1 + warp; j < m; j += nw) {
+            const T u = F[p + j * m];
+            for (int i = p + 1 + lane; i < m; i += 32) F[i + j * m] -= F[i + p * m] * u;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- tiles of large fronts -----------------------------------------------------
+
+// tile rows [r0, r0+nr) x columns [c0, c0+nc) of front F (leading dimension m) into a
+// zero-padded 32 x 32 shared-memory tile
+template <typename T>
+__device__ void load_tile(T* dst, const T* F, long long m, int r0, int nr, int c0, int nc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = warp; c < FRONT_TILE; c += nw)
+        dst[lane + c * LD] = (lane < nr && c < nc) ? __ldcg(F + (r0 + lane) + (c0 + c) * m) : (T)0;
+}
+
+template <typename T>
+__device__ void store_tile(T* F, const T* src, long long m, int r0, int nr, int c0, int nc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = warp; c < nc; c += nw)
+        if (lane < nr) __stcg(F + (r0 + lane) + (c0 + c) * m, src[lane + c * LD]);
+}
+
+// First touch: A entries of the tile, then the children's blocks in child order.
+template <typename T>
+__device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, int c0, const T* pool) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int t = threadIdx.x; t < TILE_ELEMS; t += blockDim.x) dst[t] = (T)0;
+    __syncthreads();
+    for (long long t = a.tasm_ptr[tile] + threadIdx.x; t < a.tasm_ptr[tile + 1]; t += blockDim.x)
+        dst[a.tasm_pos[t]] = (T)a.A[a.tasm_e[t]];
+    __syncthreads();
+    for (long long q = a.tch_ptr[tile]; q < a.tch_ptr[tile + 1]; q += 5) {
+        const int C = a.tch[q], rlo = a.tch[q + 1], rhi = a.tch[q + 2], clo = a.tch[q + 3], chi = a.tch[q + 4];
+        const long long mc = a.fr_ptr[C + 1] - a.fr_ptr[C];
+        const int wc = a.fr_w[C];
+        const T* FC = pool + a.fr_off[C];
+        const int* em = a.em_idx + a.em_ptr[C];
+        for (int cj = clo + warp; cj < chi; cj += nw) {
+            const int dj = (em[cj] - c0) * LD;
+            const T* src = FC + (wc + cj) * mc + wc;
+            for (int ci = rlo + lane; ci < rhi; ci += 32) dst[(em[ci] - r0) + dj] += __ldcg(src + ci);
+        }
+        __syncthreads();
+    }
+}
+
+// LU without pivoting of the leading n x n block of a tile; warp 0 holds one
+// row per lane in registers.
+template <typename T>
+__device__ void getrf_tile(T* t, int n, int* err) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        T a[FRONT_TILE];
+#pragma unroll
+        for (int c = 0; c < FRONT_TILE; ++c) a[c] = t[lane + c * LD];
+#pragma unroll
+        for (int p = 0; p < FRONT_TILE; ++p) {
+            if (p < n) {
+                T piv = __shfl_sync(0xffffffffu, a[p], p);
+                if (piv == (T)0 || !isfinite((double)piv)) {
+                    piv = (T)1e-30;
+                    if (lane == p) a[p] = piv;
+                    if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
+                }
+                if (lane > p) a[p] /= piv;
+#pragma unroll
+                for (int c = p + 1; c < FRONT_TILE; ++c) {
+                    if (c < n) {
+                        const T u = __shfl_sync(0xffffffffu, a[c], p);
+                        if (lane > p) a[c] -= a[p] * u;
+                    }
+                }
             }
         }
-        __syncthreads();
-        for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) F[i + (long long)p * ld] /= piv;
-        __syncthreads();
-        const int n = m - p - 1;
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-            const int i = p + 1 + idx % n, j = p + 1 + idx / n;
-            F[i + (long long)j * ld] -= F[i + (long long)p * ld] * F[p + (long long)j * ld];
-        }
-        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < FRONT_TILE; ++c) t[lane + c * LD] = a[c];
     }
+    __syncthreads();
+}
+
+// x := x U^-1 with U the upper triangle (with diagonal) of the n x n tile d;
+// warp 0, one row of x per lane.
+template <typename T>
+__device__ void trsm_l_tile(T* x, const T* d, int n) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        T a[FRONT_TILE];
+#pragma unroll
+        for (int c = 0; c < FRONT_TILE; ++c) a[c] = x[lane + c * LD];
+#pragma unroll
+        for (int c = 0; c < FRONT_TILE; ++c) {
+            if (c < n) {
+                a[c] /= d[c + c * LD];
+#pragma unroll
+                for (int c2 = c + 1; c2 < FRONT_TILE; ++c2)
+                    if (c2 < n) a[c2] -= a[c] * d[c + c2 * LD];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < FRONT_TILE; ++c) x[lane + c * LD] = a[c];
+    }
+    __syncthreads();
+}
+
+// x := L^-1 x with L the unit lower triangle of the n x n tile d; warp 0, one
+// column of x per lane.
+template <typename T>
+__device__ void trsm_u_tile(T* x, const T* d, int n) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        T a[FRONT_TILE];
+#pragma unroll
+        for (int r = 0; r < FRONT_TILE; ++r) a[r] = x[r + lane * LD];
+#pragma unroll
+        for (int r = 0; r < FRONT_TILE; ++r) {
+            if (r < n) {
+#pragma unroll
+                for (int r2 = r + 1; r2 < FRONT_TILE; ++r2)
+                    if (r2 < n) a[r2] -= d[r2 + r * LD] * a[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < FRONT_TILE; ++r) x[r + lane * LD] = a[r];
+    }
+    __syncthreads();
+}
+
+// c -= l u over the first nk columns of l / rows of u (all tiles zero-padded):
+// lane = row, warp w takes columns w, w + 4, ...
+template <typename T>
+__device__ void gemm_tile(T* c, const T* l, const T* u, int nk, int nj) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int Q = FRONT_TILE / (MF_THREADS / 32);
+    T acc[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) acc[q] = (T)0;
+    for (int k = 0; k < nk; ++k) {
+        const T lv = l[lane + k * LD];
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (warp + 4 * q < nj) acc[q] += lv * u[k + (warp + 4 * q) * LD];
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) c[lane + (warp + 4 * q) * LD] -= acc[q];
+    __syncthreads();
 }
 
 template <typename T>
-__global__ void __launch_bounds__(MF_THREADS) mf_factor_kernel(MFArgs a, T* pool) {
+__global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(MFArgs a, T* pool) {
     extern __shared__ double smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_task;
-    int* const done = a.flags;
-    int* const diag = a.flags + a.ns;
-    int* const panel = a.flags + 4 * (size_t)a.ns;
     while (true) {
-        if (threadIdx.x == 0) s_task = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) s_task = *(volatile int*)a.abort_flag ? a.n_tasks : atomicAdd(a.counter, 1);
         __syncthreads();
         const int t = s_task;
         __syncthreads();
@@ -158,141 +344,68 @@ __global__ void __launch_bounds__(MF_THREADS) mf_factor_kernel(MFArgs a, T* pool
         const int m = (int)(a.fr_ptr[S + 1] - a.fr_ptr[S]);
         const int w = a.fr_w[S];
         T* FS = pool + a.fr_off[S];
-        const int P = a.sn_parent[S];
-        const bool push = P >= 0 && a.fr_big[P];
         if (type == TASK_SMALL) {
-            if (!wait_children(a, S, done)) continue;
-            assemble_front<T>(a, S, sm, m, pool, true);
-            partial_lu<T>(sm, m, m, w, a.err);
-            for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) FS[idx] = sm[idx];
-            if (push) {
-                // contribution block straight into the (large) parent front
-                const int r = m - w;
-                const int mp = (int)(a.fr_ptr[P + 1] - a.fr_ptr[P]);
-                T* FP = pool + a.fr_off[P];
-                const int* em = a.em_idx + a.em_ptr[S];
-                for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
-                    const int i = idx % r, j = idx / r;
-                    atomicAdd(FP + em[i] + (long long)em[j] * mp, sm[(w + i) + (w + j) * m]);
-                }
-            }
-            __threadfence();
+            if (!wait_children(a, S)) continue;
+            assemble_small<T>(a, S, sm, m, pool);
+            partial_lu_small<T>(sm, m, w, a.err);
+            for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) __stcg(FS + idx, sm[idx]);
+            publish(a.done + S, a.epoch);
+            continue;
+        }
+        const int kb = a.fr_kb[S], nb = a.fr_nb[S];
+        const long long tb = a.fr_tile0[S];
+        int* tv = a.tver + tb;
+        const int i = a.task_i[t], j = a.task_j[t], k = a.task_k[t];
+        const int k0 = tile_lo(k, kb, w), nk = tile_hi(k, kb, nb, w, m) - k0;
+        const int r0 = tile_lo(i, kb, w), nr = tile_hi(i, kb, nb, w, m) - r0;
+        const int c0 = tile_lo(j, kb, w), nc = tile_hi(j, kb, nb, w, m) - c0;
+        T* T0 = sm;
+        T* T1 = sm + TILE_ELEMS;
+        T* T2 = sm + 2 * TILE_ELEMS;
+        if (type == TASK_GETRF) {
+            const bool ok = k == 0 ? wait_children(a, S) : wait3(a, tv + k * nb + k, k, nullptr, 0, nullptr, 0);
+            if (!ok) continue;
+            if (k == 0) assemble_tile<T>(a, tb, T0, 0, 0, pool);
+            else load_tile<T>(T0, FS, m, k0, nk, k0, nk);
             __syncthreads();
-            if (threadIdx.x == 0) st_rel(done + S, a.epoch);
-        } else if (type == TASK_DIAG) {
-            // a large front is zeroed and A-assembled before the kernel starts and its children
-            // push their contribution blocks into it: once they are done it is complete
-            if (!wait_children(a, S, done)) continue;
-            for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x)
-                sm[idx] = __ldcg(FS + idx % w + (long long)(idx / w) * m);
+            getrf_tile<T>(T0, nk, a.err);
+            store_tile<T>(FS, T0, m, k0, nk, k0, nk);
+            publish(tv + k * nb + k, TILE_FINAL);
+            if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
+        } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
+            const int* own = tv + (long long)i * nb + j;
+            if (!wait3(a, tv + k * nb + k, TILE_FINAL, k > 0 ? own : nullptr, k, nullptr, 0)) continue;
+            load_tile<T>(T0, FS, m, k0, nk, k0, nk);
+            if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T1, r0, c0, pool);
+            else load_tile<T>(T1, FS, m, r0, nr, c0, nc);
             __syncthreads();
-            partial_lu<T>(sm, w, w, w, a.err);
-            for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) FS[idx % w + (long long)(idx / w) * m] = sm[idx];
-            __threadfence();
+            if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk);
+            else trsm_u_tile<T>(T1, T0, nk);
+            store_tile<T>(FS, T1, m, r0, nr, c0, nc);
+            publish(tv + (long long)i * nb + j, TILE_FINAL);
+        } else {  // TASK_GEMM
+            int* own = tv + (long long)i * nb + j;
+            if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + j, TILE_FINAL,
+                       k > 0 ? own : nullptr, k))
+                continue;
+            load_tile<T>(T0, FS, m, r0, nr, k0, nk);
+            load_tile<T>(T1, FS, m, k0, nk, c0, nc);
+            if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T2, r0, c0, pool);
+            else load_tile<T>(T2, FS, m, r0, nr, c0, nc);
             __syncthreads();
-            if (threadIdx.x == 0) st_rel(diag + S, a.epoch);
-        } else if (type == TASK_PANEL) {
-            bool ok = true;
-            if (threadIdx.x == 0) ok = wait_eq(diag + S, a.epoch, a.abort_flag, a.err, a.spin_limit);
-            if (__syncthreads_or(!ok)) continue;
-            const int b = a.task_b0[t];
-            const int r0 = w + b * FRONT_TILE;
-            const int nr = min(FRONT_TILE, m - r0);
-            T* D = sm;                       // w x w diagonal block (L11 \ U11)
-            T* R = sm + w * w;               // nr x w rows of A21
-            T* Cc = R + FRONT_TILE * w;      // w x nr columns of A12
-            for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x)
-                D[idx] = __ldcg(FS + idx % w + (long long)(idx / w) * m);
-            for (int idx = threadIdx.x; idx < nr * w; idx += blockDim.x) {
-                const int i = idx % nr, k = idx / nr;
-                R[i + k * FRONT_TILE] = __ldcg(FS + (r0 + i) + (long long)k * m);
-                Cc[k + i * w] = __ldcg(FS + k + (long long)(r0 + i) * m);
-            }
-            __syncthreads();
-            const int tid = threadIdx.x;
-            if (tid < nr) {
-                // row i of L21: x U11 = a
-                T* x = R + tid;
-                for (int k = 0; k < w; ++k) {
-                    T s = x[k * FRONT_TILE];
-                    for (int kk = 0; kk < k; ++kk) s -= x[kk * FRONT_TILE] * D[kk + k * w];
-                    x[k * FRONT_TILE] = s / D[k + k * w];
-                }
-            } else if (tid >= 64 && tid < 64 + nr) {
-                // column j of U12: L11 y = a (unit lower)
-                T* y = Cc + (tid - 64) * w;
-                for (int k = 0; k < w; ++k) {
-                    T s = y[k];
-                    for (int kk = 0; kk < k; ++kk) s -= D[k + kk * w] * y[kk];
-                    y[k] = s;
-                }
-            }
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < nr * w; idx += blockDim.x) {
-                const int i = idx % nr, k = idx / nr;
-                FS[(r0 + i) + (long long)k * m] = R[i + k * FRONT_TILE];
-                FS[k + (long long)(r0 + i) * m] = Cc[k + i * w];
-            }
-            __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) st_rel(panel + t, a.epoch);
-        } else {  // TASK_SCHUR
-            const int bi = a.task_b0[t], bj = a.task_b1[t];
-            const int t0 = a.fr_task0[S];
-            bool ok = true;
-            if (threadIdx.x == 0) {
-                ok = wait_eq(panel + t0 + 1 + bi, a.epoch, a.abort_flag, a.err, a.spin_limit);
-                ok = ok && wait_eq(panel + t0 + 1 + bj, a.epoch, a.abort_flag, a.err, a.spin_limit);
-            }
-            if (__syncthreads_or(!ok)) continue;
-            const int i0 = w + bi * FRONT_TILE, j0 = w + bj * FRONT_TILE;
-            const int ni = min(FRONT_TILE, m - i0), nj = min(FRONT_TILE, m - j0);
-            T* Ls = sm;                        // FRONT_TILE x w
-            T* Us = sm + FRONT_TILE * w;       // w x FRONT_TILE
-            for (int idx = threadIdx.x; idx < ni * w; idx += blockDim.x) {
-                const int i = idx % ni, k = idx / ni;
-                Ls[i + k * FRONT_TILE] = __ldcg(FS + (i0 + i) + (long long)k * m);
-            }
-            for (int idx = threadIdx.x; idx < nj * w; idx += blockDim.x) {
-                const int k = idx % w, j = idx / w;
-                Us[k + j * w] = __ldcg(FS + k + (long long)(j0 + j) * m);
-            }
-            __syncthreads();
-            const int mp = push ? (int)(a.fr_ptr[P + 1] - a.fr_ptr[P]) : 0;
-            T* FP = push ? pool + a.fr_off[P] : nullptr;
-            const int* em = a.em_idx + a.em_ptr[S];
-            for (int idx = threadIdx.x; idx < ni * nj; idx += blockDim.x) {
-                const int i = idx % ni, j = idx / ni;
-                T acc = 0;
-                for (int k = 0; k < w; ++k) acc += Ls[i + k * FRONT_TILE] * Us[k + j * w];
-                const long long pos = (i0 + i) + (long long)(j0 + j) * m;
-                if (push) {
-                    const int ci = i0 - w + i, cj = j0 - w + j;  // indices inside the contribution block
-                    atomicAdd(FP + em[ci] + (long long)em[cj] * mp, __ldcg(FS + pos) - acc);
-                } else {
-                    FS[pos] = __ldcg(FS + pos) - acc;
-                }
-            }
-            __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                const int nb = a.fr_nb[S];
-                const int old = atomicAdd(a.count + S, 1);
-                if (old == nb * nb - 1) {
+            gemm_tile<T>(T2, T0, T1, nk, nc);
+            store_tile<T>(FS, T2, m, r0, nr, c0, nc);
+            publish(own, k + 1);
+            if (k == kb - 1 && i >= kb && j >= kb && threadIdx.x == 0) {
+                // a final tile of the contribution block; the last one completes the front
+                const int r = nb - kb;
+                if (atomicAdd(a.count + S, 1) == r * r - 1) {
                     __threadfence();
-                    st_rel(done + S, a.epoch);
+                    st_rel(a.done + S, a.epoch);
                 }
             }
         }
     }
-}
-
-// A entries of the large fronts, scattered once the pool is zeroed.
-template <typename T>
-__global__ void mf_init_kernel(long long n, const int* __restrict__ e, const long long* __restrict__ pos,
-                               const double* __restrict__ A, T* pool) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) pool[pos[i]] = (T)A[e[i]];
 }
 
 // ---------------------------------------------------------------------------
@@ -320,8 +433,9 @@ struct MFSolveArgs {
     unsigned spin_limit;
 };
 
-// Forward: L y = rhs.  Each front adds its children's update vectors, solves
-// with its unit-lower diagonal block and passes cv = u_tail - L21 y up.
+// Forward: L y = rhs.  Each front adds its children's update vectors (child
+// order), solves with its unit-lower diagonal block 32 pivots at a time (one
+// warp, register shuffles) and updates the rows below with the same columns.
 template <typename T>
 __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const T* __restrict__ pool,
                                                             const T* __restrict__ rhs, T* y, T* cv) {
@@ -329,8 +443,9 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
     T* u = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_S;
     int* const fdone = a.flags;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     while (true) {
-        if (threadIdx.x == 0) s_S = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) s_S = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
         __syncthreads();
         const int S = s_S;
         __syncthreads();
@@ -353,23 +468,39 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
             for (int i = threadIdx.x; i < rc; i += blockDim.x) u[em[i]] += __ldcg(cvc + i);
             __syncthreads();
         }
-        for (int p = 0; p < w; ++p) {
-            const T yp = u[p];
-            for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) u[i] -= F[i + (long long)p * m] * yp;
+        for (int p0 = 0; p0 < w; p0 += 32) {
+            const int p1 = min(p0 + 32, w);
+            if (warp == 0) {
+                // lane r - p0 holds row r of the unit-lower block; its L entries are loaded up front
+                const int r = p0 + lane;
+                T val = r < p1 ? u[r] : (T)0;
+                T lrow[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) lrow[q] = (r < p1 && p0 + q < r) ? F[r + (long long)(p0 + q) * m] : (T)0;
+#pragma unroll
+                for (int q = 0; q < 31; ++q) val -= lrow[q] * __shfl_sync(0xffffffffu, val, q);
+                if (r < p1) u[r] = val;
+            }
+            __syncthreads();
+            for (int i = p1 + threadIdx.x; i < m; i += blockDim.x) {
+                T s = (T)0;
+#pragma unroll 8
+                for (int p = p0; p < p1; ++p) s += F[i + (long long)p * m] * u[p];
+                u[i] -= s;
+            }
             __syncthreads();
         }
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             if (i < w) y[idx[i]] = u[i];
             else cv[a.cv_off[S] + (i - w)] = u[i];
         }
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) st_rel(fdone + S, a.epoch);
+        publish(fdone + S, a.epoch);
     }
 }
 
 // Backward: U x = y from the root down; a front needs only its parent done
-// (its tail indices are pivots of ancestors).
+// (its tail indices are pivots of ancestors).  z = y - U12 x_tail, then the
+// upper diagonal block 32 pivots at a time from the bottom.
 template <typename T>
 __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const T* __restrict__ pool,
                                                             const T* __restrict__ y, T* xs, double* xout) {
@@ -377,8 +508,9 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
     T* z = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_S;
     int* const bdone = a.flags + a.ns;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     while (true) {
-        if (threadIdx.x == 0) s_S = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) s_S = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
         __syncthreads();
         const int c = s_S;
         __syncthreads();
@@ -396,31 +528,46 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
         T* xt = z + w;
         for (int j = threadIdx.x; j < m - w; j += blockDim.x) xt[j] = __ldcg(xs + idx[w + j]);
         __syncthreads();
-        // z = y_S - U12 x_tail: each warp takes pivot rows, lanes split the tail
-        {
-            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-            for (int p = warp; p < w; p += nw) {
-                T s = 0;
-                for (int j = lane; j < m - w; j += 32) s += F[p + (long long)(w + j) * m] * xt[j];
-                for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0) z[p] = y[idx[p]] - s;
-            }
+        // z = y_S - U12 x_tail: one pivot row per thread, coalesced down each column
+        for (int p = threadIdx.x; p < w; p += blockDim.x) {
+            T s = (T)0;
+#pragma unroll 8
+            for (int j = 0; j < m - w; ++j) s += F[p + (long long)(w + j) * m] * xt[j];
+            z[p] = y[idx[p]] - s;
         }
         __syncthreads();
-        for (int p = w - 1; p >= 0; --p) {
-            const T xp = z[p] / F[p + (long long)p * m];
+        for (int p1 = w; p1 > 0; p1 -= 32) {
+            const int p0 = max(p1 - 32, 0);
+            if (warp == 0) {
+                // lane r - p0 holds row r of the upper block (diagonal included), loaded up front
+                const int r = p0 + lane;
+                T val = r < p1 ? z[r] : (T)0;
+                T urow[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q)
+                    urow[q] = (r < p1 && p0 + q < p1 && p0 + q >= r) ? F[r + (long long)(p0 + q) * m] : (T)0;
+#pragma unroll
+                for (int q = 31; q >= 0; --q) {
+                    if (lane == q && r < p1) val /= urow[q];
+                    const T xp = __shfl_sync(0xffffffffu, val, q);
+                    if (lane < q) val -= urow[q] * xp;
+                }
+                if (r < p1) z[r] = val;
+            }
             __syncthreads();
-            if (threadIdx.x == 0) z[p] = xp;
-            for (int i = threadIdx.x; i < p; i += blockDim.x) z[i] -= F[i + (long long)p * m] * xp;
+            for (int i = threadIdx.x; i < p0; i += blockDim.x) {
+                T s = (T)0;
+#pragma unroll 8
+                for (int p = p0; p < p1; ++p) s += F[i + (long long)p * m] * z[p];
+                z[i] -= s;
+            }
             __syncthreads();
         }
         for (int p = threadIdx.x; p < w; p += blockDim.x) {
             xs[idx[p]] = z[p];
             xout[a.q[idx[p]]] = (double)z[p];
         }
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) st_rel(bdone + S, a.epoch);
+        publish(bdone + S, a.epoch);
     }
 }
 
@@ -453,18 +600,24 @@ static MFArgs mf_args(Circuit& c, const double* A) {
     a.asm_ptr = L.d_asm_ptr.p;
     a.asm_e = L.d_asm_e.p;
     a.asm_pos = L.d_asm_pos.p;
-    a.fr_task0 = L.d_fr_task0.p;
+    a.fr_kb = L.d_fr_kb.p;
     a.fr_nb = L.d_fr_nb.p;
+    a.fr_tile0 = L.d_fr_tile0.p;
+    a.tasm_ptr = L.d_tasm_ptr.p;
+    a.tasm_e = L.d_tasm_e.p;
+    a.tasm_pos = L.d_tasm_pos.p;
+    a.tch_ptr = L.d_tch_ptr.p;
+    a.tch = L.d_tch.p;
     a.task_type = L.d_task_type.p;
     a.task_front = L.d_task_front.p;
-    a.task_b0 = L.d_task_b0.p;
-    a.task_b1 = L.d_task_b1.p;
-    a.sn_parent = L.d_sn_parent.p;
-    a.fr_big = L.d_fr_big.p;
+    a.task_i = L.d_task_i.p;
+    a.task_j = L.d_task_j.p;
+    a.task_k = L.d_task_k.p;
     a.n_tasks = (int)L.task_type.size();
     a.A = A;
-    a.flags = L.d_mf_flags.p;
+    a.done = L.d_mf_flags.p;
     a.count = L.d_mf_count.p;
+    a.tver = L.d_tver.p;
     a.counter = L.d_counters.p;
     a.abort_flag = L.d_counters.p + 3;
     a.err = &c.d_status.p->dev_err;
@@ -475,26 +628,15 @@ static MFArgs mf_args(Circuit& c, const double* A) {
 template <typename T>
 static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     SparseLU& L = c.lu;
-    static bool attr_set = false;
-    if (!attr_set) {
-        VGB_CUDA(cudaFuncSetAttribute(mf_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      MF_SMEM_DOUBLES * (int)sizeof(double)));
-        attr_set = true;
-    }
+    const int smem = MF_SMEM_ELEMS * (int)sizeof(T);
     L.epoch++;
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_count.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
-    if (!L.big_asm_e.empty()) {
-        // large fronts accumulate pushes from their children: zero them, then place A
-        // (one memset over the span that holds them)
-        VGB_CUDA(cudaMemsetAsync(pool + L.big_lo, 0, (L.big_hi - L.big_lo) * sizeof(T), s));
-        const long long n = (long long)L.big_asm_e.size();
-        mf_init_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, L.d_big_asm_e.p, L.d_big_asm_pos.p, A, pool);
-    }
+    if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, L.n_tiles * sizeof(int), s));
     MFArgs a = mf_args(c, A);
     a.epoch = L.epoch;
-    const int blocks = std::min(sm_count() * 3, std::max(a.n_tasks, 1));
-    mf_factor_kernel<T><<<blocks, MF_THREADS, MF_SMEM_DOUBLES * sizeof(double), s>>>(a, pool);
+    const int blocks = std::min(sm_count() * MF_CTAS_PER_SM, std::max(a.n_tasks, 1));
+    mf_factor_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool);
     VGB_CUDA(cudaGetLastError());
 }
 
@@ -532,6 +674,14 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.epoch = L.epoch;
     a.spin_limit = 1u << 22;
     const size_t smem = (size_t)std::max<long long>(L.mf_max_m, 1) * sizeof(T);
+    static size_t smem_set[2] = {0, 0};
+    size_t& cur = smem_set[sizeof(T) == 4 ? 0 : 1];
+    if (smem > 48 * 1024 && smem > cur) {
+        VGB_REQUIRE(smem <= 200 * 1024, "front too large for the solve kernels' shared memory");
+        VGB_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        VGB_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cur = smem;
+    }
     const int blocks = std::min(sm_count() * 4, L.nsn);
     mf_fwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, rhsM, y, cv);
     a.counter = L.d_counters.p + 2;

@@ -168,6 +168,24 @@ void build_pattern(Circuit& c) {
         if (c.csr_src_ptr[e + 1] - c.csr_src_ptr[e] > HEAVY_LIST) c.heavy_csr.push_back(e);
     for (int r = 0; r < n_unk; ++r)
         if (c.res_src_ptr[r + 1] - c.res_src_ptr[r] > HEAVY_LIST) c.heavy_row.push_back(r);
+    // split them into fixed chunks: one block per chunk, chunks summed in order
+    c.hchunk_item.clear();
+    c.hchunk_lo.clear();
+    c.hchunk_hi.clear();
+    c.hitem_ptr.assign(1, 0);
+    const int n_items = (int)(c.heavy_csr.size() + c.heavy_row.size());
+    for (int it = 0; it < n_items; ++it) {
+        const bool is_csr = it < (int)c.heavy_csr.size();
+        const int item = is_csr ? c.heavy_csr[it] : c.heavy_row[it - c.heavy_csr.size()];
+        const int lo = is_csr ? c.csr_src_ptr[item] : c.res_src_ptr[item];
+        const int hi = is_csr ? c.csr_src_ptr[item + 1] : c.res_src_ptr[item + 1];
+        for (int b = lo; b < hi; b += HEAVY_CHUNK) {
+            c.hchunk_item.push_back(it);
+            c.hchunk_lo.push_back(b);
+            c.hchunk_hi.push_back(std::min(b + HEAVY_CHUNK, hi));
+        }
+        c.hitem_ptr.push_back((int)c.hchunk_item.size());
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -228,6 +246,141 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
 // Supernodes are numbered by first column, which lists children before
 // parents.
 // ---------------------------------------------------------------------------
+
+// Order the factorisation tasks for the persistent kernel, whose CTAs claim
+// tasks in list order and then wait for their inputs.  A list schedule
+// (highest bottom level first, simulated on SCHED_SLOTS workers with rough
+// per-task costs) puts each task where it is expected to become ready, so
+// CTAs do not park behind one front's chain of dependent tiles while
+// independent subtrees wait further down the list.  Start order is a
+// topological order, which keeps every wait on an earlier task.
+constexpr int SCHED_SLOTS = 600;
+
+static void schedule_tasks(SparseLU& L) {
+    const int nt = (int)L.task_type.size();
+    if (nt == 0) return;
+    const int ns = L.nsn;
+    // index of each task inside its front's block
+    std::vector<int> front_task0(ns, -1);
+    for (int t = 0; t < nt; ++t)
+        if (front_task0[L.task_front[t]] < 0) front_task0[L.task_front[t]] = t;
+    auto blk = [&](int s, int k) {  // first task of pivot step k of a large front
+        const int nb = L.fr_nb[s];
+        long long off = 0;
+        for (int q = 0; q < k; ++q) off += (long long)(nb - q) * (nb - q);
+        return front_task0[s] + (int)off;
+    };
+    auto getrf = [&](int s, int k) { return blk(s, k); };
+    auto trsm_l = [&](int s, int i, int k) { return blk(s, k) + 1 + (i - k - 1); };
+    auto trsm_u = [&](int s, int k, int j) { return blk(s, k) + 1 + (L.fr_nb[s] - k - 1) + (j - k - 1); };
+    auto gemm = [&](int s, int i, int j, int k) {
+        const int r = L.fr_nb[s] - k - 1;
+        return blk(s, k) + 1 + 2 * r + (j - k - 1) * r + (i - k - 1);
+    };
+    // the tasks whose completion completes a front
+    std::vector<std::vector<int>> finals(ns);
+    for (int s = 0; s < ns; ++s) {
+        if (!L.fr_big[s]) { finals[s].push_back(front_task0[s]); continue; }
+        const int kb = L.fr_kb[s], nb = L.fr_nb[s];
+        if (nb == kb) { finals[s].push_back(getrf(s, kb - 1)); continue; }
+        for (int j = kb; j < nb; ++j)
+            for (int i = kb; i < nb; ++i) finals[s].push_back(gemm(s, i, j, kb - 1));
+    }
+    std::vector<std::vector<int>> pred(nt);
+    std::vector<double> cost(nt, 0.0);
+    auto children_done = [&](int s, std::vector<int>& v) {
+        for (int q = L.ch_ptr[s]; q < L.ch_ptr[s + 1]; ++q)
+            for (int f : finals[L.ch_idx[q]]) v.push_back(f);
+    };
+    for (int t = 0; t < nt; ++t) {
+        const int s = L.task_front[t], type = L.task_type[t];
+        const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s], w = L.fr_w[s];
+        const int i = L.task_i[t], j = L.task_j[t], k = L.task_k[t];
+        // rough costs in ns: a CTA shares the SM's FP64 pipe with three others (~2 flop/ns)
+        if (type == TASK_SMALL) {
+            double fl = 0;
+            for (long long p = 0; p < w; ++p) fl += 2.0 * (m - p - 1) * (m - p - 1);
+            cost[t] = 2000 + fl / 2 + 2.0 * m * m;
+            children_done(s, pred[t]);
+            continue;
+        }
+        const double tile = FRONT_TILE;
+        if (type == TASK_GETRF) {
+            cost[t] = 3000 + (2.0 / 3.0) * tile * tile * tile / 2;
+            if (k == 0) children_done(s, pred[t]);
+            else pred[t].push_back(gemm(s, k, k, k - 1));
+        } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
+            cost[t] = 2500 + tile * tile * tile / 2;
+            pred[t].push_back(getrf(s, k));
+            if (k > 0) pred[t].push_back(type == TASK_TRSM_L ? gemm(s, i, k, k - 1) : gemm(s, k, j, k - 1));
+        } else {
+            cost[t] = 2000 + 2.0 * tile * tile * tile / 2;
+            pred[t].push_back(trsm_l(s, i, k));
+            pred[t].push_back(trsm_u(s, k, j));
+            if (k > 0) pred[t].push_back(gemm(s, i, j, k - 1));
+        }
+        if (k == 0) cost[t] += 1500;  // first-touch assembly
+    }
+    std::vector<std::vector<int>> succ(nt);
+    std::vector<int> npred(nt, 0);
+    for (int t = 0; t < nt; ++t) {
+        for (int p : pred[t]) {
+            VGB_REQUIRE(p >= 0 && p < nt && p != t, "bad task dependency");
+            succ[p].push_back(t);
+        }
+        npred[t] = (int)pred[t].size();
+    }
+    // bottom levels (tasks were generated in a topological order)
+    std::vector<double> bl(nt, 0.0);
+    for (int t = nt - 1; t >= 0; --t) {
+        double best = 0.0;
+        for (int q : succ[t]) best = std::max(best, bl[q]);
+        bl[t] = cost[t] + best;
+    }
+    // list scheduling simulation
+    using RP = std::pair<double, int>;
+    std::priority_queue<RP> ready;  // highest bottom level first
+    std::priority_queue<RP, std::vector<RP>, std::greater<RP>> events;  // (finish time, task)
+    for (int t = 0; t < nt; ++t)
+        if (npred[t] == 0) ready.push({bl[t], t});
+    std::vector<int> order;
+    order.reserve(nt);
+    int idle = SCHED_SLOTS;
+    double now = 0.0;
+    while ((int)order.size() < nt) {
+        while (idle > 0 && !ready.empty()) {
+            const int t = ready.top().second;
+            ready.pop();
+            order.push_back(t);
+            events.push({now + cost[t], t});
+            --idle;
+        }
+        VGB_REQUIRE(!events.empty(), "task graph has a cycle");
+        now = events.top().first;
+        while (!events.empty() && events.top().first <= now) {
+            const int t = events.top().second;
+            events.pop();
+            ++idle;
+            for (int q : succ[t])
+                if (--npred[q] == 0) ready.push({bl[q], q});
+        }
+    }
+    std::vector<int> pos(nt);
+    for (int r = 0; r < nt; ++r) pos[order[r]] = r;
+    for (int t = 0; t < nt; ++t)
+        for (int p : pred[t]) VGB_REQUIRE(pos[p] < pos[t], "schedule is not topological");
+    auto permute = [&](std::vector<int>& v) {
+        std::vector<int> o(nt);
+        for (int r = 0; r < nt; ++r) o[r] = v[order[r]];
+        v.swap(o);
+    };
+    permute(L.task_type);
+    permute(L.task_front);
+    permute(L.task_i);
+    permute(L.task_j);
+    permute(L.task_k);
+    L.sched_makespan_ns = now;
+}
 
 void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector<std::vector<int>>& lcol,
                   const std::vector<MEntry>& entries) {
@@ -351,74 +504,131 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
         for (auto& pr : asmv[s]) { L.asm_e.push_back(pr.first); L.asm_pos.push_back(pr.second); }
         L.asm_ptr[s + 1] = (long long)L.asm_e.size();
     }
-    // task list for the numeric factorisation, in topological order
+    // task list for the numeric factorisation, in topological order: small
+    // fronts are one task; a large front of order m with w pivots has kb =
+    // ceil(w/32) pivot tiles and nb = kb + ceil((m-w)/32) tiles per dimension,
+    // and for each pivot tile k: GETRF(k), TRSM_L(i,k) and TRSM_U(k,j) for
+    // i, j > k, then GEMM(i,j,k) for i, j > k.  Every task waits only on tasks
+    // that precede it in the list.
     L.fr_cv_off.assign(ns + 1, 0);
     L.task_type.clear();
     L.task_front.clear();
-    L.task_b0.clear();
-    L.task_b1.clear();
-    L.fr_task0.assign(ns, 0);
+    L.task_i.clear();
+    L.task_j.clear();
+    L.task_k.clear();
+    L.fr_big.assign(ns, 0);
+    L.fr_kb.assign(ns, 0);
     L.fr_nb.assign(ns, 0);
+    L.fr_tile0.assign(ns + 1, 0);
+    auto push_task = [&](int type, int s, int i, int j, int k) {
+        L.task_type.push_back(type);
+        L.task_front.push_back(s);
+        L.task_i.push_back(i);
+        L.task_j.push_back(j);
+        L.task_k.push_back(k);
+    };
+    long long ntile = 0;
     for (int s = 0; s < ns; ++s) {
         const int m = (int)(L.fr_ptr[s + 1] - L.fr_ptr[s]);
         const int w = L.fr_w[s], r = m - w;
         L.fr_cv_off[s + 1] = L.fr_cv_off[s] + r;
-        L.fr_task0[s] = (int)L.task_type.size();
+        L.fr_tile0[s] = (int)ntile;
         if (m <= SMALL_FRONT) {
-            L.task_type.push_back(TASK_SMALL);
-            L.task_front.push_back(s);
-            L.task_b0.push_back(0);
-            L.task_b1.push_back(0);
+            push_task(TASK_SMALL, s, 0, 0, 0);
             continue;
         }
-        const int nb = (r + FRONT_TILE - 1) / FRONT_TILE;
-        L.fr_nb[s] = nb;
-        L.task_type.push_back(TASK_DIAG);
-        L.task_front.push_back(s);
-        L.task_b0.push_back(0);
-        L.task_b1.push_back(0);
-        for (int b = 0; b < nb; ++b) {
-            L.task_type.push_back(TASK_PANEL);
-            L.task_front.push_back(s);
-            L.task_b0.push_back(b);
-            L.task_b1.push_back(0);
-        }
-        for (int bj = 0; bj < nb; ++bj)
-            for (int bi = 0; bi < nb; ++bi) {
-                L.task_type.push_back(TASK_SCHUR);
-                L.task_front.push_back(s);
-                L.task_b0.push_back(bi);
-                L.task_b1.push_back(bj);
-            }
-    }
-    // large fronts: zeroed and A-assembled before the factor kernel, filled by their children
-    L.fr_big.assign(ns, 0);
-    L.big_asm_e.clear();
-    L.big_asm_pos.clear();
-    L.big_lo = L.fr_off.empty() ? 0 : L.fr_off.back();
-    L.big_hi = 0;
-    for (int s = 0; s < ns; ++s) {
-        const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s];
-        if (m <= SMALL_FRONT) continue;
+        const int kb = (w + FRONT_TILE - 1) / FRONT_TILE;
+        const int nb = kb + (r + FRONT_TILE - 1) / FRONT_TILE;
         L.fr_big[s] = 1;
-        L.big_lo = std::min(L.big_lo, L.fr_off[s]);
-        L.big_hi = std::max(L.big_hi, L.fr_off[s + 1]);
-        for (long long t = L.asm_ptr[s]; t < L.asm_ptr[s + 1]; ++t) {
-            L.big_asm_e.push_back(L.asm_e[t]);
-            L.big_asm_pos.push_back(L.fr_off[s] + L.asm_pos[t]);
+        L.fr_kb[s] = kb;
+        L.fr_nb[s] = nb;
+        ntile += (long long)nb * nb;
+        for (int k = 0; k < kb; ++k) {
+            push_task(TASK_GETRF, s, k, k, k);
+            for (int i = k + 1; i < nb; ++i) push_task(TASK_TRSM_L, s, i, k, k);
+            for (int j = k + 1; j < nb; ++j) push_task(TASK_TRSM_U, s, k, j, k);
+            for (int j = k + 1; j < nb; ++j)
+                for (int i = k + 1; i < nb; ++i) push_task(TASK_GEMM, s, i, j, k);
         }
     }
-    if (L.big_hi < L.big_lo) L.big_lo = L.big_hi = 0;
-    // statistics
+    L.fr_tile0[ns] = (int)ntile;
+    L.n_tiles = ntile;
+    VGB_REQUIRE(ntile < (1LL << 31) && L.task_type.size() < (1ULL << 31), "too many factorisation tasks");
+    schedule_tasks(L);
+    // first-touch assembly of each tile of a large front: its A entries
+    // (tile-local position r + c * FRONT_TILE_LD) and the blocks of each
+    // child's contribution that land in it, in child order
+    auto tile_lo = [](int t, int kb, int w) { return t < kb ? t * FRONT_TILE : w + (t - kb) * FRONT_TILE; };
+    std::vector<std::vector<std::pair<int, int>>> tasm(ntile);
+    std::vector<std::vector<int>> tchv(ntile);
+    for (int s = 0; s < ns; ++s) {
+        if (!L.fr_big[s]) continue;
+        const int m = (int)(L.fr_ptr[s + 1] - L.fr_ptr[s]);
+        const int w = L.fr_w[s], kb = L.fr_kb[s], nb = L.fr_nb[s];
+        std::vector<int> tile_of(m);
+        for (int t = 0; t < nb; ++t) {
+            const int lo = tile_lo(t, kb, w), hi = t + 1 < nb ? tile_lo(t + 1, kb, w) : m;
+            for (int x = lo; x < hi; ++x) tile_of[x] = t;
+        }
+        for (long long t = L.asm_ptr[s]; t < L.asm_ptr[s + 1]; ++t) {
+            const int pos = L.asm_pos[t];
+            const int li = pos % m, lj = pos / m;
+            const int ti = tile_of[li], tj = tile_of[lj];
+            const int loc = (li - tile_lo(ti, kb, w)) + (lj - tile_lo(tj, kb, w)) * FRONT_TILE_LD;
+            tasm[L.fr_tile0[s] + (long long)ti * nb + tj].push_back({L.asm_e[t], loc});
+        }
+        for (int q = L.ch_ptr[s]; q < L.ch_ptr[s + 1]; ++q) {
+            const int ch = L.ch_idx[q];
+            const int* em = L.em_idx.data() + L.em_ptr[ch];
+            const int rc = (int)(L.em_ptr[ch + 1] - L.em_ptr[ch]);
+            for (int x = 1; x < rc; ++x) VGB_REQUIRE(em[x] > em[x - 1], "extend-add map is not increasing");
+            // range of child contribution rows per tile of the parent
+            std::vector<int> lo(nb, 0), hi(nb, 0);
+            int x = 0;
+            for (int t = 0; t < nb; ++t) {
+                const int end = t + 1 < nb ? tile_lo(t + 1, kb, w) : m;
+                lo[t] = x;
+                while (x < rc && em[x] < end) ++x;
+                hi[t] = x;
+            }
+            for (int tj = 0; tj < nb; ++tj) {
+                if (lo[tj] == hi[tj]) continue;
+                for (int ti = 0; ti < nb; ++ti) {
+                    if (lo[ti] == hi[ti]) continue;
+                    auto& v = tchv[L.fr_tile0[s] + (long long)ti * nb + tj];
+                    v.insert(v.end(), {ch, lo[ti], hi[ti], lo[tj], hi[tj]});
+                }
+            }
+        }
+    }
+    L.tasm_ptr.assign(ntile + 1, 0);
+    L.tch_ptr.assign(ntile + 1, 0);
+    L.tasm_e.clear();
+    L.tasm_pos.clear();
+    L.tch.clear();
+    for (long long t = 0; t < ntile; ++t) {
+        for (auto& pr : tasm[t]) { L.tasm_e.push_back(pr.first); L.tasm_pos.push_back(pr.second); }
+        L.tasm_ptr[t + 1] = (long long)L.tasm_e.size();
+        L.tch.insert(L.tch.end(), tchv[t].begin(), tchv[t].end());
+        L.tch_ptr[t + 1] = (long long)L.tch.size();
+    }
+    // statistics: front flops, longest chain of dependent tasks (a small
+    // front counts 1, a large front 3 per pivot tile: GETRF, TRSM, GEMM)
     L.mf_max_m = 0;
     L.mf_flops = 0;
     L.mf_depth = 0;
-    std::vector<long long> depth(ns, 1);
+    L.crit_path = 0;
+    std::vector<long long> depth(ns, 1), chain(ns, 0);
     for (int s = 0; s < ns; ++s) {
         const long long m = L.fr_ptr[s + 1] - L.fr_ptr[s], w = L.fr_w[s];
         L.mf_max_m = std::max(L.mf_max_m, m);
         for (long long p = 0; p < w; ++p) L.mf_flops += 2 * (m - p - 1) * (m - p - 1) + (m - p - 1);
-        if (L.sn_parent[s] >= 0) depth[L.sn_parent[s]] = std::max(depth[L.sn_parent[s]], depth[s] + 1);
+        chain[s] += L.fr_big[s] ? 3LL * L.fr_kb[s] : 1;
+        L.crit_path = std::max(L.crit_path, chain[s]);
+        if (L.sn_parent[s] >= 0) {
+            depth[L.sn_parent[s]] = std::max(depth[L.sn_parent[s]], depth[s] + 1);
+            chain[L.sn_parent[s]] = std::max(chain[L.sn_parent[s]], chain[s]);
+        }
         L.mf_depth = std::max(L.mf_depth, depth[s]);
     }
 }
@@ -600,35 +810,16 @@ void build_sparse_symbolic(Circuit& c) {
     for (int i = 0; i < nM; ++i)
         for (int k : rowstruct[i]) lcol[k].push_back(i);
 
-    // 6. column storage: [U rows asc][diag][L rows asc]
-    L.col_ptr.assign(nM + 1, 0);
-    L.nU.resize(nM);
+    // 6. statistics of the exact factor and the A entries of M / couplings to F
+    L.nnz_lu = nM;
+    L.flops = 0;
+    L.max_col = 0;
     for (int j = 0; j < nM; ++j) {
-        L.nU[j] = (int)rowstruct[j].size();
-        L.col_ptr[j + 1] = L.col_ptr[j] + rowstruct[j].size() + 1 + lcol[j].size();
+        const long long lc = (long long)lcol[j].size();
+        L.nnz_lu += 2 * lc;
+        L.flops += 2 * lc * lc;
+        L.max_col = std::max(L.max_col, lc + (long long)rowstruct[j].size() + 1);
     }
-    L.nnz_lu = L.col_ptr[nM];
-    L.rows.resize(L.nnz_lu);
-    for (int j = 0; j < nM; ++j) {
-        long long s = L.col_ptr[j];
-        for (int r : rowstruct[j]) L.rows[s++] = r;
-        L.rows[s++] = j;
-        for (int r : lcol[j]) L.rows[s++] = r;
-    }
-    auto slot_of = [&](int i, int j) -> long long {
-        long long s0 = L.col_ptr[j], s1 = L.col_ptr[j + 1];
-        if (i < j) {
-            auto b = L.rows.begin() + s0, e = b + L.nU[j];
-            auto it = std::lower_bound(b, e, i);
-            return (it != e && *it == i) ? (long long)(it - L.rows.begin()) : -1;
-        }
-        if (i == j) return s0 + L.nU[j];
-        auto b = L.rows.begin() + s0 + L.nU[j] + 1, e = L.rows.begin() + s1;
-        auto it = std::lower_bound(b, e, i);
-        return (it != e && *it == i) ? (long long)(it - L.rows.begin()) : -1;
-    };
-    // 7. A -> factor slot (M x M entries) and the F couplings of each M row
-    L.f2a.assign(L.nnz_lu, -1);
     L.pre_ptr.assign(nM + 1, 0);
     std::vector<std::vector<std::pair<int, int>>> pre(nM);
     std::vector<MEntry> m_entries;
@@ -639,9 +830,6 @@ void build_sparse_symbolic(Circuit& c) {
         for (int e = c.indptr[ra]; e < c.indptr[ra + 1]; ++e) {
             const int col = c.indices[e];
             if (kind[col] == 0) {
-                long long s = slot_of(i, L.qinv[col]);
-                VGB_REQUIRE(s >= 0, "symbolic factor misses an entry of A");
-                L.f2a[s] = e;
                 m_entries.push_back({e, i, L.qinv[col]});
             } else if (kind[col] == 1) {
                 pre[i].push_back({e, fidx[col]});
@@ -656,68 +844,16 @@ void build_sparse_symbolic(Circuit& c) {
         for (auto& pe : pre[i]) { L.pre_e.push_back(pe.first); L.pre_f.push_back(pe.second); }
         L.pre_ptr[i + 1] = (int)L.pre_e.size();
     }
-    // 8. left-looking update maps
-    L.ustart.assign(nM + 1, 0);
-    for (int j = 0; j < nM; ++j) L.ustart[j + 1] = L.ustart[j] + L.nU[j];
-    const long long nUtot = L.ustart[nM];
-    L.umap_ptr.assign(nUtot + 1, 0);
-    L.ukl.assign(std::max<long long>(nUtot, 1), 0);
-    L.umap.clear();
-    std::vector<int> lookup(nM, -1);
-    long long u = 0;
-    for (int j = 0; j < nM; ++j) {
-        long long s0 = L.col_ptr[j], s1 = L.col_ptr[j + 1];
-        for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = (int)(s - s0);
-        for (int t = 0; t < L.nU[j]; ++t, ++u) {
-            int k = rowstruct[j][t];
-            L.ukl[u] = L.col_ptr[k] + L.nU[k] + 1;
-            for (int i : lcol[k]) {
-                int pos = lookup[i];
-                VGB_REQUIRE(pos >= 0, "fill pattern is not closed under elimination");
-                L.umap.push_back(pos);
-            }
-            L.umap_ptr[u + 1] = (long long)L.umap.size();
-        }
-        for (long long s = s0; s < s1; ++s) lookup[L.rows[s]] = -1;
-    }
-    L.flops = 2 * (long long)L.umap.size();
     {
-        std::vector<long long> h(nM, 1), cp(nM, 0);
+        std::vector<long long> h(nM, 1);
         L.etree_height = nM ? 1 : 0;
-        L.max_col = 0;
-        L.crit_path = 0;
         for (int j = 0; j < nM; ++j) {
-            long long best = 0;
-            for (int k : rowstruct[j]) best = std::max(best, cp[k]);
-            cp[j] = best + L.nU[j] + 1;
-            L.crit_path = std::max(L.crit_path, cp[j]);
-            L.max_col = std::max(L.max_col, L.col_ptr[j + 1] - L.col_ptr[j]);
             if (parent[j] >= 0) h[parent[j]] = std::max(h[parent[j]], h[j] + 1);
             L.etree_height = std::max(L.etree_height, h[j]);
         }
     }
+    // 7. supernodes, fronts, tile tasks
     build_fronts(L, parent, lcol, m_entries);
-    // 9. row access for the triangular solves
-    L.lrow_ptr.assign(nM + 1, 0);
-    L.lrow_pos.clear();
-    L.lrow_col.clear();
-    for (int i = 0; i < nM; ++i) {
-        for (int k : rowstruct[i]) {
-            L.lrow_pos.push_back(slot_of(i, k));
-            L.lrow_col.push_back(k);
-        }
-        L.lrow_ptr[i + 1] = (long long)L.lrow_pos.size();
-    }
-    L.urow_ptr.assign(nM + 1, 0);
-    L.urow_pos.clear();
-    L.urow_col.clear();
-    for (int i = 0; i < nM; ++i) {
-        for (int j : lcol[i]) {
-            L.urow_pos.push_back(slot_of(i, j));
-            L.urow_col.push_back(j);
-        }
-        L.urow_ptr[i + 1] = (long long)L.urow_pos.size();
-    }
 }
 
 } // namespace vgb

@@ -110,20 +110,21 @@ __global__ void assemble_kernel(AssembleArgs a) {
     finish_row(a, r, fr, q, mc);
 }
 
-// One block per heavy CSR entry or heavy node row; fixed-order block reduction.
-__global__ void __launch_bounds__(256) assemble_heavy_kernel(AssembleArgs a) {
-    __shared__ double s_sum[256], s_q[256], s_max[256];
-    const int b = blockIdx.x;
-    const bool is_csr = b < a.n_heavy_csr;
-    const int item = is_csr ? a.heavy_csr[b] : a.heavy_row[b - a.n_heavy_csr];
-    const int e0 = is_csr ? a.csr_src_ptr[item] : a.res_src_ptr[item];
-    const int e1 = is_csr ? a.csr_src_ptr[item + 1] : a.res_src_ptr[item + 1];
+// Heavy CSR entries and node rows: one block per HEAVY_CHUNK-entry chunk
+// reduces it with a fixed tree, then one thread per item adds its chunks in
+// order, so the sums are deterministic.
+constexpr int HEAVY_THREADS = 256;
+__global__ void __launch_bounds__(HEAVY_THREADS) assemble_heavy_kernel(AssembleArgs a) {
+    __shared__ double s_sum[HEAVY_THREADS], s_q[HEAVY_THREADS], s_max[HEAVY_THREADS];
+    const int ch = blockIdx.x;
+    const int it = a.hchunk_item[ch];
+    const bool is_csr = it < a.n_heavy_csr;
     double s = 0.0, q = 0.0, m = 0.0;
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    for (int e = a.hchunk_lo[ch] + threadIdx.x; e < a.hchunk_hi[ch]; e += HEAVY_THREADS) {
         if (is_csr) {
             s += a.contrib[a.csr_src[e]];
         } else {
-            double v = nan0(a.contrib[a.res_src[e]]);
+            const double v = nan0(a.contrib[a.res_src[e]]);
             s += v;
             m = fmax(m, fabs(v));
             q += nan0(a.contrib[a.rq_src[e]]);
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(256) assemble_heavy_kernel(AssembleArgs a) {
     s_q[threadIdx.x] = q;
     s_max[threadIdx.x] = m;
     __syncthreads();
-    for (int o = blockDim.x / 2; o; o >>= 1) {
+    for (int o = HEAVY_THREADS / 2; o; o >>= 1) {
         if ((int)threadIdx.x < o) {
             s_sum[threadIdx.x] += s_sum[threadIdx.x + o];
             s_q[threadIdx.x] += s_q[threadIdx.x + o];
@@ -141,14 +142,29 @@ __global__ void __launch_bounds__(256) assemble_heavy_kernel(AssembleArgs a) {
         }
         __syncthreads();
     }
-    if (threadIdx.x != 0) return;
-    if (is_csr) {
-        double v = s_sum[0];
-        if (a.csr_diag[item]) v += a.gdiag;
-        v += a.csr_const[item];
-        a.csr_vals[item] = v;
+    if (threadIdx.x == 0) {
+        a.hpart[ch] = s_sum[0];
+        a.hpart[a.n_hchunk + ch] = s_q[0];
+        a.hpart[2 * a.n_hchunk + ch] = s_max[0];
+    }
+}
+
+__global__ void assemble_heavy_finish_kernel(AssembleArgs a) {
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= a.n_heavy_csr + a.n_heavy_row) return;
+    double s = 0.0, q = 0.0, m = 0.0;
+    for (int ch = a.hitem_ptr[it]; ch < a.hitem_ptr[it + 1]; ++ch) {
+        s += a.hpart[ch];
+        q += a.hpart[a.n_hchunk + ch];
+        m = fmax(m, a.hpart[2 * a.n_hchunk + ch]);
+    }
+    if (it < a.n_heavy_csr) {
+        const int item = a.heavy_csr[it];
+        if (a.csr_diag[item]) s += a.gdiag;
+        s += a.csr_const[item];
+        a.csr_vals[item] = s;
     } else {
-        finish_row(a, item, s_sum[0], s_q[0], s_max[0]);
+        finish_row(a, a.heavy_row[it - a.n_heavy_csr], s, q, m);
     }
 }
 
@@ -156,7 +172,10 @@ void launch_assemble(const AssembleArgs& a, cudaStream_t s) {
     const long long total = (long long)a.nnz + a.n_unk + a.n_vsrc;
     if (total == 0) return;
     assemble_kernel<<<ceil_div(total, 256), 256, 0, s>>>(a);
-    if (a.n_heavy_csr + a.n_heavy_row) assemble_heavy_kernel<<<a.n_heavy_csr + a.n_heavy_row, 256, 0, s>>>(a);
+    if (a.n_heavy_csr + a.n_heavy_row) {
+        assemble_heavy_kernel<<<a.n_hchunk, HEAVY_THREADS, 0, s>>>(a);
+        assemble_heavy_finish_kernel<<<ceil_div(a.n_heavy_csr + a.n_heavy_row, 64), 64, 0, s>>>(a);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -240,16 +259,27 @@ __global__ void lu_pre_kernel(int nM, int nF, const int* brow, const int* pre_pt
 }
 
 
-// Singletons solved last: x_c = (b_c - sum_j B(c, j) x_j) / B(c, c), one warp per row.
-__global__ void lu_post_kernel(int nL, const int* l_col, const int* l_arow, const int* l_diag_e, const int* l_ptr,
-                               const int* l_e, const int* l_x, const double* A, const double* b, double* xout) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= nL) return;
+// Singletons solved last: x_c = (b_c - sum_j B(c, j) x_j) / B(c, c), one block
+// per row (the supply-rail rows hold one entry per connected device) with a
+// fixed-order tree reduction.
+constexpr int POST_THREADS = 256;
+__global__ void __launch_bounds__(POST_THREADS) lu_post_kernel(int nL, const int* l_col, const int* l_arow,
+                                                              const int* l_diag_e, const int* l_ptr, const int* l_e,
+                                                              const int* l_x, const double* A, const double* b,
+                                                              double* xout) {
+    __shared__ double part[POST_THREADS / 32];
+    const int row = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double acc = 0.0;
-    for (int e = l_ptr[warp] + lane; e < l_ptr[warp + 1]; e += 32) acc += A[l_e[e]] * xout[l_x[e]];
+    for (int e = l_ptr[row] + threadIdx.x; e < l_ptr[row + 1]; e += POST_THREADS) acc += A[l_e[e]] * xout[l_x[e]];
     for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) xout[l_col[warp]] = (b[l_arow[warp]] - acc) / A[l_diag_e[warp]];
+    if (lane == 0) part[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < POST_THREADS / 32; ++w) s += part[w];
+        xout[l_col[row]] = (b[l_arow[row]] - s) / A[l_diag_e[row]];
+    }
 }
 
 
@@ -266,7 +296,7 @@ static void lu_solve_once(Circuit& c, const double* A, const double* rhs, double
                                                                 L.d_f_diag_e.p, A, rhs, rhsM, x);
     if (nM) mf_solve_t<T>(c, rhsM, ybuf, xbuf, x, s);
     if (nL)
-        lu_post_kernel<<<ceil_div((long long)nL * 32, 256), 256, 0, s>>>(nL, L.d_l_col.p, L.d_l_arow.p,
+        lu_post_kernel<<<nL, POST_THREADS, 0, s>>>(nL, L.d_l_col.p, L.d_l_arow.p,
                                                                         L.d_l_diag_e.p, L.d_l_ptr.p, L.d_l_e.p,
                                                                         L.d_l_x.p, A, rhs, x);
     VGB_CUDA(cudaGetLastError());

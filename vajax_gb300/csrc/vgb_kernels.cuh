@@ -22,6 +22,9 @@ struct AssembleArgs {
     NRStatus* st;
     const int* heavy_csr; int n_heavy_csr;   // CSR entries with gather lists longer than HEAVY_LIST
     const int* heavy_row; int n_heavy_row;   // node rows with gather lists longer than HEAVY_LIST
+    const int* hchunk_item; const int* hchunk_lo; const int* hchunk_hi; const int* hitem_ptr;
+    int n_hchunk;
+    double* hpart;                           // [3][n_hchunk] partials of the heavy chunks
 };
 
 void launch_assemble(const AssembleArgs& a, cudaStream_t s);

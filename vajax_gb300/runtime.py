@@ -110,7 +110,8 @@ class DeviceCircuit:
         out = np.zeros(16, np.int64)
         self._check(self.lib.vgb_solver_info(self.h, out.ctypes.data_as(_lib.i64p)))
         keys = ["n_aug", "nnz", "nnz_lu", "lu_flops", "etree_height", "max_col", "crit_path", "contrib_slots",
-                "supernodes", "max_front", "front_storage", "front_flops", "front_depth"]
+                "supernodes", "max_front", "front_storage", "front_flops", "front_depth", "sched_makespan_ns",
+                "tasks"]
         return dict(zip(keys, map(int, out)))
 
     def solver_order(self):
