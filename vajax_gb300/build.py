@@ -22,7 +22,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libvajax_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["vgb_api.cu", "vgb_transient.cu", "vgb_kernels.cu", "vgb_frontal.cu", "vgb_host.cpp"]
+SOURCES = ["vgb_api.cu", "vgb_transient.cu", "vgb_kernels.cu", "vgb_frontal.cu", "vgb_dense_static.cu",
+           "vgb_host.cpp"]
 
 
 def nvcc() -> str:
