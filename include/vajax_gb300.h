@@ -107,6 +107,13 @@ int vgb_profile(void* h, int mode, double* out);
  * (vajax/analysis/transient/full_mna.py:344-690). */
 int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps);
 
+/* Switch the LU precision of a finalized circuit (same meaning as finalize's
+ * arguments); the front storage of a precision not used before is allocated
+ * on the first switch to it.  Mirrors the reference's choice between the f64
+ * and the f32-with-refinement solvers (full_mna.py:584-684); a caller can run
+ * the DC operating point in FP64 and the transient in FP32. */
+int vgb_set_precision(void* h, int precision, int refine_sweeps);
+
 /* Pattern and maps (bit-exact contract with the reference) ----------------- */
 
 /* Sizes: n_aug, CSR nnz, LU nnz, LU flops (2 * multiply-adds). */

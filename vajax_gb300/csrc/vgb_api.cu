@@ -43,6 +43,21 @@ static void require_final(Circuit* c) {
     if (!c->finalized) throw Error(VGB_ERR_STATE, "circuit is not finalized");
 }
 
+// front pools of the requested precision (allocated once, kept)
+static void ensure_pools(Circuit& c, int precision) {
+    SparseLU& L = c.lu;
+    const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
+    const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
+    if (precision == 1 && !L.d_pool32.p) {
+        L.d_pool32.alloc(pool);
+        L.d_cv32.alloc(cvn);
+    }
+    if (precision == 0 && !L.d_pool64.p) {
+        L.d_pool64.alloc(pool);
+        L.d_cv64.alloc(cvn);
+    }
+}
+
 static void require_analyzed(Circuit* c) {
     if (!c->analyzed) throw Error(VGB_ERR_STATE, "circuit is not analyzed (call vgb_circuit_analyze)");
 }
@@ -331,6 +346,19 @@ int vgb_profile(void* h, int mode, double* out) {
     });
 }
 
+int vgb_set_precision(void* h, int precision, int refine_sweeps) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        VGB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (FP64) or 1 (FP32+refinement)");
+        VGB_REQUIRE(refine_sweeps >= 0 && refine_sweeps <= 3, "refine_sweeps must be in [0, 3]");
+        ensure_pools(*c, precision);
+        c->solver_kind = precision;
+        c->refine_sweeps = refine_sweeps;
+    });
+}
+
 int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
@@ -422,6 +450,8 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         up64(L.d_cv_off, L.fr_cv_off);
         up64(L.d_tasm_ptr, L.tasm_ptr);
         up64(L.d_tch_ptr, L.tch_ptr);
+        up64(L.d_fg_ptr, L.fg_ptr);
+        up64(L.d_fg_src, L.fg_src);
         up(L.d_fr_idx, L.fr_idx);
         up(L.d_fr_w, L.fr_w);
         up(L.d_sn_parent, L.sn_parent);
@@ -445,13 +475,7 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         L.d_tver.alloc(std::max<long long>(L.n_tiles, 1));
         const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
         const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
-        if (precision == 1) {
-            L.d_pool32.alloc(pool);
-            L.d_cv32.alloc(cvn);
-        } else {
-            L.d_pool64.alloc(pool);
-            L.d_cv64.alloc(cvn);
-        }
+        ensure_pools(*c, precision);
         L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
         L.d_mf_flags.zero(c->stream);
         L.d_mf_count.alloc(std::max(L.nsn, 1));

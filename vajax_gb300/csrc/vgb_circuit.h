@@ -127,6 +127,8 @@ struct SparseLU {
     std::vector<int> asm_e, asm_pos;                  // A slot, position r + c*m inside the front
     long long mf_max_m = 0, mf_flops = 0, mf_depth = 0;
     std::vector<long long> fr_cv_off;                 // forward-solve contribution vector offsets
+    std::vector<long long> fg_ptr;                    // per front row (fr_idx numbering): children's cv entries ...
+    std::vector<long long> fg_src;                    // ... added to it, in child order (offsets into cv)
     // task list and tiles of the large fronts
     std::vector<int> task_type, task_front, task_i, task_j, task_k;
     std::vector<int> fr_big;                          // 1 = front handled by tile tasks
@@ -139,7 +141,7 @@ struct SparseLU {
     std::vector<long long> tch_ptr;                   // per tile: child blocks {child, r0, r1, c0, c1}
     std::vector<int> tch;
     // device mirrors
-    DevBuf<long long> d_fr_ptr, d_fr_off, d_em_ptr, d_asm_ptr, d_cv_off, d_tasm_ptr, d_tch_ptr;
+    DevBuf<long long> d_fr_ptr, d_fr_off, d_em_ptr, d_asm_ptr, d_cv_off, d_tasm_ptr, d_tch_ptr, d_fg_ptr, d_fg_src;
     DevBuf<int> d_fr_idx, d_fr_w, d_sn_parent, d_ch_ptr, d_ch_idx, d_em_idx, d_asm_e, d_asm_pos;
     DevBuf<int> d_task_type, d_task_front, d_task_i, d_task_j, d_task_k;
     DevBuf<int> d_fr_big, d_fr_kb, d_fr_nb, d_fr_tile0, d_tasm_e, d_tasm_pos, d_tch;

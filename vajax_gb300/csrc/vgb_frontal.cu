@@ -424,6 +424,8 @@ struct MFSolveArgs {
     const long long* em_ptr;
     const int* em_idx;
     const long long* cv_off;
+    const long long* fg_ptr;   // per front row: children's update entries, in child order
+    const long long* fg_src;
     const int* q;          // B index of each permuted M index
     int* flags;            // fwd [ns], bwd [ns]
     int* counter;
@@ -458,16 +460,15 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
         const int w = a.fr_w[S];
         const int* idx = a.fr_idx + a.fr_ptr[S];
         const T* F = pool + a.fr_off[S];
-        for (int i = threadIdx.x; i < m; i += blockDim.x) u[i] = i < w ? rhs[idx[i]] : (T)0;
-        __syncthreads();
-        for (int q = a.ch_ptr[S]; q < a.ch_ptr[S + 1]; ++q) {
-            const int C = a.ch_idx[q];
-            const int rc = (int)(a.cv_off[C + 1] - a.cv_off[C]);
-            const int* em = a.em_idx + a.em_ptr[C];
-            const T* cvc = cv + a.cv_off[C];
-            for (int i = threadIdx.x; i < rc; i += blockDim.x) u[em[i]] += __ldcg(cvc + i);
-            __syncthreads();
+        {
+            const long long* gp = a.fg_ptr + a.fr_ptr[S];
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                T v = i < w ? rhs[idx[i]] : (T)0;
+                for (long long e = gp[i]; e < gp[i + 1]; ++e) v += __ldcg(cv + a.fg_src[e]);
+                u[i] = v;
+            }
         }
+        __syncthreads();
         for (int p0 = 0; p0 < w; p0 += 32) {
             const int p1 = min(p0 + 32, w);
             if (warp == 0) {
@@ -529,11 +530,26 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
         for (int j = threadIdx.x; j < m - w; j += blockDim.x) xt[j] = __ldcg(xs + idx[w + j]);
         __syncthreads();
         // z = y_S - U12 x_tail: one pivot row per thread, coalesced down each column
-        for (int p = threadIdx.x; p < w; p += blockDim.x) {
-            T s = (T)0;
-#pragma unroll 8
-            for (int j = 0; j < m - w; ++j) s += F[p + (long long)(w + j) * m] * xt[j];
-            z[p] = y[idx[p]] - s;
+        {
+            // P lanes over pivot rows (coalesced down each column), G groups over tail columns;
+            // the G partial sums of a row are added in group order
+            int P = 32;
+            while (P > 1 && P / 2 >= w) P >>= 1;
+            const int G = MF_THREADS / P;
+            T* part = z + m;  // [G][w]
+            const int pl = threadIdx.x % P, g = threadIdx.x / P;
+            for (int p = pl; p < w; p += P) {
+                T s = (T)0;
+#pragma unroll 4
+                for (int j = g; j < m - w; j += G) s += F[p + (long long)(w + j) * m] * xt[j];
+                part[g * w + p] = s;
+            }
+            __syncthreads();
+            for (int p = threadIdx.x; p < w; p += blockDim.x) {
+                T s = (T)0;
+                for (int q = 0; q < G; ++q) s += part[q * w + p];
+                z[p] = y[idx[p]] - s;
+            }
         }
         __syncthreads();
         for (int p1 = w; p1 > 0; p1 -= 32) {
@@ -666,6 +682,8 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.em_ptr = L.d_em_ptr.p;
     a.em_idx = L.d_em_idx.p;
     a.cv_off = L.d_cv_off.p;
+    a.fg_ptr = L.d_fg_ptr.p;
+    a.fg_src = L.d_fg_src.p;
     a.q = L.d_q.p;
     a.flags = L.d_mf_flags.p + 2 * (size_t)L.nsn;
     a.counter = L.d_counters.p + 1;
@@ -673,7 +691,8 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.err = &c.d_status.p->dev_err;
     a.epoch = L.epoch;
     a.spin_limit = 1u << 22;
-    const size_t smem = (size_t)std::max<long long>(L.mf_max_m, 1) * sizeof(T);
+    // bwd: z and x_tail (m) plus the partial sums of U12 x_tail (at most max(4 w, 128) <= 4 m + 128)
+    const size_t smem = (size_t)(5 * std::max<long long>(L.mf_max_m, 1) + MF_THREADS) * sizeof(T);
     static size_t smem_set[2] = {0, 0};
     size_t& cur = smem_set[sizeof(T) == 4 ? 0 : 1];
     if (smem > 48 * 1024 && smem > cur) {

@@ -553,6 +553,23 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
     }
     L.fr_tile0[ns] = (int)ntile;
     L.n_tiles = ntile;
+    // forward solve: each front row gathers its children's update entries in child order
+    {
+        std::vector<std::vector<long long>> g(L.fr_idx.size());
+        for (int s = 0; s < ns; ++s)
+            for (int q = L.ch_ptr[s]; q < L.ch_ptr[s + 1]; ++q) {
+                const int ch = L.ch_idx[q];
+                const int rc = (int)(L.em_ptr[ch + 1] - L.em_ptr[ch]);
+                for (int x = 0; x < rc; ++x)
+                    g[L.fr_ptr[s] + L.em_idx[L.em_ptr[ch] + x]].push_back(L.fr_cv_off[ch] + x);
+            }
+        L.fg_ptr.assign(L.fr_idx.size() + 1, 0);
+        L.fg_src.clear();
+        for (size_t r = 0; r < g.size(); ++r) {
+            L.fg_src.insert(L.fg_src.end(), g[r].begin(), g[r].end());
+            L.fg_ptr[r + 1] = (long long)L.fg_src.size();
+        }
+    }
     VGB_REQUIRE(ntile < (1LL << 31) && L.task_type.size() < (1ULL << 31), "too many factorisation tasks");
     schedule_tasks(L);
     // first-touch assembly of each tile of a large front: its A entries

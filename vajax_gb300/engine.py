@@ -185,6 +185,19 @@ class CircuitEngine:
         return V
 
     def initial_state(self):
+        """DC operating point (or initial conditions).  The mixed-precision
+        engine solves it with the FP64 LU and switches back to FP32 after."""
+        dev = self.device
+        prec = getattr(dev, "precision", 0)
+        if prec == 0:
+            return self._initial_state()
+        dev.set_precision(0)
+        try:
+            return self._initial_state()
+        finally:
+            dev.set_precision(prec)
+
+    def _initial_state(self):
         import torch
         rc = self.rc
         dev = self.device

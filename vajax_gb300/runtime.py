@@ -40,6 +40,7 @@ class DeviceCircuit:
     def __init__(self, rc: ResolvedCircuit, precision: int = 0, refine_sweeps: int = 3, gmin: float = 1e-12,
                  device: bool = True):
         self.rc = rc
+        self.precision = precision
         self.lib = _lib.load()
         h = C.c_void_p()
         vp_ = np.ascontiguousarray(rc.vsrc_p, np.int32)
@@ -86,6 +87,11 @@ class DeviceCircuit:
 
     def _check(self, code):
         _lib.check(code, self.h)
+
+    def set_precision(self, precision: int, refine_sweeps: int = 3):
+        """0: FP64 LU; 1: FP32 LU + FP64-residual refinement."""
+        self._check(self.lib.vgb_set_precision(self.h, int(precision), int(refine_sweeps)))
+        self.precision = int(precision)
 
     def close(self):
         if self.h is not None:
