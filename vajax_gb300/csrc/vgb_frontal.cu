@@ -227,84 +227,105 @@ __device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, i
     }
 }
 
-// LU without pivoting of the leading n x n block of a tile; warp 0 holds one
-// row per lane in registers.
+// The tile kernels below spread each elimination step over the CTA's four
+// warps (one per SM sub-partition: FP64 issue is the bottleneck on this part)
+// and exchange the step's pivot row or column through shared memory.
+constexpr int NWARP = MF_THREADS / 32;
+constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
+
+// LU without pivoting of the leading n x n block of a tile.  lane = row; warp
+// g owns columns g, g + 4, ... in registers.
 template <typename T>
-__device__ void getrf_tile(T* t, int n, int* err) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        T a[FRONT_TILE];
+__device__ void getrf_tile(T* t, int n, int* err, T* xch) {
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    T a[QPW];
 #pragma unroll
-        for (int c = 0; c < FRONT_TILE; ++c) a[c] = t[lane + c * LD];
+    for (int q = 0; q < QPW; ++q) a[q] = t[lane + (g + NWARP * q) * LD];
 #pragma unroll
-        for (int p = 0; p < FRONT_TILE; ++p) {
-            if (p < n) {
-                T piv = __shfl_sync(0xffffffffu, a[p], p);
+    for (int p = 0; p < FRONT_TILE; ++p) {
+        if (p < n) {
+            if (g == (p & (NWARP - 1))) {
+                // owner of column p: pivot, multipliers L(:, p) for the other warps
+                const int qp = p / NWARP;
+                T piv = __shfl_sync(0xffffffffu, a[qp], p);
                 if (piv == (T)0 || !isfinite((double)piv)) {
                     piv = (T)1e-30;
-                    if (lane == p) a[p] = piv;
+                    if (lane == p) a[qp] = piv;
                     if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
                 }
-                if (lane > p) a[p] /= piv;
-#pragma unroll
-                for (int c = p + 1; c < FRONT_TILE; ++c) {
-                    if (c < n) {
-                        const T u = __shfl_sync(0xffffffffu, a[c], p);
-                        if (lane > p) a[c] -= a[p] * u;
-                    }
-                }
+                if (lane > p) a[qp] /= piv;
+                xch[lane] = a[qp];
             }
-        }
+            __syncthreads();
+            const T l = xch[lane];
 #pragma unroll
-        for (int c = 0; c < FRONT_TILE; ++c) t[lane + c * LD] = a[c];
+            for (int q = 0; q < QPW; ++q) {
+                const int c = g + NWARP * q;
+                const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
+                if (c > p && c < n && lane > p) a[q] -= l * u;
+            }
+            __syncthreads();
+        }
     }
+#pragma unroll
+    for (int q = 0; q < QPW; ++q) t[lane + (g + NWARP * q) * LD] = a[q];
     __syncthreads();
 }
 
-// x := x U^-1 with U the upper triangle (with diagonal) of the n x n tile d;
-// warp 0, one row of x per lane.
+// x := x U^-1 with U the upper triangle (with diagonal) of the n x n tile d.
+// lane = row of x; warp g owns columns g, g + 4, ...
 template <typename T>
-__device__ void trsm_l_tile(T* x, const T* d, int n) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        T a[FRONT_TILE];
+__device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    T a[QPW];
 #pragma unroll
-        for (int c = 0; c < FRONT_TILE; ++c) a[c] = x[lane + c * LD];
+    for (int q = 0; q < QPW; ++q) a[q] = x[lane + (g + NWARP * q) * LD];
 #pragma unroll
-        for (int c = 0; c < FRONT_TILE; ++c) {
-            if (c < n) {
-                a[c] /= d[c + c * LD];
-#pragma unroll
-                for (int c2 = c + 1; c2 < FRONT_TILE; ++c2)
-                    if (c2 < n) a[c2] -= a[c] * d[c + c2 * LD];
+    for (int c = 0; c < FRONT_TILE; ++c) {
+        if (c < n) {
+            if (g == (c & (NWARP - 1))) {
+                a[c / NWARP] /= d[c + c * LD];
+                xch[lane] = a[c / NWARP];
             }
-        }
+            __syncthreads();
+            const T xc = xch[lane];
 #pragma unroll
-        for (int c = 0; c < FRONT_TILE; ++c) x[lane + c * LD] = a[c];
+            for (int q = 0; q < QPW; ++q) {
+                const int c2 = g + NWARP * q;
+                if (c2 > c && c2 < n) a[q] -= xc * d[c + c2 * LD];
+            }
+            __syncthreads();
+        }
     }
+#pragma unroll
+    for (int q = 0; q < QPW; ++q) x[lane + (g + NWARP * q) * LD] = a[q];
     __syncthreads();
 }
 
-// x := L^-1 x with L the unit lower triangle of the n x n tile d; warp 0, one
-// column of x per lane.
+// x := L^-1 x with L the unit lower triangle of the n x n tile d.  lane =
+// column of x; warp g owns rows g, g + 4, ...
 template <typename T>
-__device__ void trsm_u_tile(T* x, const T* d, int n) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        T a[FRONT_TILE];
+__device__ void trsm_u_tile(T* x, const T* d, int n, T* xch) {
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    T a[QPW];
 #pragma unroll
-        for (int r = 0; r < FRONT_TILE; ++r) a[r] = x[r + lane * LD];
+    for (int q = 0; q < QPW; ++q) a[q] = x[(g + NWARP * q) + lane * LD];
 #pragma unroll
-        for (int r = 0; r < FRONT_TILE; ++r) {
-            if (r < n) {
+    for (int r = 0; r < FRONT_TILE; ++r) {
+        if (r < n) {
+            if (g == (r & (NWARP - 1))) xch[lane] = a[r / NWARP];  // row r is final
+            __syncthreads();
+            const T yr = xch[lane];
 #pragma unroll
-                for (int r2 = r + 1; r2 < FRONT_TILE; ++r2)
-                    if (r2 < n) a[r2] -= d[r2 + r * LD] * a[r];
+            for (int q = 0; q < QPW; ++q) {
+                const int r2 = g + NWARP * q;
+                if (r2 > r && r2 < n) a[q] -= d[r2 + r * LD] * yr;
             }
+            __syncthreads();
         }
-#pragma unroll
-        for (int r = 0; r < FRONT_TILE; ++r) x[r + lane * LD] = a[r];
     }
+#pragma unroll
+    for (int q = 0; q < QPW; ++q) x[(g + NWARP * q) + lane * LD] = a[q];
     __syncthreads();
 }
 
@@ -368,7 +389,7 @@ __global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(M
             if (k == 0) assemble_tile<T>(a, tb, T0, 0, 0, pool);
             else load_tile<T>(T0, FS, m, k0, nk, k0, nk);
             __syncthreads();
-            getrf_tile<T>(T0, nk, a.err);
+            getrf_tile<T>(T0, nk, a.err, T2);
             store_tile<T>(FS, T0, m, k0, nk, k0, nk);
             publish(tv + k * nb + k, TILE_FINAL);
             if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
@@ -379,8 +400,8 @@ __global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(M
             if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T1, r0, c0, pool);
             else load_tile<T>(T1, FS, m, r0, nr, c0, nc);
             __syncthreads();
-            if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk);
-            else trsm_u_tile<T>(T1, T0, nk);
+            if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk, T2);
+            else trsm_u_tile<T>(T1, T0, nk, T2);
             store_tile<T>(FS, T1, m, r0, nr, c0, nc);
             publish(tv + (long long)i * nb + j, TILE_FINAL);
         } else {  // TASK_GEMM
@@ -475,11 +496,13 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
                 // lane r - p0 holds row r of the unit-lower block; its L entries are loaded up front
                 const int r = p0 + lane;
                 T val = r < p1 ? u[r] : (T)0;
+                const int nbk = p1 - p0;
                 T lrow[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) lrow[q] = (r < p1 && p0 + q < r) ? F[r + (long long)(p0 + q) * m] : (T)0;
 #pragma unroll
-                for (int q = 0; q < 31; ++q) val -= lrow[q] * __shfl_sync(0xffffffffu, val, q);
+                for (int q = 0; q < 31; ++q)
+                    if (q < nbk - 1) val -= lrow[q] * __shfl_sync(0xffffffffu, val, q);
                 if (r < p1) u[r] = val;
             }
             __syncthreads();
@@ -558,15 +581,20 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
                 // lane r - p0 holds row r of the upper block (diagonal included), loaded up front
                 const int r = p0 + lane;
                 T val = r < p1 ? z[r] : (T)0;
+                const int nbk = p1 - p0;
                 T urow[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q)
-                    urow[q] = (r < p1 && p0 + q < p1 && p0 + q >= r) ? F[r + (long long)(p0 + q) * m] : (T)0;
+                    urow[q] = (r < p1 && p0 + q < p1 && p0 + q > r) ? F[r + (long long)(p0 + q) * m] : (T)0;
+                // every lane divides once, in parallel: x_r = (z_r - sum_{q > r} U(r,q) x_q) / U(r,r)
+                const T dinv = r < p1 ? (T)1 / F[r + (long long)r * m] : (T)0;
 #pragma unroll
                 for (int q = 31; q >= 0; --q) {
-                    if (lane == q && r < p1) val /= urow[q];
-                    const T xp = __shfl_sync(0xffffffffu, val, q);
-                    if (lane < q) val -= urow[q] * xp;
+                    if (q < nbk) {
+                        if (lane == q) val *= dinv;
+                        const T xp = __shfl_sync(0xffffffffu, val, q);
+                        if (lane < q) val -= urow[q] * xp;
+                    }
                 }
                 if (r < p1) z[r] = val;
             }
