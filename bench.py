@@ -39,6 +39,13 @@ sys.path.insert(0, str(ROOT))
 WORKLOAD = dict(workload="random_gate_network_80k_transistors_adaptive_bdf2", gates=23530, depth=60, n_inputs=32,
                 seed=1, c_wire=5e-15, period=0.5e-9, edge=50e-12, t_stop=20e-9, dt0=1e-12, method="gear2",
                 model="ekv")
+# 7-stage CMOS ring, fixed-step BDF2, dt = 1 ps, 20,000 steps, node n1 starts at VDD
+RING = dict(workload="ring7_fixed_bdf2_1ps", stages=7, vdd=1.2, c_load=10e-15, dt=1e-12, steps=20000)
+# batched Monte-Carlo corners: VTH shift ~ N(0, 30 mV), mobility ~ N(1, 0.05), T in {-40, 27, 125} C,
+# 2,000 fixed 1 ps steps, one batched circuit per run
+CORNERS = dict(ring=dict(workload="corners_1024x_ring7_fixed_bdf2_1ps", instances=1024),
+               gates=dict(workload="corners_256x_gates2000T_fixed_bdf2_1ps", instances=256, gates=588),
+               steps=2000, seed=7)
 L2_BYTES = 129 * 2 ** 20
 STATUS_BYTES = 48  # NRStatus read back per Newton iteration
 
@@ -73,6 +80,57 @@ def make_engine(gates: int, max_steps: int, precision: str = "fp64"):
     w = WORKLOAD
     eng.prepare(t_stop=w["t_stop"], dt=w["dt0"], max_steps=max_steps)
     return eng, stats, depth
+
+
+def make_corners_engine(kind: str, precision: str = "fp64", device: bool = True, instances: int = 0):
+    """`instances` Monte-Carlo copies of the ring or of a ~2,000-transistor gate network in one batched
+    circuit, fixed-step gear2 at 1 ps."""
+    from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions
+    from vajax_gb300.generators import random_gate_network, ring_oscillator
+    spec = CORNERS[kind]
+    n = instances or spec["instances"]
+    corners = create_monte_carlo_corners(n, seed=CORNERS["seed"])
+    if kind == "ring":
+        base = ring_oscillator(stages=RING["stages"], vdd=RING["vdd"], c_load=RING["c_load"])
+        opts = SimulationOptions(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0, icmode="uic",
+                                 ic={f"c{k}.{nd}": RING["vdd"] for k in range(n) for nd in ("n1", "vdd")})
+    else:
+        w = WORKLOAD
+        g = spec["gates"]
+        base = random_gate_network(n_gates=g, depth=max(4, g // 20), n_inputs=w["n_inputs"], seed=w["seed"],
+                                   c_wire=w["c_wire"], period=w["period"], edge=w["edge"])[0]
+        opts = SimulationOptions(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0)
+    eng = CircuitEngine(batch_circuit(base, corners), opts, precision=precision)
+    eng.parse()
+    t_stop = CORNERS["steps"] * RING["dt"]
+    if device:
+        eng.prepare(t_stop=t_stop, dt=RING["dt"], max_steps=CORNERS["steps"] + 1)
+    else:
+        eng.t_stop, eng.dt = t_stop, RING["dt"]
+        eng.config = eng._config(t_stop, RING["dt"], None)
+        eng.max_steps = CORNERS["steps"] + 1
+    return eng, n, len(base.instances)
+
+
+def make_ring_engine(precision: str = "fp64", device: bool = True):
+    """7-stage ring: fixed-step gear2 at dt = 1 ps from the initial condition n1 = VDD (uic)."""
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions
+    from vajax_gb300.generators import ring_oscillator
+    r = RING
+    c = ring_oscillator(stages=r["stages"], vdd=r["vdd"], c_load=r["c_load"])
+    opts = SimulationOptions(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0, icmode="uic",
+                             ic={"n1": r["vdd"], "vdd": r["vdd"]})
+    eng = CircuitEngine(c, opts, precision=precision)
+    eng.parse()
+    t_stop = r["steps"] * r["dt"]
+    if device:
+        eng.prepare(t_stop=t_stop, dt=r["dt"], max_steps=r["steps"] + 1)
+    else:
+        eng.t_stop, eng.dt = t_stop, r["dt"]
+        eng.config = eng._config(t_stop, r["dt"], None)
+        eng.max_steps = r["steps"] + 1
+    return eng
 
 
 # ---------------------------------------------------------------------------
@@ -192,7 +250,16 @@ def run_gb300(args):
         pg = dist
     K, W = args.steps, args.warmup
     prof_steps = 2
-    eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4, precision=args.precision)
+    ring = args.workload in ("ring", "corners_ring", "corners_gates")  # fixed-step workloads
+    n_inst = 1
+    if args.workload == "ring":
+        eng = make_ring_engine(args.precision)
+        nstats, depth = None, None
+    elif args.workload.startswith("corners_"):
+        eng, n_inst, per_copy = make_corners_engine(args.workload.split("_")[1], args.precision)
+        nstats, depth = per_copy, None
+    else:
+        eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4, precision=args.precision)
     dev = eng.device
     info = dev.solver_info()
     t0 = time.perf_counter()
@@ -255,7 +322,7 @@ def run_gb300(args):
     fac_bytes = info["nnz_lu"] * 20
     fac_ms = phase["factor_ms"]
     achieved = fac_bytes / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0
-    work = f"gates{args.gates}"
+    work = args.workload if ring else f"gates{args.gates}"
     roofline = {"kernel": "mf_factor_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": ncu_traffic("mf_factor_kernel", work),
@@ -267,6 +334,8 @@ def run_gb300(args):
     e2e = None
     if rank == 0 or world > 1:
         eng.max_steps = K + 1
+        if ring:
+            eng.t_stop = K * RING["dt"]
         r = eng.run_transient()
         acc = max(r.stats["n_steps"] - 1, 1)  # row 0 is the initial point
         n_x = len(X0)
@@ -278,18 +347,16 @@ def run_gb300(args):
 
     cpu = None
     if rank == 0 and world == 1:
-        cpu = cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg)
+        cpu = cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg,
+                                  steps={"ring": 300, "corners_ring": 3}.get(args.workload, 1))
 
     out = {"metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world, "steps": K,
            "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32lu",
            "data": "synthetic (seeded generator)",
-           "config": {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors,
-                      "precision": args.precision, "depth": depth, "n_unknowns": info["n_aug"], "nnz": info["nnz"], "nnz_lu": info["nnz_lu"],
-                      "front_flops": info["front_flops"], "seed": WORKLOAD["seed"],
-                      "parallelism": f"replicas{world}", "l2": "flushed (2x L2 write) before every timed step",
-                      "dc_seconds": dc_s, "dc_method": eng.dc_method},
+           "config": workload_config(args, ring, nstats, depth, info, world, dc_s, eng),
            "newton_iters_per_s": nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
+           "instances": n_inst, "solves_per_s": n_inst * nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "newton_iters": nr_iters, "rejected_steps": rejected, "host_wall_ms_per_step": wall_s * 1e3 / K,
            "phase_ms_per_newton_iter": phase, "gpu_launches": launches, "roofline": roofline,
            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
@@ -297,6 +364,23 @@ def run_gb300(args):
         print(json.dumps(out), flush=True)
     if pg:
         pg.destroy_process_group()
+
+
+def workload_config(args, ring, nstats, depth, info, world, dc_s, eng):
+    common = {"precision": args.precision, "n_unknowns": info["n_aug"], "nnz": info["nnz"], "nnz_lu": info["nnz_lu"],
+              "front_flops": info["front_flops"], "parallelism": f"replicas{world}",
+              "l2": "flushed (2x L2 write) before every timed step"}
+    if args.workload.startswith("corners_"):
+        kind = args.workload.split("_")[1]
+        spec = CORNERS[kind]
+        return {"workload": spec["workload"], "instances": spec["instances"], "devices_per_instance": nstats,
+                "corner_seed": CORNERS["seed"], "layout": "one block-diagonal batched circuit, one launch per kernel",
+                "dc_method": eng.dc_method, **common}
+    if ring:
+        return {"workload": RING["workload"], "stages": RING["stages"], "transistors": 2 * RING["stages"],
+                "dt": RING["dt"], "initial_condition": "n1 = VDD, others 0 (uic)", **common}
+    return {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors, "depth": depth,
+            "seed": WORKLOAD["seed"], "dc_seconds": dc_s, "dc_method": eng.dc_method, **common}
 
 
 def _oracle_system(eng, threads=1):
@@ -318,8 +402,9 @@ def cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg, steps=1):
     o = run_transient(S, c, X0, Q0, I0, maxc0)
     wall = time.perf_counter() - t0
     acc = max(o["n_steps"] - 1, 1)
-    return {"value": wall * 1e3 / acc, "unit": "ms/step", "cores": 1, "kind": "port",
-            "sample": f"first {acc} accepted adaptive step(s) from the DC point, full network, numpy + SuperLU"}
+    what = ("fixed steps from the initial condition, dense solve" if cfg.get("fixed_step") else
+            "accepted adaptive step(s) from the DC point, full network, numpy + SuperLU")
+    return {"value": wall * 1e3 / acc, "unit": "ms/step", "cores": 1, "kind": "port", "sample": f"first {acc} {what}"}
 
 
 def run_reference(args):
@@ -335,12 +420,23 @@ def run_reference(args):
     from oracle.dc import dc_operating_point
     from oracle.transient import run_transient
     K, W = args.steps, args.warmup
-    eng, nstats, depth = make_engine_host(args.gates)
+    ring = args.workload == "ring"
+    if ring:
+        eng = make_ring_engine(device=False)
+        nstats, depth = None, None
+    else:
+        eng, nstats, depth = make_engine_host(args.gates)
     S = _oracle_system(eng, threads=threads)
     rc = eng.rc
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
-    X0[: rc.n_nodes] = eng.initial_guess()
-    r = dc_operating_point(S, rc.source_values(0.0), X0)
+    if ring:
+        for node, v in eng.options.ic.items():
+            X0[rc.node_names[node]] = v
+        _, _, Q0, I0, _, _ = S.build_system(X0, rc.source_values(0.0))
+        r = {"X": X0, "Q": Q0, "I_vsource": I0, "max_res_contrib": np.zeros(rc.n_nodes - 1), "converged": True}
+    else:
+        X0[: rc.n_nodes] = eng.initial_guess()
+        r = dc_operating_point(S, rc.source_values(0.0), X0)
     if not r["converged"]:
         print(json.dumps({"impl": "reference", "unavailable": "oracle DC operating point did not converge"}))
         return
@@ -360,13 +456,14 @@ def run_reference(args):
     wall = time.perf_counter() - t0
     steps_done = max(o["n_steps"] - 1, 1)
     value = wall * 1e3 / steps_done
-    sample = (f"{steps_done} accepted adaptive steps from the DC point (cap {budget_s:.0f} s), full network, "
-              f"oracle numpy + SuperLU, {min(1, W)} warm-up step")
+    sample = (f"{steps_done} {'fixed steps from the initial condition' if ring else 'accepted adaptive steps from the DC point'} "
+              f"(cap {budget_s:.0f} s), oracle numpy, {min(1, W)} warm-up step")
     out = {"impl": "reference", "metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world,
            "steps": steps_done, "warmup": min(1, W), "ms_per_step": value, "higher_is_better": False,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-           "config": {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors,
-                      "depth": depth, "seed": WORKLOAD["seed"], "parallelism": "host"},
+           "config": ({"workload": RING["workload"], "stages": RING["stages"], "parallelism": "host"} if ring else
+                      {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors,
+                       "depth": depth, "seed": WORKLOAD["seed"], "parallelism": "host"}),
            "cpu_baseline": {"value": value, "unit": "ms/step", "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -378,6 +475,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates"], default="gates",
+                    help="gates: seeded random gate network, adaptive BDF2 (default, 80k transistors); "
+                         "ring: 7-stage ring, fixed-step BDF2 at 1 ps; corners_ring / corners_gates: 1,024 "
+                         "ring or 256 ~2,000-transistor network Monte-Carlo corners batched in one circuit")
     ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="fp64: FP64 LU; mixed: FP32 LU + FP64-residual refinement (3 sweeps)")

@@ -280,3 +280,39 @@ class CircuitEngine:
                      strategy="fixed_step_full_mna" if cfg["fixed_step"] else "adaptive_full_mna",
                      solver=f"gb300-sparse-{self.precision}", X0=X0)
         return TransientResult(times=out["times"], voltages=voltages, currents=currents, stats=stats)
+
+
+def _run_corners(self: CircuitEngine, corners, analysis: str = "transient", **prepare_kwargs):
+    """All corners as one batched circuit in one transient run
+    (replaces the serial loop of engine.py:2235-2320).  ``prepare_kwargs``
+    are those of ``prepare()`` (t_stop, dt, adaptive_config, max_steps)."""
+    import copy as _copy
+
+    from vajax_gb300.corners import CornerResult, CornerSweepResult, batch_circuit
+    if analysis != "transient":
+        raise ValueError(f"Unsupported analysis type: {analysis}")
+    if not corners:
+        return CornerSweepResult(corners=[], results=[])
+    batched = batch_circuit(self.circuit, corners)
+    opts = _copy.deepcopy(self.options)
+    opts.ic = {f"c{k}.{n}": v for k in range(len(corners)) for n, v in self.options.ic.items()}
+    eng = CircuitEngine(batched, opts, precision=self.precision)
+    eng.parse()
+    prepare_kwargs = dict(prepare_kwargs)
+    prepare_kwargs.pop("temperature", None)  # temperatures are per corner, per instance
+    eng.prepare(**prepare_kwargs)
+    res = eng.run_transient()
+    self.last_batch = eng
+    results = []
+    for k, cfg in enumerate(corners):
+        pre = f"c{k}."
+        volts = {n[len(pre):]: v for n, v in res.voltages.items() if n.startswith(pre)}
+        curs = {n[len(pre):]: v for n, v in res.currents.items() if n.startswith(pre)}
+        ok = bool(res.stats.get("dc_converged", True)) and res.stats.get("nr_failures", 0) == 0 and all(
+            np.all(np.isfinite(v)) for v in volts.values())
+        tr = TransientResult(times=res.times, voltages=volts, currents=curs, stats=dict(res.stats, batch=len(corners)))
+        results.append(CornerResult(corner=cfg, result=tr, converged=ok, stats=tr.stats))
+    return CornerSweepResult(corners=list(corners), results=results)
+
+
+CircuitEngine.run_corners = _run_corners
