@@ -469,25 +469,132 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+SERVING = dict(workload="serving_poisson200_dc_plus_1000_steps", rate=200.0, jobs=32, steps=1000, seed=11,
+               ring_stages=(3, 31), network_transistors=(200, 20000))
+
+
+def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
+    """Seeded job stream: Poisson arrivals, sizes log-uniform over rings of 3-31 stages and gate networks of
+    200..max_transistors transistors, a Monte-Carlo corner per job, DC + 1,000 transient steps each."""
+    from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
+    from vajax_gb300.generators import random_gate_network, ring_oscillator
+    from vajax_gb300.serving import Job
+    rng = np.random.default_rng(seed)
+    corners = create_monte_carlo_corners(n_jobs, seed=seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVING["rate"], n_jobs))
+    arrivals -= arrivals[0]
+    jobs, sizes = [], []
+    steps = SERVING["steps"]
+    for k in range(n_jobs):
+        corner = corners[k]
+        if rng.random() < 0.5:
+            lo, hi = SERVING["ring_stages"]
+            st = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+            st += 1 - st % 2  # odd stage count
+            make = (lambda st=st, corner=corner: batch_circuit(ring_oscillator(stages=st), [corner]))
+            opts = dict(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0)
+            jobs.append(Job(k, make, t_stop=steps * 1e-12, dt=1e-12, max_steps=steps + 1, options=opts))
+            sizes.append(("ring", 2 * st))
+        else:
+            lo, hi = SERVING["network_transistors"][0], max_transistors
+            nt = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+            gates = max(20, int(nt / 3.4))
+            depth = 60 if gates >= 1200 else max(4, gates // 20)
+            s2 = int(rng.integers(1 << 30))
+            make = (lambda gates=gates, depth=depth, s2=s2, corner=corner: batch_circuit(
+                random_gate_network(n_gates=gates, depth=depth, n_inputs=32, seed=s2)[0], [corner]))
+            opts = dict(tran_method="gear2")
+            jobs.append(Job(k, make, t_stop=20e-9, dt=1e-12, max_steps=steps + 1, options=opts))
+            sizes.append(("network", int(3.4 * gates)))
+    return jobs, arrivals.tolist(), sizes
+
+
+def run_serving(args):
+    """Served stream vs the plain FP64 path one job at a time, on the same seeded jobs."""
+    import torch
+    from vajax_gb300.serving import run_group, serve
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    n = args.jobs
+    jobs, arrivals, sizes = serving_jobs(n, SERVING["seed"], args.max_transistors)
+    # warm-up: one small job of each kind (library load, module load)
+    warm, _, _ = serving_jobs(2, SERVING["seed"] + 1, 400)
+    for j in warm:
+        run_group([j])
+    sampler = ClockSampler(gpu_index(local))
+    sampler.start()
+    torch.cuda.synchronize()
+    srv = serve(jobs, arrivals, slots=args.slots, precision=args.precision, max_batch=args.max_batch)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    st = srv.stats()
+    # the same jobs, one at a time, each started when the previous finished
+    seq_jobs, _, _ = serving_jobs(n, SERVING["seed"], args.max_transistors)
+    t0 = time.perf_counter()
+    iters = 0
+    seq_lat = []
+    for j in seq_jobs:
+        a = time.perf_counter()
+        run_group([j], precision="fp64")
+        iters += j.newton_iters
+        seq_lat.append(time.perf_counter() - a)
+    seq_wall = time.perf_counter() - t0
+    seq_solves = iters / seq_wall
+    # results of the served jobs against the same jobs alone
+    worst = 0.0
+    for a, b in zip(srv.results(), seq_jobs):
+        if a.result is None or b.result is None or len(a.result.times) != len(b.result.times):
+            continue
+        worst = max(worst, max(float(np.max(np.abs(a.result.voltages[k] - b.result.voltages[k])))
+                               for k in b.result.voltages))
+    out = {"metric": "served_newton_solves_per_s", "value": st.get("solves_per_s", 0.0), "unit": "solves/s",
+           "n_gpus": world, "steps": n, "warmup": len(warm), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32lu",
+           "data": "synthetic (seeded job stream)",
+           "config": {"workload": SERVING["workload"], "jobs": n, "arrival_rate_per_s": SERVING["rate"],
+                      "ring_stages": SERVING["ring_stages"], "network_transistors": [200, args.max_transistors],
+                      "slots": args.slots, "max_batch": args.max_batch, "precision": args.precision,
+                      "seed": SERVING["seed"], "l2": "inputs and fronts of concurrent jobs exceed L2"},
+           "p50_latency_s": st.get("p50_s"), "p99_latency_s": st.get("p99_s"), "jobs_per_s": st.get("jobs_per_s"),
+           "groups": st.get("groups"), "mean_group": st.get("mean_group"), "failed": st.get("failed"),
+           "sequential_fp64": {"solves_per_s": seq_solves, "wall_s": seq_wall,
+                               "p50_job_s": float(np.percentile(seq_lat, 50)),
+                               "p99_job_s": float(np.percentile(seq_lat, 99))},
+           "speedup_vs_sequential": st.get("solves_per_s", 0.0) / seq_solves if seq_solves else None,
+           "max_abs_dv_vs_alone_V": worst, "clocks": clocks,
+           "e2e": {"value": st.get("solves_per_s", 0.0), "unit": "solves/s", "h2d_bytes_per_step": None,
+                   "d2h_bytes_per_step": None}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates"], default="gates",
+    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates", "serving"],
+                    default="gates",
                     help="gates: seeded random gate network, adaptive BDF2 (default, 80k transistors); "
                          "ring: 7-stage ring, fixed-step BDF2 at 1 ps; corners_ring / corners_gates: 1,024 "
                          "ring or 256 ~2,000-transistor network Monte-Carlo corners batched in one circuit")
     ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="fp64: FP64 LU; mixed: FP32 LU + FP64-residual refinement (3 sweeps)")
+    ap.add_argument("--jobs", type=int, default=SERVING["jobs"], help="serving: jobs in the stream")
+    ap.add_argument("--slots", type=int, default=8, help="serving: concurrent groups")
+    ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")
+    ap.add_argument("--max-transistors", type=int, default=SERVING["network_transistors"][1],
+                    help="serving: largest gate network in the stream")
     ap.add_argument("--reference-budget", type=float, default=150.0, help="seconds of timed CPU work, reference arm")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_gb300(args)
 

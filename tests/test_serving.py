@@ -1,0 +1,53 @@
+"""Continuous-batching server: every job's result in the mix equals its result alone."""
+
+import numpy as np
+import pytest
+
+from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
+from vajax_gb300.generators import random_gate_network, ring_oscillator
+from vajax_gb300.serving import Job, job_key, run_group
+
+RING_OPTS = dict(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0, icmode="uic",
+                 ic={"c0.n1": 1.2, "c0.vdd": 1.2})
+
+
+def _ring_job(i, corner, stages=7):
+    return Job(i, lambda: batch_circuit(ring_oscillator(stages=stages), [corner]), t_stop=150e-12, dt=1e-12,
+               max_steps=151, options=dict(RING_OPTS))
+
+
+def _net_job(i, seed):
+    return Job(i, lambda: random_gate_network(n_gates=60, depth=6, n_inputs=8, seed=seed)[0], t_stop=0.4e-9,
+               dt=1e-12, max_steps=41, options=dict(tran_method="gear2", maxstep=0.4e-9 / 50))
+
+
+def test_job_keys_group_same_patterns():
+    cs = create_monte_carlo_corners(3, seed=2)
+    a, b, c = _ring_job(0, cs[0]), _ring_job(1, cs[1]), _ring_job(2, cs[2], stages=5)
+    keys = [job_key(j, j.make_circuit().resolve()) for j in (a, b, c)]
+    assert keys[0] == keys[1] != keys[2]
+
+
+@pytest.mark.gpu
+def test_served_results_match_alone(cuda):
+    from vajax_gb300.serving import serve
+    cs = create_monte_carlo_corners(5, seed=4)
+
+    def jobs():
+        return [_ring_job(0, cs[0]), _ring_job(1, cs[1]), _ring_job(2, cs[2]), _ring_job(3, cs[3], stages=5),
+                _net_job(4, 5), _net_job(5, 6), _ring_job(6, cs[4])]
+
+    mix = jobs()
+    srv = serve(mix, arrivals=[0.0, 0.0, 0.0, 0.01, 0.02, 0.02, 0.03], slots=3, max_batch=8)
+    st = srv.stats()
+    assert st["jobs"] == len(mix) and st["failed"] == 0
+    assert st["p99_s"] >= st["p50_s"] > 0
+    for served, alone in zip(srv.results(), jobs()):
+        run_group([alone])
+        ra, rb = alone.result, served.result
+        assert np.array_equal(ra.times, rb.times)
+        err = max(np.max(np.abs(ra.voltages[n] - rb.voltages[n])) for n in ra.voltages)
+        if served.group_size == 1:
+            assert err == 0.0, (served.job_id, err)
+        else:
+            assert err < 1e-6, (served.job_id, err)

@@ -158,6 +158,25 @@ def batch_circuit(base: Circuit, corners: List[CornerConfig], prefix: str = "c")
     return out
 
 
+def concat_circuits(circuits: List[Circuit], prefix: str = "j") -> Circuit:
+    """One circuit holding a disjoint copy of each circuit (names prefixed
+    ``{prefix}{k}.``, ground shared): the batch of several jobs."""
+    out = Circuit(f"batch{len(circuits)}", temperature=circuits[0].temperature if circuits else 300.15)
+    for k, c in enumerate(circuits):
+        def node(n, c=c, k=k):
+            return n if c._is_ground(n) else f"{prefix}{k}.{n}"
+        for inst in c.instances:
+            t = inst.temperature if inst.temperature is not None else c.temperature
+            out.add(f"{prefix}{k}.{inst.name}", inst.model, [node(n) for n in inst.nodes], temperature=t, **inst.params)
+        for s in c.vsources:
+            out.vsource(f"{prefix}{k}.{s.name}", node(s.p), node(s.n), s.kind, **copy.deepcopy(s.params))
+        for s in c.isources:
+            out.isource(f"{prefix}{k}.{s.name}", node(s.p), node(s.n), s.kind, **copy.deepcopy(s.params))
+        for n, v in c.nodeset.items():
+            out.nodeset[node(n)] = v
+    return out
+
+
 def create_monte_carlo_corners(n: int, seed: int = 0, vth_sigma: float = 0.03, mobility_sigma: float = 0.05,
                                temperatures_c=(-40.0, 27.0, 125.0)) -> List[CornerConfig]:
     """Seeded Monte-Carlo corners: VTH shift ~ N(0, vth_sigma), mobility scale
