@@ -533,10 +533,15 @@ def run_serving(args):
     t0 = time.perf_counter()
     iters = 0
     seq_lat = []
+    seq_failed = 0
     for j in seq_jobs:
         a = time.perf_counter()
-        run_group([j], precision="fp64")
-        iters += j.newton_iters
+        try:
+            run_group([j], precision="fp64")
+            iters += j.newton_iters
+        except RuntimeError as e:
+            j.error = str(e)
+            seq_failed += 1
         seq_lat.append(time.perf_counter() - a)
     seq_wall = time.perf_counter() - t0
     seq_solves = iters / seq_wall
@@ -557,7 +562,8 @@ def run_serving(args):
                       "seed": SERVING["seed"], "l2": "inputs and fronts of concurrent jobs exceed L2"},
            "p50_latency_s": st.get("p50_s"), "p99_latency_s": st.get("p99_s"), "jobs_per_s": st.get("jobs_per_s"),
            "groups": st.get("groups"), "mean_group": st.get("mean_group"), "failed": st.get("failed"),
-           "sequential_fp64": {"solves_per_s": seq_solves, "wall_s": seq_wall,
+           "failed_jobs": [(j.job_id, j.error) for j in srv.results() if j.error],
+           "sequential_fp64": {"solves_per_s": seq_solves, "wall_s": seq_wall, "failed": seq_failed,
                                "p50_job_s": float(np.percentile(seq_lat, 50)),
                                "p99_job_s": float(np.percentile(seq_lat, 99))},
            "speedup_vs_sequential": st.get("solves_per_s", 0.0) / seq_solves if seq_solves else None,

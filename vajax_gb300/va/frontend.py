@@ -1014,6 +1014,14 @@ class Differentiator:
                 self._diff_phi(inst, b)
             out += self._cur_out
             for inst in nonphi:
+                if inst.opcode == "fdiv" and any(self.d.get(o) for o in inst.operands):
+                    # a differentiated quotient becomes a * (1/b); its derivatives reuse 1/b
+                    rb = f.new_id()
+                    f.vtype[rb] = "f"
+                    out.append(Inst("fdiv", b, rb, [V_F_ONE, inst.operands[1]]))
+                    inst.quot = (inst.operands[0], inst.operands[1], rb)
+                    inst.opcode = "fmul"
+                    inst.operands = [inst.operands[0], rb]
                 out.append(inst)
                 self._cur_out = []
                 self._cur_block = b
@@ -1051,6 +1059,10 @@ class Differentiator:
     def _diff(self, inst: Inst):
         op = inst.opcode
         ops = inst.operands
+        quot = getattr(inst, "quot", None)
+        if quot is not None:  # q = a * (1/b) from a quotient
+            op = "fdiv"
+            ops = [quot[0], quot[1]]
         dl = [self.d.get(o, {}) for o in ops]
         if not any(dl):
             return
@@ -1080,30 +1092,32 @@ class Differentiator:
                     terms.append(e("fmul", [ops[0], dl[1][p]]))
                 out[p] = terms[0] if len(terms) == 1 else e("fadd", terms)
         elif op == "fdiv":
-            # d(a/b) = (da - (a/b) db) / b
+            # d(a/b) = (da - (a/b) db) * (1/b): one reciprocal shared by every derivative
+            rb = quot[2] if quot is not None else e("fdiv", [V_F_ONE, ops[1]])
             for p in keys:
                 if p in dl[1]:
                     t = e("fmul", [r, dl[1][p]])
                     num = e("fsub", [dl[0][p], t]) if p in dl[0] else e("fneg", [t])
                 else:
                     num = dl[0][p]
-                out[p] = e("fdiv", [num, ops[1]])
+                out[p] = e("fmul", [num, rb])
         elif op == "exp":
             for p in keys:
                 out[p] = e("fmul", [r, dl[0][p]])
         elif op == "ln":
+            rx = e("fdiv", [V_F_ONE, ops[0]])
             for p in keys:
-                out[p] = e("fdiv", [dl[0][p], ops[0]])
+                out[p] = e("fmul", [dl[0][p], rx])
         elif op == "log":
             ln10 = self._c(math.log(10.0))
+            rden = e("fdiv", [V_F_ONE, e("fmul", [ops[0], ln10])])
             for p in keys:
-                den = e("fmul", [ops[0], ln10])
-                out[p] = e("fdiv", [dl[0][p], den])
+                out[p] = e("fmul", [dl[0][p], rden])
         elif op == "sqrt":
             two = self._c(2.0)
+            rden = e("fdiv", [V_F_ONE, e("fmul", [r, two])])
             for p in keys:
-                den = e("fmul", [r, two])
-                out[p] = e("fdiv", [dl[0][p], den])
+                out[p] = e("fmul", [dl[0][p], rden])
         elif op == "fabs":
             zero = V_F_ZERO
             for p in keys:
@@ -1121,10 +1135,11 @@ class Differentiator:
                 out[p] = e("select", [ops[0], dl[1].get(p, V_F_ZERO), dl[2].get(p, V_F_ZERO)])
         elif op == "pow":
             # d(x^y) = x^y * (dy ln x + y dx / x)
+            rx = e("fdiv", [V_F_ONE, ops[0]]) if any(p in dl[0] for p in keys) else None
             for p in keys:
                 terms = []
                 if p in dl[0]:
-                    q = e("fdiv", [dl[0][p], ops[0]])
+                    q = e("fmul", [dl[0][p], rx])
                     terms.append(e("fmul", [ops[1], q]))
                 if p in dl[1]:
                     lx = e("ln", [ops[0]])
