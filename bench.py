@@ -74,9 +74,10 @@ def make_engine_host(gates: int):
     return eng, stats, depth
 
 
-def make_engine(gates: int, max_steps: int, precision: str = "fp64"):
+def make_engine(gates: int, max_steps: int, precision: str = "fp64", refine: int = 3):
     eng, stats, depth = make_engine_host(gates)
     eng.precision = precision
+    eng.refine_sweeps = refine
     w = WORKLOAD
     eng.prepare(t_stop=w["t_stop"], dt=w["dt0"], max_steps=max_steps)
     return eng, stats, depth
@@ -259,7 +260,8 @@ def run_gb300(args):
         eng, n_inst, per_copy = make_corners_engine(args.workload.split("_")[1], args.precision)
         nstats, depth = per_copy, None
     else:
-        eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4, precision=args.precision)
+        eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4, precision=args.precision,
+                                         refine=args.refine)
     dev = eng.device
     info = dev.solver_info()
     t0 = time.perf_counter()
@@ -313,6 +315,21 @@ def run_gb300(args):
     dev.profile(0)
     its = max(prof["iterations"], 1)
     phase = {k: prof[k] / its for k in ("eval_ms", "assemble_ms", "factor_ms", "solve_ms", "update_ms")}
+    mixed_vs_fp64 = None
+    if args.precision == "mixed":
+        # the same steps with the FP64 LU from the same initial state: node-voltage error of the mixed run
+        out_m = sess.read()
+        dev.set_precision(0)
+        s64 = dev.session(cfg, X0, Q0, I0, maxc0)
+        s64.advance(out_m["n_steps"] - 1)
+        out_d = s64.read()
+        s64.close()
+        dev.set_precision(1, args.refine)
+        n = min(out_m["n_steps"], out_d["n_steps"])
+        same_t = bool(np.allclose(out_m["times"][:n], out_d["times"][:n], rtol=1e-12, atol=0))
+        dv = float(np.max(np.abs(out_m["V"][:n] - out_d["V"][:n])))
+        mixed_vs_fp64 = {"max_abs_dv_V": dv, "steps_compared": n, "times_identical": same_t,
+                         "newton_iters_mixed": out_m["total_nr_iters"], "newton_iters_fp64": out_d["total_nr_iters"]}
     sess.close()
 
     # roofline of the dominant kernel: the multifrontal refactorisation
@@ -359,6 +376,7 @@ def run_gb300(args):
            "instances": n_inst, "solves_per_s": n_inst * nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "newton_iters": nr_iters, "rejected_steps": rejected, "host_wall_ms_per_step": wall_s * 1e3 / K,
            "phase_ms_per_newton_iter": phase, "gpu_launches": launches, "roofline": roofline,
+           "mixed_vs_fp64": mixed_vs_fp64,
            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -367,7 +385,8 @@ def run_gb300(args):
 
 
 def workload_config(args, ring, nstats, depth, info, world, dc_s, eng):
-    common = {"precision": args.precision, "n_unknowns": info["n_aug"], "nnz": info["nnz"], "nnz_lu": info["nnz_lu"],
+    common = {"precision": args.precision, "refine_sweeps": args.refine if args.precision == "mixed" else 0,
+              "n_unknowns": info["n_aug"], "nnz": info["nnz"], "nnz_lu": info["nnz_lu"],
               "front_flops": info["front_flops"], "parallelism": f"replicas{world}",
               "l2": "flushed (2x L2 write) before every timed step"}
     if args.workload.startswith("corners_"):
@@ -415,9 +434,9 @@ def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    from oracle.dc import dc_operating_point
+    # one thread: splitting the interpreter's numpy work over threads was measured 10x
+    # slower (per-op GIL hand-offs), and SuperLU is single-threaded
+    threads = 1
     from oracle.transient import run_transient
     K, W = args.steps, args.warmup
     ring = args.workload == "ring"
@@ -429,14 +448,25 @@ def run_reference(args):
     S = _oracle_system(eng, threads=threads)
     rc = eng.rc
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
+    start = "the initial condition"
     if ring:
         for node, v in eng.options.ic.items():
             X0[rc.node_names[node]] = v
-        _, _, Q0, I0, _, _ = S.build_system(X0, rc.source_values(0.0))
-        r = {"X": X0, "Q": Q0, "I_vsource": I0, "max_res_contrib": np.zeros(rc.n_nodes - 1), "converged": True}
+        _, _, Q0, I0, maxc, _ = S.build_system(X0, rc.source_values(0.0))
+        r = {"X": X0, "Q": Q0, "I_vsource": I0, "max_res_contrib": maxc, "converged": True}
     else:
-        X0[: rc.n_nodes] = eng.initial_guess()
-        r = dc_operating_point(S, rc.source_values(0.0), X0)
+        from oracle.make_dc_state import dc_state_path
+        p = dc_state_path(args.gates, WORKLOAD["seed"])
+        if p.exists():
+            # the oracle's own DC operating point, solved once offline (minutes on the CPU)
+            z = np.load(p)
+            r = {"X": z["X"], "Q": z["Q"], "I_vsource": z["I"], "max_res_contrib": z["maxc"], "converged": True}
+            start = "the oracle's DC point"
+        else:
+            from oracle.dc import dc_operating_point
+            X0[: rc.n_nodes] = eng.initial_guess()
+            r = dc_operating_point(S, rc.source_values(0.0), X0)
+            start = "the DC point"
     if not r["converged"]:
         print(json.dumps({"impl": "reference", "unavailable": "oracle DC operating point did not converge"}))
         return
@@ -456,7 +486,7 @@ def run_reference(args):
     wall = time.perf_counter() - t0
     steps_done = max(o["n_steps"] - 1, 1)
     value = wall * 1e3 / steps_done
-    sample = (f"{steps_done} {'fixed steps from the initial condition' if ring else 'accepted adaptive steps from the DC point'} "
+    sample = (f"{steps_done} {'fixed' if ring else 'accepted adaptive'} steps from {start} "
               f"(cap {budget_s:.0f} s), oracle numpy, {min(1, W)} warm-up step")
     out = {"impl": "reference", "metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world,
            "steps": steps_done, "warmup": min(1, W), "ms_per_step": value, "higher_is_better": False,
@@ -475,7 +505,9 @@ SERVING = dict(workload="serving_poisson200_dc_plus_1000_steps", rate=200.0, job
 
 def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
     """Seeded job stream: Poisson arrivals, sizes log-uniform over rings of 3-31 stages and gate networks of
-    200..max_transistors transistors, a Monte-Carlo corner per job, DC + 1,000 transient steps each."""
+    200..max_transistors transistors, a Monte-Carlo corner per job, DC + 1,000 fixed 1 ps gear2 steps each
+    (fixed steps keep every job's work bounded; the adaptive controller of the reference can stall on some
+    corner-shifted networks, in the oracle as on the GPU)."""
     from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
     from vajax_gb300.generators import random_gate_network, ring_oscillator
     from vajax_gb300.serving import Job
@@ -503,8 +535,8 @@ def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
             s2 = int(rng.integers(1 << 30))
             make = (lambda gates=gates, depth=depth, s2=s2, corner=corner: batch_circuit(
                 random_gate_network(n_gates=gates, depth=depth, n_inputs=32, seed=s2)[0], [corner]))
-            opts = dict(tran_method="gear2")
-            jobs.append(Job(k, make, t_stop=20e-9, dt=1e-12, max_steps=steps + 1, options=opts))
+            opts = dict(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0)
+            jobs.append(Job(k, make, t_stop=steps * 1e-12, dt=1e-12, max_steps=steps + 1, options=opts))
             sizes.append(("network", int(3.4 * gates)))
     return jobs, arrivals.tolist(), sizes
 
@@ -587,7 +619,8 @@ def main():
                          "ring or 256 ~2,000-transistor network Monte-Carlo corners batched in one circuit")
     ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
-                    help="fp64: FP64 LU; mixed: FP32 LU + FP64-residual refinement (3 sweeps)")
+                    help="fp64: FP64 LU; mixed: FP32 LU + FP64-residual refinement (--refine sweeps)")
+    ap.add_argument("--refine", type=int, default=3, help="mixed: refinement sweeps (0-3)")
     ap.add_argument("--jobs", type=int, default=SERVING["jobs"], help="serving: jobs in the stream")
     ap.add_argument("--slots", type=int, default=8, help="serving: concurrent groups")
     ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")

@@ -102,7 +102,11 @@ int vgb_profile(void* h, int mode, double* out);
 
 /* Build the CSR pattern, stamp maps, gather lists and the sparse symbolic
  * factorisation; allocate device state.  precision: 0 = FP64 LU,
- * 1 = FP32 LU with FP64-residual iterative refinement (refine_sweeps <= 3).
+ * 1 = FP32 LU with FP64-residual iterative refinement (refine_sweeps <= 3),
+ * 2 = dense FP64 LU with partial pivoting in one CTA, for circuits with
+ * n_aug <= VGB_DENSE_STATIC_MAX (the reference's dense path for small
+ * circuits, solver_factories.py:784-788; robust where static pivoting is not,
+ * e.g. the high-gain DC point of a ring oscillator).
  * Replaces FullMNAStrategy._ensure_full_mna_solver
  * (vajax/analysis/transient/full_mna.py:344-690). */
 int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps);
@@ -113,6 +117,14 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
  * and the f32-with-refinement solvers (full_mna.py:584-684); a caller can run
  * the DC operating point in FP64 and the transient in FP32. */
 int vgb_set_precision(void* h, int precision, int refine_sweeps);
+
+/* Reference voltages of the gshunt term: with ref (device, n_nodes-1 values,
+ * node 1 first) set, gshunt pulls each node towards ref instead of ground,
+ * f_node += gshunt * (V - ref).  NULL restores the reference's shunt to
+ * ground (mna.py:673-719).  The pointer is kept, not copied, until the next
+ * call.  Extension used by the DC operating-point continuation from a
+ * nodeset. */
+int vgb_set_shunt_ref(void* h, const double* ref);
 
 /* Pattern and maps (bit-exact contract with the reference) ----------------- */
 

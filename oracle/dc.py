@@ -76,6 +76,9 @@ def source_stepping(S, vs, X0, itl=20, step=0.1, step_min=0.001, scale=2.0, max_
     return X_good, False
 
 
+NODESET_CONTINUATION = (1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12)
+
+
 def dc_operating_point(S, vs, X0, itl=20, node_limit=0.3, node_limit_itl=100):
     """Plain Newton, then Newton with a per-node step clip (the product's
     extension, skipped when node_limit is 0), then gshunt stepping, then source
@@ -86,7 +89,24 @@ def dc_operating_point(S, vs, X0, itl=20, node_limit=0.3, node_limit_itl=100):
     if node_limit > 0:
         r = nr_solve(S, np.array(X0, np.float64), vs, max_iterations=node_limit_itl, node_limit=node_limit)
         if r["converged"] and np.all(np.isfinite(r["X"])):
-            return nr_solve(S, r["X"], vs, max_iterations=itl)
+            r = nr_solve(S, r["X"], vs, max_iterations=itl)
+            if r["converged"] and np.all(np.isfinite(r["X"])):
+                return r
+        # continuation from the initial guess: gshunt towards it, stepped down to 0
+        ref = np.array(X0, np.float64)[1:S.n_nodes]
+        X, ok = np.array(X0, np.float64), True
+        for g in NODESET_CONTINUATION:
+            rg = nr_solve(S, X, vs, max_iterations=node_limit_itl, node_limit=node_limit, gshunt=g, shunt_ref=ref)
+            if not (rg["converged"] and np.all(np.isfinite(rg["X"]))):
+                ok = False
+                break
+            X = rg["X"]
+        if ok:
+            r = nr_solve(S, X, vs, max_iterations=node_limit_itl, node_limit=node_limit)
+            if r["converged"]:
+                r = nr_solve(S, r["X"], vs, max_iterations=itl)
+                if r["converged"] and np.all(np.isfinite(r["X"])):
+                    return r
     X, ok = gshunt_stepping(S, vs, X0, itl=itl)
     if not ok:
         X, ok = source_stepping(S, vs, X0, itl=itl)

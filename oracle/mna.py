@@ -168,7 +168,8 @@ class OracleSystem:
 
     # ---- build_system (mna_builder.py:759-1076) ----------------------------
     def build_system(self, X, vsrc_vals, isrc_vals=None, Q_prev=None, c0=0.0, gshunt=0.0, c1=0.0, d1=0.0,
-                     dQdt_prev=None, c2=0.0, Q_prev2=None):
+                     dQdt_prev=None, c2=0.0, Q_prev2=None, shunt_ref=None):
+        """shunt_ref (extension): gshunt pulls node voltages towards it instead of ground."""
         n_unk = self.n_unk
         z = np.zeros(n_unk)
         Q_prev = z if Q_prev is None else Q_prev
@@ -225,6 +226,8 @@ class OracleSystem:
             fr = fr + kcl
         eff = self.gmin + gshunt
         f_node = fr + c0 * Q + c1 * Q_prev + d1 * dQdt_prev + c2 * Q_prev2 + eff * V[1:]
+        if shunt_ref is not None:
+            f_node = f_node - gshunt * np.asarray(shunt_ref)
         f_branch = V[self.vp] - V[self.vn] - np.asarray(vsrc_vals) if self.n_vsrc else np.zeros(0)
         return csr, np.concatenate([f_node, f_branch]), Q, I_vs, maxc, f_resist
 
@@ -244,14 +247,25 @@ class OracleSystem:
         import scipy.sparse.linalg as spl
         A = sp.csr_matrix((csr, self.indices, self.indptr), shape=(self.n_aug, self.n_aug)).tocsc()
         # minimum degree on A^T + A: circuit matrices are nearly structurally
-        # symmetric, and COLAMD fills far more on the large gate networks
-        return spl.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.01).solve(rhs)
+        # symmetric, and COLAMD fills far more on the large gate networks.
+        # SuperLU's threshold pivoting can stop on the 1e-12 (gmin) pivots of
+        # floating stack nodes; then retry with full partial pivoting, and last
+        # with the reference dense path's 1e-14 diagonal (solver_factories.py:784-788)
+        try:
+            return spl.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.01).solve(rhs)
+        except RuntimeError:
+            pass
+        try:
+            return spl.splu(A, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=1.0).solve(rhs)
+        except RuntimeError:
+            A2 = (A + 1e-14 * sp.identity(self.n_aug, format="csc")).tocsc()
+            return spl.splu(A2, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=1.0).solve(rhs)
 
 
 def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None, c0=0.0, gshunt=0.0, c1=0.0,
              d1=0.0, dQdt_prev=None, c2=0.0, Q_prev2=None, res_tol_floor=None, max_iterations=20, reltol=1e-3,
              abstol=1e-12, vntol=1e-6, nr_damping=1.0, max_step=1e30, conv_mask: Optional[np.ndarray] = None,
-             node_limit: float = 0.0):
+             node_limit: float = 0.0, shunt_ref=None):
     """solver_factories.py:140-325 + while-loop nr_solve (:526-725)."""
     n_unk, n_v = sys_.n_unk, sys_.n_vsrc
     X = np.array(X_init, dtype=np.float64)
@@ -262,11 +276,14 @@ def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None,
     max_f = np.inf
     while (not converged) and it < max_iterations:
         csr, f, Q, _, maxc, _ = sys_.build_system(X, vsrc_vals, isrc_vals, Q_prev, c0, gshunt, c1, d1, dQdt_prev, c2,
-                                                  Q_prev2)
+                                                  Q_prev2, shunt_ref)
         res_tol = np.concatenate([np.maximum(maxc * reltol, floor_), np.full(n_v, vntol)])
         f_check = f if conv_mask is None else np.where(conv_mask, f, 0.0)
         max_f = float(np.max(np.abs(f_check))) if len(f_check) else 0.0
         residual_converged = bool(np.all(np.abs(f_check) < res_tol))
+        if not (np.all(np.isfinite(csr)) and np.all(np.isfinite(f))):
+            it += 1  # the iterate left the finite range: stop, not converged
+            break
         delta = sys_.solve(csr, -f)
         conv_delta = np.concatenate([delta[:n_unk] * nr_damping, delta[n_unk:]])
         X_ref = X[1:]
@@ -283,7 +300,7 @@ def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None,
         converged = residual_converged and delta_converged
         it += 1
     _, _, Q, I_vs, maxc, _ = sys_.build_system(X, vsrc_vals, isrc_vals, Q_prev, c0, gshunt, c1, d1, dQdt_prev, c2,
-                                               Q_prev2)
+                                               Q_prev2, shunt_ref)
     z = np.zeros(n_unk)
     dQdt = c0 * Q + c1 * (z if Q_prev is None else Q_prev) + d1 * (z if dQdt_prev is None else dQdt_prev) + \
         c2 * (z if Q_prev2 is None else Q_prev2)

@@ -37,6 +37,7 @@ SIGNATURES = {
     "vgb_solver_info": (C.c_int, [vp, i64p]),
     "vgb_circuit_finalize": (C.c_int, [vp, C.c_double, C.c_int, C.c_int]),
     "vgb_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
+    "vgb_set_shunt_ref": (C.c_int, [vp, vp]),
     "vgb_pattern_info": (C.c_int, [vp, i32p, i32p, i64p, i64p]),
     "vgb_pattern_csr": (C.c_int, [vp, i32p, i32p]),
     "vgb_stamp_positions": (C.c_int, [vp, C.c_int, i32p]),

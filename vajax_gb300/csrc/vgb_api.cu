@@ -46,6 +46,11 @@ static void require_final(Circuit* c) {
 // front pools of the requested precision (allocated once, kept)
 static void ensure_pools(Circuit& c, int precision) {
     SparseLU& L = c.lu;
+    if (precision == 2) {
+        VGB_REQUIRE(c.n_aug <= VGB_DENSE_STATIC_MAX, "the dense solver is limited to n_aug <= VGB_DENSE_STATIC_MAX");
+        if (!c.d_dense.p) c.d_dense.alloc(std::max<size_t>((size_t)c.n_aug * c.n_aug, 1));
+        return;
+    }
     const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
     const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
     if (precision == 1 && !L.d_pool32.p) {
@@ -100,9 +105,15 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
         launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
         if (prof) VGB_CUDA(cudaEventRecord(c.ev[2], s));
         const bool fp32 = c.solver_kind == 1;
-        lu_factor(c, c.d_csr_vals.p, fp32, s);
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
-        lu_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, fp32, c.refine_sweeps, s);
+        if (c.solver_kind == 2) {
+            if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
+            launch_dense_solve(c.n_aug, c.d_indptr.p, c.d_indices.p, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p,
+                               c.d_dense.p, &c.d_status.p->dev_err, s);
+        } else {
+            lu_factor(c, c.d_csr_vals.p, fp32, s);
+            if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
+            lu_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, fp32, c.refine_sweeps, s);
+        }
         if (prof) VGB_CUDA(cudaEventRecord(c.ev[4], s));
         launch_nr_reduce(u, s);
         launch_nr_apply(u, s);
@@ -123,6 +134,10 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
         r.max_f = bits_to_double(st.max_f);
         r.dev_err |= st.dev_err;
         if (st.dev_err & DEV_ERR_TIMEOUT) throw Error(VGB_ERR_TIMEOUT, "sparse LU dependency wait timed out");
+        if (st.nonfinite) {  // the residual left the finite range: stop, not converged
+            r.nonfinite = true;
+            break;
+        }
         const bool conv = st.res_ok && (it == 0 || st.delta_ok);
         if (conv) {
             r.converged = true;
@@ -346,12 +361,22 @@ int vgb_profile(void* h, int mode, double* out) {
     });
 }
 
+int vgb_set_shunt_ref(void* h, const double* ref) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        c->shunt_ref = ref;
+    });
+}
+
 int vgb_set_precision(void* h, int precision, int refine_sweeps) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
         require_final(c);
-        VGB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (FP64) or 1 (FP32+refinement)");
+        VGB_REQUIRE(precision >= 0 && precision <= 2,
+                    "precision must be 0 (FP64), 1 (FP32+refinement) or 2 (dense FP64, small circuits)");
         VGB_REQUIRE(refine_sweeps >= 0 && refine_sweeps <= 3, "refine_sweeps must be in [0, 3]");
         ensure_pools(*c, precision);
         c->solver_kind = precision;
@@ -364,7 +389,8 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
     return guarded(c, [&] {
         c = as_circuit(h);
         VGB_REQUIRE(!c->finalized, "circuit already finalized");
-        VGB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (FP64) or 1 (FP32+refinement)");
+        VGB_REQUIRE(precision >= 0 && precision <= 2,
+                    "precision must be 0 (FP64), 1 (FP32+refinement) or 2 (dense FP64, small circuits)");
         VGB_REQUIRE(refine_sweeps >= 0 && refine_sweeps <= 3, "refine_sweeps must be in [0, 3]");
         c->gmin = gmin;
         c->solver_kind = precision;

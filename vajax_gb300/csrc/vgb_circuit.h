@@ -175,7 +175,9 @@ struct Circuit {
     Sources vsrc_wave, isrc_wave;
     double gmin = 1e-12;
     bool finalized = false;
-    int solver_kind = 0;  // 0 = sparse FP64, 1 = sparse FP32 + FP64 refinement
+    int solver_kind = 0;  // 0 = sparse FP64, 1 = sparse FP32 + FP64 refinement, 2 = dense FP64 (small circuits)
+    DevBuf<double> d_dense;  // n_aug^2 working matrix of the dense solver
+    const double* shunt_ref = nullptr;  // device [n_unk]: voltages gshunt pulls towards (NULL: ground)
     int refine_sweeps = 3;
     std::string last_error;
 

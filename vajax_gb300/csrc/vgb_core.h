@@ -19,6 +19,7 @@ inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
 
 // Kernel launches of one linear solve (factor + triangular solves + refinement).
 inline long long solve_launches(const Circuit& c) {
+    if (c.solver_kind == 2) return 1;
     const SparseLU& L = c.lu;
     long long once = (L.nM + (long long)L.f_col.size() ? 1 : 0) + (L.nsn ? 2 : 0) + (L.l_col.empty() ? 0 : 1);
     long long n = (L.nsn ? 1 : 0) + once;
@@ -75,6 +76,8 @@ inline void assemble(Circuit& c, const double* X, const double* vs, const double
     a.d1 = k.d1;
     a.c2 = k.c2;
     a.gdiag = c.gmin + k.gshunt;
+    a.gshunt = k.gshunt;
+    a.shunt_ref = c.shunt_ref;
     a.res_tol_floor = res_tol_floor;
     a.reltol = reltol;
     a.vntol = vntol;
@@ -99,6 +102,10 @@ inline void assemble(Circuit& c, const double* X, const double* vs, const double
 }
 
 inline void linear_solve(Circuit& c, const double* csr, const double* rhs, double* x, cudaStream_t s) {
+    if (c.solver_kind == 2) {
+        launch_dense_solve(c.n_aug, c.d_indptr.p, c.d_indices.p, csr, rhs, x, c.d_dense.p, &c.d_status.p->dev_err, s);
+        return;
+    }
     const bool fp32 = c.solver_kind == 1;
     lu_factor(c, csr, fp32, s);
     lu_solve(c, csr, rhs, x, fp32, c.refine_sweeps, s);

@@ -122,6 +122,13 @@ __global__ void __launch_bounds__(DENSE_THREADS) dense_static_solve_kernel(int n
 
 }  // namespace
 
+// The same dense LU with partial pivoting on a caller-owned matrix buffer
+// (the per-circuit dense solver of small circuits).
+void launch_dense_solve(int n, const int* indptr, const int* indices, const double* vals, const double* rhs,
+                        double* x, double* M, int* err, cudaStream_t s) {
+    if (n > 0) dense_static_solve_kernel<<<1, DENSE_THREADS, 0, s>>>(n, indptr, indices, vals, rhs, x, M, err);
+}
+
 }  // namespace vgb
 
 using namespace vgb;

@@ -61,6 +61,7 @@ __device__ __forceinline__ void finish_row(const AssembleArgs& a, int r, double 
         }
         fn = fr + a.c0 * q + a.c1 * a.Q_prev[r] + a.d1 * a.dQdt_prev[r] + a.c2 * a.Q_prev2[r] +
              a.gdiag * a.X[r + 1];
+        if (a.shunt_ref) fn -= a.gshunt * a.shunt_ref[r];
         a.Q[r] = q;
         a.maxc[r] = mc;
         tol = fmax(mc * a.reltol, a.res_tol_floor[r]);

@@ -16,6 +16,7 @@ struct AssembleArgs {
     const double* vsrc_vals; const double* isrc_vals;
     const double* Q_prev; const double* dQdt_prev; const double* Q_prev2;
     double c0, c1, d1, c2, gdiag;
+    double gshunt; const double* shunt_ref;  // gshunt pulls node r towards shunt_ref[r] (NULL: ground)
     const double* res_tol_floor; double reltol, vntol;
     const unsigned char* conv_mask;
     double* csr_vals; double* f; double* Q; double* maxc; double* fres;
@@ -38,6 +39,8 @@ struct NRUpdateArgs {
     NRStatus* st;
 };
 void launch_nr_reduce(const NRUpdateArgs& a, cudaStream_t s);
+void launch_dense_solve(int n, const int* indptr, const int* indices, const double* vals, const double* rhs,
+                        double* x, double* M, int* err, cudaStream_t s);
 void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s);
 void launch_status_reset(NRStatus* st, cudaStream_t s);
 

@@ -19,6 +19,12 @@ import numpy as np
 
 from vajax_gb300.circuit import Circuit, ResolvedCircuit
 
+# circuits up to this many unknowns use the dense solver (VGB_DENSE_STATIC_MAX)
+DENSE_MAX = 128
+
+# gshunt steps (siemens) of the DC continuation from the initial guess
+NODESET_CONTINUATION = (1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12)
+
 METHODS = {"be": 0, "euler": 0, "backward_euler": 0, "trap": 1, "trapezoidal": 1, "am2": 1,
            "gear2": 2, "gear": 2, "bdf2": 2, "bdf": 2}
 
@@ -142,7 +148,10 @@ class CircuitEngine:
         self.max_steps = max_steps if max_steps is not None else int(t_stop / dt * 1.1) + 10
         if self.device is None:
             prec = {"fp64": 0, "fp32": 1, "mixed": 1}[self.precision]
-            self.device = DeviceCircuit(self.rc, precision=prec, refine_sweeps=3, gmin=self.options.gmin)
+            if self.rc.n_nodes - 1 + len(self.rc.vsources) <= DENSE_MAX:
+                prec = 2  # small circuits: dense LU with partial pivoting, as the reference's dense path
+            self.device = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 3),
+                                        gmin=self.options.gmin)
         self._prepared = True
         return self
 
@@ -189,13 +198,14 @@ class CircuitEngine:
         engine solves it with the FP64 LU and switches back to FP32 after."""
         dev = self.device
         prec = getattr(dev, "precision", 0)
-        if prec == 0:
+        if prec != 1:
             return self._initial_state()
+        sweeps = getattr(self, "refine_sweeps", 3)
         dev.set_precision(0)
         try:
             return self._initial_state()
         finally:
-            dev.set_precision(prec)
+            dev.set_precision(prec, sweeps)
 
     def _initial_state(self):
         import torch
@@ -233,6 +243,26 @@ class CircuitEngine:
             self.dc_method = "newton_limited"
             if ok:
                 Xn, _, ok, r = solve(Xn)
+        if not ok and o.dc_node_limit > 0:
+            # ... then a continuation from the initial guess: gshunt pulls every node
+            # towards its guess and is stepped down to 0 (extension) ...
+            ref = torch.as_tensor(np.array(X0[1: rc.n_nodes], np.float64), device="cuda")
+            dev.set_shunt_ref(ref)
+            X, cont_ok = X0, True
+            try:
+                for g in NODESET_CONTINUATION:
+                    Xg, _, okg, _ = solve(X, gshunt=g, node_limit=o.dc_node_limit, itl=o.dc_node_limit_itl)
+                    if not okg:
+                        cont_ok = False
+                        break
+                    X = Xg
+            finally:
+                dev.set_shunt_ref(None)
+            if cont_ok:
+                Xn, _, ok, r = solve(X, node_limit=o.dc_node_limit, itl=o.dc_node_limit_itl)
+                if ok:
+                    Xn, _, ok, r = solve(Xn)
+            self.dc_method = "nodeset_continuation"
         if not ok and self.homotopy:
             # ... then the homotopy chain when it does not converge (homotopy.py:470-567)
             from vajax_gb300.dc import homotopy_chain

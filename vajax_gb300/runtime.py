@@ -88,6 +88,11 @@ class DeviceCircuit:
     def _check(self, code):
         _lib.check(code, self.h)
 
+    def set_shunt_ref(self, ref=None):
+        """ref: torch CUDA float64 tensor [n_nodes-1] the gshunt term pulls towards, or None (ground)."""
+        self._shunt_ref = ref
+        self._check(self.lib.vgb_set_shunt_ref(self.h, _ptr(ref)))
+
     def set_precision(self, precision: int, refine_sweeps: int = 3):
         """0: FP64 LU; 1: FP32 LU + FP64-residual refinement."""
         self._check(self.lib.vgb_set_precision(self.h, int(precision), int(refine_sweeps)))
