@@ -240,6 +240,18 @@ def dist_setup():
     return world, rank, local
 
 
+def aggregate_replicas(dev_ms: float, steps: int, world: int, pg=None, device: str = "cpu"):
+    """Replicas only (one independent circuit per rank): the slowest rank's time
+    (all_reduce MAX) is the job's time; the whole-job ms/step divides it by the
+    steps of all ranks.  Returns (max_ms, ms_per_step_per_replica, whole_job_ms_per_step)."""
+    if pg is not None and world > 1:
+        import torch
+        t = torch.tensor([dev_ms], dtype=torch.float64, device=device)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    return dev_ms, dev_ms / steps, dev_ms / (steps * world)
+
+
 def run_gb300(args):
     import torch
     world, rank, local = dist_setup()
@@ -301,12 +313,7 @@ def run_gb300(args):
     nr_iters = int(st1[2] - st0[2])
     launches = int(st1[7] - st0[7])
     rejected = int(st1[1] - st0[1])
-    if pg:
-        t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    ms_per_step = dev_ms / K
-    value = dev_ms / (K * world)  # whole-job: all replicas' steps over the slowest rank's time
+    dev_ms, ms_per_step, value = aggregate_replicas(dev_ms, K, world, pg, device="cuda")
 
     # per-phase split on two more steps (CUDA events on the library's stream)
     dev.profile(1)
@@ -606,13 +613,82 @@ def run_serving(args):
         print(json.dumps(out), flush=True)
 
 
+def mir_flops(model: str) -> int:
+    """FP64 operations per instance of a compiled model, from its MIR op histogram
+    (every arithmetic op, division, square root, exp and log counted as one)."""
+    from vajax_gb300.devices import load_model
+    ops = ("fadd", "fsub", "fmul", "fdiv", "fneg", "sqrt", "exp", "ln", "log", "pow", "fmax", "fmin")
+    return sum(1 for i in load_model(model)["mir"]["instructions"] if i["opcode"] in ops)
+
+
+def run_eval_stamp(args):
+    """Device evaluation + stamping (vgb_build_system) of the network's instances, K timed builds."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    eng, nstats, depth = make_engine(args.gates, max_steps=4)
+    dev, rc = eng.device, eng.rc
+    X = np.zeros(rc.n_nodes + len(rc.vsources))
+    X[: rc.n_nodes] = eng.initial_guess()
+    Xd = torch.as_tensor(X, device="cuda")
+    vs = torch.as_tensor(rc.source_values(0.0), device="cuda")
+    stream = torch.cuda.current_stream()
+    out = dev.build_system(Xd, vs, c0=1e11, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        dev.build_system(Xd, vs, c0=1e11, stream=stream.cuda_stream, out=out)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    sampler = ClockSampler(gpu_index(local))
+    sampler.start()
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dev.build_system(Xd, vs, c0=1e11, stream=stream.cuda_stream, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    t = float(np.mean(ms))
+    n_inst = {g.model: g.n_dev for g in rc.groups}
+    flops = sum(mir_flops(m) * n for m, n in n_inst.items())
+    info = dev.solver_info()
+    # algorithmic bytes: per instance its varying parameters, node voltages and node map and its
+    # contribution slots written; per CSR entry / node row the gather indices, the slots read, the value written
+    nbytes = 0
+    for g in rc.groups:
+        nn = g.node_map.shape[0]
+        from vajax_gb300.devices import model_info
+        nj = len(model_info(g.model).jac)
+        nbytes += g.n_dev * (8 * g.varying.shape[0] + 12 * nn + 8 * (nj + 2 * nn))
+    slots = info["contrib_slots"]
+    nbytes += 12 * slots + 8 * (info["nnz"] + 4 * info["n_aug"])
+    peak, peak_kind = measured_peaks()
+    out_line = {"metric": "eval_plus_stamp_ms", "value": t, "unit": "ms", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                "config": {"workload": "eval_stamp_" + WORKLOAD["workload"], "gates": args.gates,
+                           "instances": n_inst, "l2": "flushed (2x L2 write) before every timed build"},
+                "instances_per_s": sum(n_inst.values()) / (t * 1e-3),
+                "fp64": {"mir_ops_per_instance": {m: mir_flops(m) for m in n_inst}, "achieved_gflops": flops / (t * 1e-3) / 1e9,
+                         "nominal_peak_gflops": 1250.0},
+                "roofline": {"kernel": "eval_kernel + assemble", "bound": "hbm", "achieved": nbytes / (t * 1e-3) / 1e9,
+                             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                             "frac": nbytes / (t * 1e-3) / 1e9 / peak, "traffic": None,
+                             "algorithmic_bytes_per_launch": nbytes},
+                "gpu_launches": len(rc.groups) + 3, "clocks": clocks,
+                "e2e": None}
+    if rank == 0:
+        print(json.dumps(out_line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates", "serving"],
+    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates", "serving", "eval_stamp"],
                     default="gates",
                     help="gates: seeded random gate network, adaptive BDF2 (default, 80k transistors); "
                          "ring: 7-stage ring, fixed-step BDF2 at 1 ps; corners_ring / corners_gates: 1,024 "
@@ -634,6 +710,8 @@ def main():
         run_reference(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "eval_stamp":
+        run_eval_stamp(args)
     else:
         run_gb300(args)
 

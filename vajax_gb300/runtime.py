@@ -152,18 +152,24 @@ class DeviceCircuit:
 
     # ---- device entry points (torch CUDA tensors) -------------------------
     def build_system(self, X, vsrc_vals=None, isrc_vals=None, Q_prev=None, dQdt_prev=None, Q_prev2=None,
-                     c0=0.0, c1=0.0, d1=0.0, c2=0.0, gshunt=0.0):
+                     c0=0.0, c1=0.0, d1=0.0, c2=0.0, gshunt=0.0, stream=None, out=None):
+        """stream: a cudaStream_t handle (int) to launch on (None: the circuit's stream);
+        out: preallocated (csr, f, Q, maxc, fres) tensors to fill."""
         import torch
         dev = X.device
-        csr = torch.empty(max(self.nnz, 1), dtype=torch.float64, device=dev)
-        f = torch.empty(max(self.n_aug, 1), dtype=torch.float64, device=dev)
-        Q = torch.empty(max(self.n_unk, 1), dtype=torch.float64, device=dev)
-        maxc = torch.empty_like(Q)
-        fres = torch.empty_like(Q)
+        if out is None:
+            csr = torch.empty(max(self.nnz, 1), dtype=torch.float64, device=dev)
+            f = torch.empty(max(self.n_aug, 1), dtype=torch.float64, device=dev)
+            Q = torch.empty(max(self.n_unk, 1), dtype=torch.float64, device=dev)
+            maxc = torch.empty_like(Q)
+            fres = torch.empty_like(Q)
+        else:
+            csr, f, Q, maxc, fres = out
         coeffs = np.asarray([c0, c1, d1, c2, gshunt], np.float64)
         self._check(self.lib.vgb_build_system(self.h, _ptr(X), _ptr(vsrc_vals), _ptr(isrc_vals), _ptr(Q_prev),
                                               _ptr(dQdt_prev), _ptr(Q_prev2), _dp(coeffs), _ptr(csr), _ptr(f),
-                                              _ptr(Q), _ptr(maxc), _ptr(fres), None))
+                                              _ptr(Q), _ptr(maxc), _ptr(fres),
+                                              None if stream is None else C.c_void_p(stream)))
         return csr[: self.nnz], f[: self.n_aug], Q[: self.n_unk], maxc[: self.n_unk], fres[: self.n_unk]
 
     def eval_group(self, group: int, X):
