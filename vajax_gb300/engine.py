@@ -105,7 +105,15 @@ class TransientResult:
 
 
 class CircuitEngine:
-    def __init__(self, circuit: Circuit, options: Optional[SimulationOptions] = None, precision: str = "fp64"):
+    def __init__(self, circuit, options: Optional[SimulationOptions] = None, precision: str = "fp64"):
+        """`circuit`: a Circuit, or the path of a VACASK netlist (as the reference's
+        CircuitEngine(sim_path), engine.py:421-486)."""
+        self.analyses = []
+        if not isinstance(circuit, Circuit):
+            from vajax_gb300 import netlist
+            nl = netlist.parse(open(circuit).read(), __import__("pathlib").Path(circuit).parent)
+            self.analyses = nl.analyses
+            circuit = netlist.to_circuit(nl)
         self.circuit = circuit
         self.options = options or SimulationOptions()
         self.precision = precision
@@ -134,9 +142,18 @@ class CircuitEngine:
                 cfg.max_dt = o.maxstep
         return cfg
 
-    def prepare(self, *, t_stop: float, dt: float, adaptive_config: Optional[AdaptiveConfig] = None,
-                max_steps: Optional[int] = None, temperature: Optional[float] = None):
+    def prepare(self, *, t_stop: Optional[float] = None, dt: Optional[float] = None,
+                adaptive_config: Optional[AdaptiveConfig] = None, max_steps: Optional[int] = None,
+                temperature: Optional[float] = None):
+        """t_stop / dt default to the netlist's first ``tran`` analysis (stop=, step=)."""
         from vajax_gb300.runtime import DeviceCircuit
+        if t_stop is None or dt is None:
+            from vajax_gb300.netlist import evaluate
+            tran = next((a for a in self.analyses if a[1] == "tran"), None)
+            if tran is None:
+                raise ValueError("prepare() needs t_stop and dt (the netlist has no tran analysis)")
+            t_stop = float(evaluate(tran[2]["stop"], {})) if t_stop is None else t_stop
+            dt = float(evaluate(tran[2]["step"], {})) if dt is None else dt
         if temperature is not None:
             self.options.temp = temperature - 273.15
         if self.rc is None or temperature is not None:
