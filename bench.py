@@ -372,7 +372,8 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg,
-                                  steps={"ring": 300, "corners_ring": 3}.get(args.workload, 1))
+                                  steps={"ring": 300, "corners_ring": 3}.get(args.workload, 1),
+                                  iters_per_step=nr_iters / max(K, 1))
 
     out = {"metric": "transient_ms_per_step", "value": value, "unit": "ms/step", "n_gpus": world, "steps": K,
            "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
@@ -417,11 +418,24 @@ def _oracle_system(eng, threads=1):
                         threads=threads)
 
 
-def cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg, steps=1):
+def cpu_baseline_sample(eng, X0, Q0, I0, maxc0, cfg, steps=1, iters_per_step=None):
     """The oracle (CPU restatement of the reference path) timed on the host
-    on the first `steps` accepted steps from the same DC state."""
+    on the first `steps` accepted steps from the same DC state.  Networks above
+    60k unknowns (one oracle step takes many minutes there) time a single
+    Newton iteration and scale it by the GPU run's iterations per step (+1
+    post-convergence rebuild)."""
     from oracle.transient import run_transient
     S = _oracle_system(eng)
+    if S.n_aug > 60000 and iters_per_step:
+        from oracle.mna import nr_solve
+        vs = eng.rc.source_values(0.0)
+        t0 = time.perf_counter()
+        nr_solve(S, np.array(X0, np.float64), vs, Q_prev=Q0, c0=1.5e12, c1=-2e12, c2=0.5e12, max_iterations=1)
+        wall = time.perf_counter() - t0
+        return {"value": wall * 1e3 * (iters_per_step + 1), "unit": "ms/step", "cores": 1, "kind": "port",
+                "sample": f"one oracle Newton iteration (build + SuperLU) at the DC point, x {iters_per_step:.2f} "
+                          f"iterations/step of the GPU run + 1 rebuild (an estimate: a full oracle step takes "
+                          f"many minutes at this size)"}
     c = dict(cfg)
     c["max_steps"] = steps + 1
     t0 = time.perf_counter()
@@ -512,7 +526,8 @@ SERVING = dict(workload="serving_poisson200_dc_plus_1000_steps", rate=200.0, job
 
 def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
     """Seeded job stream: Poisson arrivals, sizes log-uniform over rings of 3-31 stages and gate networks of
-    200..max_transistors transistors, a Monte-Carlo corner per job, DC + 1,000 fixed 1 ps gear2 steps each
+    200..max_transistors transistors, a Monte-Carlo corner per job, 1,000 fixed 1 ps gear2 steps each from
+    the DC operating point (networks) or from n1 = VDD (rings)
     (fixed steps keep every job's work bounded; the adaptive controller of the reference can stall on some
     corner-shifted networks, in the oracle as on the GPU)."""
     from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
@@ -531,7 +546,10 @@ def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
             st = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
             st += 1 - st % 2  # odd stage count
             make = (lambda st=st, corner=corner: batch_circuit(ring_oscillator(stages=st), [corner]))
-            opts = dict(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0)
+            # rings start from n1 = VDD: their DC point is metastable, and a transient from it
+            # turns rounding-level differences into an arbitrary oscillation phase
+            opts = dict(tran_method="gear2", fixed_step_transient=True, tran_fs=1.0, icmode="uic",
+                        ic={"c0.n1": 1.2, "c0.vdd": 1.2})
             jobs.append(Job(k, make, t_stop=steps * 1e-12, dt=1e-12, max_steps=steps + 1, options=opts))
             sizes.append(("ring", 2 * st))
         else:

@@ -477,6 +477,8 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         up64(L.d_tasm_ptr, L.tasm_ptr);
         up64(L.d_tch_ptr, L.tch_ptr);
         up64(L.d_fg_ptr, L.fg_ptr);
+        up(L.d_fwd_order, L.fwd_order);
+        up(L.d_bwd_order, L.bwd_order);
         up64(L.d_fg_src, L.fg_src);
         up(L.d_fr_idx, L.fr_idx);
         up(L.d_fr_w, L.fr_w);

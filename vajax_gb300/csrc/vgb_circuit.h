@@ -129,6 +129,7 @@ struct SparseLU {
     std::vector<long long> fr_cv_off;                 // forward-solve contribution vector offsets
     std::vector<long long> fg_ptr;                    // per front row (fr_idx numbering): children's cv entries ...
     std::vector<long long> fg_src;                    // ... added to it, in child order (offsets into cv)
+    std::vector<int> fwd_order, bwd_order;            // claim order of the tree solves (by height / by depth)
     // task list and tiles of the large fronts
     std::vector<int> task_type, task_front, task_i, task_j, task_k;
     std::vector<int> fr_big;                          // 1 = front handled by tile tasks
@@ -145,6 +146,7 @@ struct SparseLU {
     DevBuf<int> d_fr_idx, d_fr_w, d_sn_parent, d_ch_ptr, d_ch_idx, d_em_idx, d_asm_e, d_asm_pos;
     DevBuf<int> d_task_type, d_task_front, d_task_i, d_task_j, d_task_k;
     DevBuf<int> d_fr_big, d_fr_kb, d_fr_nb, d_fr_tile0, d_tasm_e, d_tasm_pos, d_tch;
+    DevBuf<int> d_fwd_order, d_bwd_order;
     DevBuf<int> d_mf_flags;                            // done, -, fwd_done, bwd_done [4 ns]
     DevBuf<int> d_mf_count;                            // final contribution tiles per front [ns]
     DevBuf<int> d_tver;                                // per tile: updates applied, or TILE_FINAL

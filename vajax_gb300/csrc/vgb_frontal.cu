@@ -233,36 +233,57 @@ __device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, i
 constexpr int NWARP = MF_THREADS / 32;
 constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
 
+// Pivot of step p (checked, replaced by 1e-30 and flagged when zero) and its
+// reciprocal; called by the warp that owns column p after its last update.
+template <typename T>
+__device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T* rinv) {
+    T piv = __shfl_sync(0xffffffffu, col, p);
+    if (piv == (T)0 || !isfinite((double)piv)) {
+        piv = (T)1e-30;
+        if (lane == p) col = piv;
+        if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
+    }
+    const T r = (T)1 / piv;
+    if (lane == 0) *rinv = r;
+}
+
 // LU without pivoting of the leading n x n block of a tile.  lane = row; warp
-// g owns columns g, g + 4, ... in registers.
+// g owns columns g, g + 4, ... in registers.  The owner of column p + 1
+// updates that column first and forms the next pivot's reciprocal while the
+// other warps finish step p, which keeps the FP64 division off the chain of
+// dependent steps.
 template <typename T>
 __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    T* rinv = xch + 32;
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = t[lane + (g + NWARP * q) * LD];
+    if (g == 0 && n > 0) next_pivot<T>(a[0], 0, lane, err, rinv);
+    __syncthreads();
 #pragma unroll
     for (int p = 0; p < FRONT_TILE; ++p) {
         if (p < n) {
             if (g == (p & (NWARP - 1))) {
-                // owner of column p: pivot, multipliers L(:, p) for the other warps
+                // owner of column p: multipliers L(:, p) for the other warps
                 const int qp = p / NWARP;
-                T piv = __shfl_sync(0xffffffffu, a[qp], p);
-                if (piv == (T)0 || !isfinite((double)piv)) {
-                    piv = (T)1e-30;
-                    if (lane == p) a[qp] = piv;
-                    if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
-                }
-                if (lane > p) a[qp] /= piv;
+                if (lane > p) a[qp] *= *rinv;
                 xch[lane] = a[qp];
             }
             __syncthreads();
             const T l = xch[lane];
+            const int p1 = p + 1;
+            if (p1 < n && g == (p1 & (NWARP - 1))) {
+                const int q1 = p1 / NWARP;
+                const T u = __shfl_sync(0xffffffffu, a[q1], p);
+                if (lane > p) a[q1] -= l * u;
+                next_pivot<T>(a[q1], p1, lane, err, rinv);
+            }
 #pragma unroll
             for (int q = 0; q < QPW; ++q) {
                 const int c = g + NWARP * q;
                 const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
-                if (c > p && c < n && lane > p) a[q] -= l * u;
+                if (c > p1 && c < n && lane > p) a[q] -= l * u;
             }
             __syncthreads();
         }
@@ -277,14 +298,17 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
 template <typename T>
 __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    T* dinv = xch + 32;  // reciprocals of the diagonal, formed once in parallel
+    if (threadIdx.x < n) dinv[threadIdx.x] = (T)1 / d[threadIdx.x + threadIdx.x * LD];
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = x[lane + (g + NWARP * q) * LD];
+    __syncthreads();
 #pragma unroll
     for (int c = 0; c < FRONT_TILE; ++c) {
         if (c < n) {
             if (g == (c & (NWARP - 1))) {
-                a[c / NWARP] /= d[c + c * LD];
+                a[c / NWARP] *= dinv[c];
                 xch[lane] = a[c / NWARP];
             }
             __syncthreads();
@@ -448,6 +472,7 @@ struct MFSolveArgs {
     const long long* fg_ptr;   // per front row: children's update entries, in child order
     const long long* fg_src;
     const int* q;          // B index of each permuted M index
+    const int* order;      // claim order of the fronts
     int* flags;            // fwd [ns], bwd [ns]
     int* counter;
     int* abort_flag;
@@ -468,7 +493,10 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
     int* const fdone = a.flags;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     while (true) {
-        if (threadIdx.x == 0) s_S = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) {
+            const int c = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
+            s_S = c < a.ns ? a.order[c] : a.ns;
+        }
         __syncthreads();
         const int S = s_S;
         __syncthreads();
@@ -539,7 +567,7 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
         const int c = s_S;
         __syncthreads();
         if (c >= a.ns) return;
-        const int S = a.ns - 1 - c;
+        const int S = a.order[c];
         const int P = a.sn_parent[S];
         bool ok = true;
         if (threadIdx.x == 0 && P >= 0) ok = wait_eq(bdone + P, a.epoch, a.abort_flag, a.err, a.spin_limit);
@@ -730,8 +758,10 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
         cur = smem;
     }
     const int blocks = std::min(sm_count() * 4, L.nsn);
+    a.order = L.d_fwd_order.p;
     mf_fwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, rhsM, y, cv);
     a.counter = L.d_counters.p + 2;
+    a.order = L.d_bwd_order.p;
     mf_bwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, y, xs, xout);
     VGB_CUDA(cudaGetLastError());
 }

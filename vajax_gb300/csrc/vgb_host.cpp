@@ -553,6 +553,22 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
     }
     L.fr_tile0[ns] = (int)ntile;
     L.n_tiles = ntile;
+    // claim orders of the tree solves: forward by height (leaves first, a front
+    // after all of its children), backward by depth (root first, a front after
+    // its parent); both are topological and put ready fronts early
+    {
+        std::vector<int> height(ns, 0), depth(ns, 0);
+        for (int s = 0; s < ns; ++s)
+            if (L.sn_parent[s] >= 0) height[L.sn_parent[s]] = std::max(height[L.sn_parent[s]], height[s] + 1);
+        for (int s = ns - 1; s >= 0; --s)
+            if (L.sn_parent[s] >= 0) depth[s] = depth[L.sn_parent[s]] + 1;
+        L.fwd_order.resize(ns);
+        L.bwd_order.resize(ns);
+        std::iota(L.fwd_order.begin(), L.fwd_order.end(), 0);
+        std::iota(L.bwd_order.begin(), L.bwd_order.end(), 0);
+        std::stable_sort(L.fwd_order.begin(), L.fwd_order.end(), [&](int a, int b) { return height[a] < height[b]; });
+        std::stable_sort(L.bwd_order.begin(), L.bwd_order.end(), [&](int a, int b) { return depth[a] < depth[b]; });
+    }
     // forward solve: each front row gathers its children's update entries in child order
     {
         std::vector<std::vector<long long>> g(L.fr_idx.size());
