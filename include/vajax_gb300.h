@@ -83,7 +83,7 @@ int vgb_circuit_analyze(void* h);
 /* Solver statistics after analysis, out[16] = {n_aug, nnz, nnz_lu, lu_flops,
  * etree_height, max_factor_column, critical_path_tasks, contribution_slots,
  * supernodes, max_front, front_storage, front_flops, front_tree_depth,
- * schedule_makespan_ns (simulated), factorisation_tasks, 0}. */
+ * schedule_makespan_ns (simulated), factorisation_tasks, warp_solved_fronts}. */
 int vgb_solver_info(void* h, int64_t* out);
 
 /* Static-pivot ordering: perm_r[n_aug] (row r of the factorised matrix is row

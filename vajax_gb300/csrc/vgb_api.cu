@@ -320,6 +320,7 @@ int vgb_solver_info(void* h, int64_t* out) {
         out[12] = L.mf_depth;
         out[13] = (int64_t)L.sched_makespan_ns;
         out[14] = (int64_t)L.task_type.size();
+        out[15] = L.n_small_solve;
     });
 }
 
@@ -507,7 +508,7 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
         L.d_mf_flags.zero(c->stream);
         L.d_mf_count.alloc(std::max(L.nsn, 1));
-        L.d_counters.alloc(4);
+        L.d_counters.alloc(8);
         const size_t na = std::max(c->n_aug, 1), nu = std::max(c->n_unk, 1);
         c->d_csr_vals.alloc(std::max(c->nnz, 1));
         c->d_f.alloc(na);

@@ -129,7 +129,9 @@ struct SparseLU {
     std::vector<long long> fr_cv_off;                 // forward-solve contribution vector offsets
     std::vector<long long> fg_ptr;                    // per front row (fr_idx numbering): children's cv entries ...
     std::vector<long long> fg_src;                    // ... added to it, in child order (offsets into cv)
-    std::vector<int> fwd_order, bwd_order;            // claim order of the tree solves (by height / by depth)
+    std::vector<int> fwd_order, bwd_order;            // claim order of the tree solves (by height / by depth):
+    int n_small_solve = 0;                            // the first n_small fronts of fwd_order / last of bwd_order
+                                                      // are solved by one warp each (subtrees of small fronts)
     // task list and tiles of the large fronts
     std::vector<int> task_type, task_front, task_i, task_j, task_k;
     std::vector<int> fr_big;                          // 1 = front handled by tile tasks

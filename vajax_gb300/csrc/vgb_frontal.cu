@@ -473,17 +473,95 @@ struct MFSolveArgs {
     const long long* fg_src;
     const int* q;          // B index of each permuted M index
     const int* order;      // claim order of the fronts
+    int n_small;           // fronts solved one per warp: order[0, n_small) forward, order[ns - n_small, ns) backward
     int* flags;            // fwd [ns], bwd [ns]
     int* counter;
+    int* counter_small;
     int* abort_flag;
     int* err;
     int epoch;
     unsigned spin_limit;
 };
 
+// One warp solves a front of order m <= 32 (lane = row): forward with its
+// unit-lower columns, the update vector for the parent in the same pass.
+template <typename T>
+__device__ void fwd_small_warp(const MFSolveArgs& a, int S, const T* __restrict__ pool, const T* __restrict__ rhs,
+                               T* y, T* cv, int lane) {
+    int* const fdone = a.flags;
+    bool ok = true;
+    for (int q = a.ch_ptr[S] + lane; q < a.ch_ptr[S + 1]; q += 32)
+        ok = ok && wait_eq(fdone + a.ch_idx[q], a.epoch, a.abort_flag, a.err, a.spin_limit);
+    if (!__all_sync(0xffffffffu, ok)) return;
+    const int m = (int)(a.fr_ptr[S + 1] - a.fr_ptr[S]);
+    const int w = a.fr_w[S];
+    const int* idx = a.fr_idx + a.fr_ptr[S];
+    const T* F = pool + a.fr_off[S];
+    const long long* gp = a.fg_ptr + a.fr_ptr[S];
+    T u = (T)0;
+    if (lane < m) {
+        u = lane < w ? rhs[idx[lane]] : (T)0;
+        for (long long e = gp[lane]; e < gp[lane + 1]; ++e) u += __ldcg(cv + a.fg_src[e]);
+    }
+    for (int p = 0; p < w; ++p) {
+        const T yp = __shfl_sync(0xffffffffu, u, p);
+        if (lane > p && lane < m) u -= F[lane + (long long)p * m] * yp;
+    }
+    if (lane < m) {
+        if (lane < w) y[idx[lane]] = u;
+        else cv[a.cv_off[S] + (lane - w)] = u;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        __threadfence();
+        st_rel(fdone + S, a.epoch);
+    }
+}
+
+// One warp solves a front of order m <= 32 (lane = row): z = y - U12 x_tail,
+// then back substitution with the upper diagonal block.
+template <typename T>
+__device__ void bwd_small_warp(const MFSolveArgs& a, int S, const T* __restrict__ pool, const T* __restrict__ y,
+                               T* xs, double* xout, int lane) {
+    int* const bdone = a.flags + a.ns;
+    const int P = a.sn_parent[S];
+    bool ok = true;
+    if (lane == 0 && P >= 0) ok = wait_eq(bdone + P, a.epoch, a.abort_flag, a.err, a.spin_limit);
+    if (!__shfl_sync(0xffffffffu, ok, 0)) return;
+    const int m = (int)(a.fr_ptr[S + 1] - a.fr_ptr[S]);
+    const int w = a.fr_w[S];
+    const int* idx = a.fr_idx + a.fr_ptr[S];
+    const T* F = pool + a.fr_off[S];
+    const T xt = lane < m - w ? __ldcg(xs + idx[w + lane]) : (T)0;
+    T z = (T)0;
+    T s = (T)0;
+    for (int j = 0; j < m - w; ++j) {
+        const T xj = __shfl_sync(0xffffffffu, xt, j);
+        if (lane < w) s += F[lane + (long long)(w + j) * m] * xj;
+    }
+    if (lane < w) z = y[idx[lane]] - s;
+    const T dinv = lane < w ? (T)1 / F[lane + (long long)lane * m] : (T)0;
+    for (int p = w - 1; p >= 0; --p) {
+        if (lane == p) z *= dinv;
+        const T xp = __shfl_sync(0xffffffffu, z, p);
+        if (lane < p) z -= F[lane + (long long)p * m] * xp;
+    }
+    if (lane < w) {
+        xs[idx[lane]] = z;
+        xout[a.q[idx[lane]]] = (double)z;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        __threadfence();
+        st_rel(bdone + S, a.epoch);
+    }
+}
+
 // Forward: L y = rhs.  Each front adds its children's update vectors (child
 // order), solves with its unit-lower diagonal block 32 pivots at a time (one
 // warp, register shuffles) and updates the rows below with the same columns.
+// Subtrees of small fronts come first, one front per warp; then the CTAs take
+// the remaining fronts one at a time.
 template <typename T>
 __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const T* __restrict__ pool,
                                                             const T* __restrict__ rhs, T* y, T* cv) {
@@ -493,8 +571,16 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
     int* const fdone = a.flags;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     while (true) {
+        int c = 0;
+        if (lane == 0) c = *(volatile int*)a.abort_flag ? a.n_small : atomicAdd(a.counter_small, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= a.n_small) break;
+        fwd_small_warp<T>(a, a.order[c], pool, rhs, y, cv, lane);
+    }
+    __syncthreads();
+    while (true) {
         if (threadIdx.x == 0) {
-            const int c = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
+            const int c = *(volatile int*)a.abort_flag ? a.ns : a.n_small + atomicAdd(a.counter, 1);
             s_S = c < a.ns ? a.order[c] : a.ns;
         }
         __syncthreads();
@@ -561,12 +647,13 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
     __shared__ int s_S;
     int* const bdone = a.flags + a.ns;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n_big = a.ns - a.n_small;
     while (true) {
-        if (threadIdx.x == 0) s_S = *(volatile int*)a.abort_flag ? a.ns : atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) s_S = *(volatile int*)a.abort_flag ? n_big : atomicAdd(a.counter, 1);
         __syncthreads();
         const int c = s_S;
         __syncthreads();
-        if (c >= a.ns) return;
+        if (c >= n_big) break;
         const int S = a.order[c];
         const int P = a.sn_parent[S];
         bool ok = true;
@@ -640,6 +727,13 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
             xout[a.q[idx[p]]] = (double)z[p];
         }
         publish(bdone + S, a.epoch);
+    }
+    while (true) {
+        int c = 0;
+        if (lane == 0) c = *(volatile int*)a.abort_flag ? a.n_small : atomicAdd(a.counter_small, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= a.n_small) break;
+        bwd_small_warp<T>(a, a.order[n_big + c], pool, y, xs, xout, lane);
     }
 }
 
@@ -725,7 +819,7 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     const T* pool = std::is_same<T, float>::value ? (const T*)L.d_pool32.p : (const T*)L.d_pool64.p;
     T* cv = std::is_same<T, float>::value ? (T*)L.d_cv32.p : (T*)L.d_cv64.p;
     L.epoch++;
-    VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
+    VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(int), s));
     MFSolveArgs a{};
     a.ns = L.nsn;
     a.fr_ptr = L.d_fr_ptr.p;
@@ -741,6 +835,7 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.fg_ptr = L.d_fg_ptr.p;
     a.fg_src = L.d_fg_src.p;
     a.q = L.d_q.p;
+    a.n_small = L.n_small_solve;
     a.flags = L.d_mf_flags.p + 2 * (size_t)L.nsn;
     a.counter = L.d_counters.p + 1;
     a.abort_flag = L.d_counters.p + 3;
@@ -759,8 +854,10 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     }
     const int blocks = std::min(sm_count() * 4, L.nsn);
     a.order = L.d_fwd_order.p;
+    a.counter_small = L.d_counters.p + 4;
     mf_fwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, rhsM, y, cv);
     a.counter = L.d_counters.p + 2;
+    a.counter_small = L.d_counters.p + 5;
     a.order = L.d_bwd_order.p;
     mf_bwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, y, xs, xout);
     VGB_CUDA(cudaGetLastError());

@@ -566,8 +566,24 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
         L.bwd_order.resize(ns);
         std::iota(L.fwd_order.begin(), L.fwd_order.end(), 0);
         std::iota(L.bwd_order.begin(), L.bwd_order.end(), 0);
-        std::stable_sort(L.fwd_order.begin(), L.fwd_order.end(), [&](int a, int b) { return height[a] < height[b]; });
-        std::stable_sort(L.bwd_order.begin(), L.bwd_order.end(), [&](int a, int b) { return depth[a] < depth[b]; });
+        // fronts whose whole subtree has order <= 32 are solved by one warp each; they come
+        // first in the forward order and last in the backward order
+        std::vector<char> small(ns, 0);
+        for (int s = 0; s < ns; ++s) {
+            bool ok = (L.fr_ptr[s + 1] - L.fr_ptr[s]) <= 32;
+            for (int q = L.ch_ptr[s]; q < L.ch_ptr[s + 1] && ok; ++q) ok = small[L.ch_idx[q]] != 0;
+            small[s] = ok ? 1 : 0;
+        }
+        std::stable_sort(L.fwd_order.begin(), L.fwd_order.end(), [&](int a, int b) {
+            if (small[a] != small[b]) return small[a] > small[b];
+            return height[a] < height[b];
+        });
+        std::stable_sort(L.bwd_order.begin(), L.bwd_order.end(), [&](int a, int b) {
+            if (small[a] != small[b]) return small[a] < small[b];
+            return depth[a] < depth[b];
+        });
+        L.n_small_solve = 0;
+        for (int s = 0; s < ns; ++s) L.n_small_solve += small[s];
     }
     // forward solve: each front row gathers its children's update entries in child order
     {

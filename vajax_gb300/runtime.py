@@ -122,7 +122,7 @@ class DeviceCircuit:
         self._check(self.lib.vgb_solver_info(self.h, out.ctypes.data_as(_lib.i64p)))
         keys = ["n_aug", "nnz", "nnz_lu", "lu_flops", "etree_height", "max_col", "crit_path", "contrib_slots",
                 "supernodes", "max_front", "front_storage", "front_flops", "front_depth", "sched_makespan_ns",
-                "tasks"]
+                "tasks", "warp_solved_fronts"]
         return dict(zip(keys, map(int, out)))
 
     def solver_order(self):
