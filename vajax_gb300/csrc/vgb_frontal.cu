@@ -10,7 +10,9 @@
 //                of one warp;
 //   TASK_TRSM_L  tile (i, k) below it: L(i,k) = A(i,k) U(k,k)^-1;
 //   TASK_TRSM_U  tile (k, j) right of it: U(k,j) = L(k,k)^-1 A(k,j);
-//   TASK_GEMM    trailing tile (i, j): A(i,j) -= L(i,k) U(k,j).
+//   TASK_GEMM    trailing tile (i, j): A(i,j) -= L(i,k) U(k,j), except the
+//                update of the next diagonal tile (k+1, k+1) of the pivot block,
+//                which GETRF(k+1) applies itself before it factorises the tile.
 //
 // Large fronts are never assembled as a whole: the first task that touches a
 // tile (the k = 0 task of that tile) builds it in shared memory from its A
@@ -187,13 +189,36 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
 
 // ---- tiles of large fronts -----------------------------------------------------
 
-// tile rows [r0, r0+nr) x columns [c0, c0+nc) of front F (leading dimension m) into a
-// zero-padded 32 x 32 shared-memory tile
+// The tile kernels below spread each elimination step over the CTA's four
+// warps (one per SM sub-partition: FP64 issue is the bottleneck on this part)
+// and exchange the step's pivot row or column through shared memory.
+constexpr int NWARP = MF_THREADS / 32;
+constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
+
+// Tile rows [r0, r0+nr) x columns [c0, c0+nc) of front F (leading dimension m),
+// zero-padded to 32 x 32, held in registers (lane = row, warp w has columns w,
+// w + 4, ...).  fetch_tile only issues the loads, so a task fetches all of its
+// tiles before the first shared-memory store and their L2 latencies overlap.
 template <typename T>
-__device__ void load_tile(T* dst, const T* F, long long m, int r0, int nr, int c0, int nc) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int c = warp; c < FRONT_TILE; c += nw)
-        dst[lane + c * LD] = (lane < nr && c < nc) ? __ldcg(F + (r0 + lane) + (c0 + c) * m) : (T)0;
+struct TileRegs {
+    T v[QPW];
+};
+
+template <typename T>
+__device__ __forceinline__ void fetch_tile(TileRegs<T>& t, const T* F, long long m, int r0, int nr, int c0, int nc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < QPW; ++q) {
+        const int c = warp + NWARP * q;
+        t.v[q] = (lane < nr && c < nc) ? __ldcg(F + (r0 + lane) + (c0 + c) * m) : (T)0;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void put_tile(T* dst, const TileRegs<T>& t) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < QPW; ++q) dst[lane + (warp + NWARP * q) * LD] = t.v[q];
 }
 
 template <typename T>
@@ -226,12 +251,6 @@ __device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, i
         __syncthreads();
     }
 }
-
-// The tile kernels below spread each elimination step over the CTA's four
-// warps (one per SM sub-partition: FP64 issue is the bottleneck on this part)
-// and exchange the step's pivot row or column through shared memory.
-constexpr int NWARP = MF_THREADS / 32;
-constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
 
 // Pivot of step p (checked, replaced by 1e-30 and flagged when zero) and its
 // reciprocal; called by the warp that owns column p after its last update.
@@ -282,8 +301,10 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
 #pragma unroll
             for (int q = 0; q < QPW; ++q) {
                 const int c = g + NWARP * q;
-                const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
-                if (c > p1 && c < n && lane > p) a[q] -= l * u;
+                if (c > p1) {  // warp-uniform: finished columns issue no FP64 work
+                    const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
+                    if (c < n && lane > p) a[q] -= l * u;
+                }
             }
             __syncthreads();
         }
@@ -408,21 +429,44 @@ __global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(M
         T* T1 = sm + TILE_ELEMS;
         T* T2 = sm + 2 * TILE_ELEMS;
         if (type == TASK_GETRF) {
-            const bool ok = k == 0 ? wait_children(a, S) : wait3(a, tv + k * nb + k, k, nullptr, 0, nullptr, 0);
+            // GETRF(k) for k > 0 first applies the last update of its diagonal tile,
+            // A(k,k) -= L(k,k-1) U(k-1,k), which has no task of its own: that keeps one
+            // hand-off per pivot step off the chain of dependent diagonal tiles.
+            const long long dk = (long long)k * nb + k;
+            bool ok;
+            if (k == 0) ok = wait_children(a, S);
+            else ok = wait3(a, tv + dk - 1, TILE_FINAL, tv + (long long)(k - 1) * nb + k, TILE_FINAL,
+                            k > 1 ? tv + dk : nullptr, k - 1);
             if (!ok) continue;
-            if (k == 0) assemble_tile<T>(a, tb, T0, 0, 0, pool);
-            else load_tile<T>(T0, FS, m, k0, nk, k0, nk);
+            if (k == 0) {
+                assemble_tile<T>(a, tb, T2, 0, 0, pool);
+            } else {
+                const int p0 = tile_lo(k - 1, kb, w), np = tile_hi(k - 1, kb, nb, w, m) - p0;
+                TileRegs<T> lt, ut, dt;
+                fetch_tile(lt, FS, m, k0, nk, p0, np);
+                fetch_tile(ut, FS, m, p0, np, k0, nk);
+                if (k > 1) fetch_tile(dt, FS, m, k0, nk, k0, nk);
+                put_tile(T0, lt);
+                put_tile(T1, ut);
+                if (k > 1) put_tile(T2, dt);
+                else assemble_tile<T>(a, tb + dk, T2, k0, k0, pool);  // first touch of tile (1, 1)
+                __syncthreads();
+                gemm_tile<T>(T2, T0, T1, np, nk);
+            }
             __syncthreads();
-            getrf_tile<T>(T0, nk, a.err, T2);
-            store_tile<T>(FS, T0, m, k0, nk, k0, nk);
-            publish(tv + k * nb + k, TILE_FINAL);
+            getrf_tile<T>(T2, nk, a.err, T0);
+            store_tile<T>(FS, T2, m, k0, nk, k0, nk);
+            publish(tv + dk, TILE_FINAL);
             if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
         } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
             const int* own = tv + (long long)i * nb + j;
-            if (!wait3(a, tv + k * nb + k, TILE_FINAL, k > 0 ? own : nullptr, k, nullptr, 0)) continue;
-            load_tile<T>(T0, FS, m, k0, nk, k0, nk);
+            if (!wait3(a, tv + (long long)k * nb + k, TILE_FINAL, k > 0 ? own : nullptr, k, nullptr, 0)) continue;
+            TileRegs<T> dt, xt;
+            fetch_tile(dt, FS, m, k0, nk, k0, nk);
+            if (k > 0) fetch_tile(xt, FS, m, r0, nr, c0, nc);
+            put_tile(T0, dt);
             if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T1, r0, c0, pool);
-            else load_tile<T>(T1, FS, m, r0, nr, c0, nc);
+            else put_tile(T1, xt);
             __syncthreads();
             if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk, T2);
             else trsm_u_tile<T>(T1, T0, nk, T2);
@@ -433,10 +477,14 @@ __global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(M
             if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + j, TILE_FINAL,
                        k > 0 ? own : nullptr, k))
                 continue;
-            load_tile<T>(T0, FS, m, r0, nr, k0, nk);
-            load_tile<T>(T1, FS, m, k0, nk, c0, nc);
+            TileRegs<T> lt, ut, ct;
+            fetch_tile(lt, FS, m, r0, nr, k0, nk);
+            fetch_tile(ut, FS, m, k0, nk, c0, nc);
+            if (k > 0) fetch_tile(ct, FS, m, r0, nr, c0, nc);
+            put_tile(T0, lt);
+            put_tile(T1, ut);
             if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T2, r0, c0, pool);
-            else load_tile<T>(T2, FS, m, r0, nr, c0, nc);
+            else put_tile(T2, ct);
             __syncthreads();
             gemm_tile<T>(T2, T0, T1, nk, nc);
             store_tile<T>(FS, T2, m, r0, nr, c0, nc);

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <numeric>
 #include <queue>
+#include <unordered_map>
 
 #include "vgb_circuit.h"
 
@@ -260,23 +261,28 @@ static void schedule_tasks(SparseLU& L) {
     const int nt = (int)L.task_type.size();
     if (nt == 0) return;
     const int ns = L.nsn;
-    // index of each task inside its front's block
+    // task of (front, type, tile (i, j), step k)
+    std::unordered_map<long long, int> task_of;
+    task_of.reserve(2 * (size_t)nt);
+    auto key = [&](int s, int type, int i, int j, int k) {
+        const long long tile = (long long)L.fr_tile0[s] + (long long)i * L.fr_nb[s] + j;
+        return ((tile << 16) + k) * 8 + type;  // k < nb < 2^16
+    };
     std::vector<int> front_task0(ns, -1);
-    for (int t = 0; t < nt; ++t)
-        if (front_task0[L.task_front[t]] < 0) front_task0[L.task_front[t]] = t;
-    auto blk = [&](int s, int k) {  // first task of pivot step k of a large front
-        const int nb = L.fr_nb[s];
-        long long off = 0;
-        for (int q = 0; q < k; ++q) off += (long long)(nb - q) * (nb - q);
-        return front_task0[s] + (int)off;
+    for (int t = 0; t < nt; ++t) {
+        const int s = L.task_front[t];
+        if (front_task0[s] < 0) front_task0[s] = t;
+        if (L.task_type[t] != TASK_SMALL) task_of[key(s, L.task_type[t], L.task_i[t], L.task_j[t], L.task_k[t])] = t;
+    }
+    auto find = [&](int s, int type, int i, int j, int k) {
+        const auto it = task_of.find(key(s, type, i, j, k));
+        VGB_REQUIRE(it != task_of.end(), "missing factorisation task");
+        return it->second;
     };
-    auto getrf = [&](int s, int k) { return blk(s, k); };
-    auto trsm_l = [&](int s, int i, int k) { return blk(s, k) + 1 + (i - k - 1); };
-    auto trsm_u = [&](int s, int k, int j) { return blk(s, k) + 1 + (L.fr_nb[s] - k - 1) + (j - k - 1); };
-    auto gemm = [&](int s, int i, int j, int k) {
-        const int r = L.fr_nb[s] - k - 1;
-        return blk(s, k) + 1 + 2 * r + (j - k - 1) * r + (i - k - 1);
-    };
+    auto getrf = [&](int s, int k) { return find(s, TASK_GETRF, k, k, k); };
+    auto trsm_l = [&](int s, int i, int k) { return find(s, TASK_TRSM_L, i, k, k); };
+    auto trsm_u = [&](int s, int k, int j) { return find(s, TASK_TRSM_U, k, j, k); };
+    auto gemm = [&](int s, int i, int j, int k) { return find(s, TASK_GEMM, i, j, k); };
     // the tasks whose completion completes a front
     std::vector<std::vector<int>> finals(ns);
     for (int s = 0; s < ns; ++s) {
@@ -307,8 +313,15 @@ static void schedule_tasks(SparseLU& L) {
         const double tile = FRONT_TILE;
         if (type == TASK_GETRF) {
             cost[t] = 3000 + (2.0 / 3.0) * tile * tile * tile / 2;
-            if (k == 0) children_done(s, pred[t]);
-            else pred[t].push_back(gemm(s, k, k, k - 1));
+            if (k == 0) {
+                children_done(s, pred[t]);
+            } else {
+                // also applies the diagonal tile's update of step k - 1
+                cost[t] += 2.0 * tile * tile * tile / 2;
+                pred[t].push_back(trsm_l(s, k, k - 1));
+                pred[t].push_back(trsm_u(s, k - 1, k));
+                if (k > 1) pred[t].push_back(gemm(s, k, k, k - 2));
+            }
         } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
             cost[t] = 2500 + tile * tile * tile / 2;
             pred[t].push_back(getrf(s, k));
@@ -508,8 +521,9 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
     // fronts are one task; a large front of order m with w pivots has kb =
     // ceil(w/32) pivot tiles and nb = kb + ceil((m-w)/32) tiles per dimension,
     // and for each pivot tile k: GETRF(k), TRSM_L(i,k) and TRSM_U(k,j) for
-    // i, j > k, then GEMM(i,j,k) for i, j > k.  Every task waits only on tasks
-    // that precede it in the list.
+    // i, j > k, then GEMM(i,j,k) for i, j > k except the next diagonal pivot
+    // tile (k+1, k+1), whose update GETRF(k+1) applies.  Every task waits only
+    // on tasks that precede it in the list.
     L.fr_cv_off.assign(ns + 1, 0);
     L.task_type.clear();
     L.task_front.clear();
@@ -542,13 +556,15 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
         L.fr_big[s] = 1;
         L.fr_kb[s] = kb;
         L.fr_nb[s] = nb;
+        VGB_REQUIRE(nb < (1 << 16), "front has too many tiles");
         ntile += (long long)nb * nb;
         for (int k = 0; k < kb; ++k) {
             push_task(TASK_GETRF, s, k, k, k);
             for (int i = k + 1; i < nb; ++i) push_task(TASK_TRSM_L, s, i, k, k);
             for (int j = k + 1; j < nb; ++j) push_task(TASK_TRSM_U, s, k, j, k);
             for (int j = k + 1; j < nb; ++j)
-                for (int i = k + 1; i < nb; ++i) push_task(TASK_GEMM, s, i, j, k);
+                for (int i = k + 1; i < nb; ++i)
+                    if (!(i == k + 1 && j == k + 1 && k + 1 < kb)) push_task(TASK_GEMM, s, i, j, k);
         }
     }
     L.fr_tile0[ns] = (int)ntile;
