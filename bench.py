@@ -276,6 +276,7 @@ def run_gb300(args):
                                          refine=args.refine)
     dev = eng.device
     info = dev.solver_info()
+    tuning = eng.tune()["tuning"] if args.autotune == "on" else dev.tuning()
     t0 = time.perf_counter()
     X0, Q0, I0, maxc0, dc_ok = eng.initial_state()
     dc_s = time.perf_counter() - t0
@@ -379,7 +380,7 @@ def run_gb300(args):
            "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32lu",
            "data": "synthetic (seeded generator)",
-           "config": workload_config(args, ring, nstats, depth, info, world, dc_s, eng),
+           "config": {**workload_config(args, ring, nstats, depth, info, world, dc_s, eng), "tuning": tuning},
            "newton_iters_per_s": nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "instances": n_inst, "solves_per_s": n_inst * nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "newton_iters": nr_iters, "rejected_steps": rejected, "host_wall_ms_per_step": wall_s * 1e3 / K,
@@ -720,6 +721,8 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")
     ap.add_argument("--max-transistors", type=int, default=SERVING["network_transistors"][1],
                     help="serving: largest gate network in the stream")
+    ap.add_argument("--autotune", choices=["on", "off"], default="on",
+                    help="tune launch shapes and the factorisation schedule before the run (outside the timing)")
     ap.add_argument("--reference-budget", type=float, default=150.0, help="seconds of timed CPU work, reference arm")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":

@@ -76,6 +76,28 @@ int vgb_circuit_set_sources(void* h, int is_current, int n, const int* kinds, co
  * convergence test (solver_factories.py:37-100, residual_conv_mask). */
 int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx);
 
+/* Circuit node indices of NOI (noise-correlation) nodes.  Before every Newton
+ * solve their Jacobian rows and columns are zeroed, their diagonal set to 1
+ * and their residual to 0, so their update is exactly 0, and they are left out
+ * of the residual test (solver_factories.py:37-137 _compute_noi_masks,
+ * :775-782 enforce_noi; full_mna.py:360-369).  Call before analysis. */
+int vgb_circuit_set_noi_nodes(void* h, int n, const int* node_idx);
+
+/* Launch shapes and the factorisation schedule, picked per circuit by the
+ * autotuner (vajax_gb300/autotune.py).  The reference has no counterpart: its
+ * sparse solve is a library call (solver_factories.py:895-922, cuDSS).
+ *   VGB_TUNE_FACTOR_CTAS_PER_SM  1..4 persistent factorisation CTAs per SM; the
+ *                                task list is re-scheduled for that many workers
+ *   VGB_TUNE_SOLVE_CTAS_PER_SM   1..8 tree-solve CTAs per SM
+ *   VGB_TUNE_EVAL_BLOCK          32..256 (multiple of 32) device-evaluation threads
+ *                                per block
+ * Defaults: 4, 4, 64.  Not thread-safe against work in flight on other streams. */
+#define VGB_TUNE_FACTOR_CTAS_PER_SM 0
+#define VGB_TUNE_SOLVE_CTAS_PER_SM 1
+#define VGB_TUNE_EVAL_BLOCK 2
+int vgb_set_tuning(void* h, int knob, int value);
+int vgb_get_tuning(void* h, int knob, int* value);
+
 /* Host-only analysis: CSR pattern, stamp maps, gather lists, ordering and
  * symbolic factorisation.  Touches no GPU; the pattern getters below work
  * after this call.  finalize() runs it when it has not been run. */

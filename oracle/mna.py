@@ -76,6 +76,7 @@ class OracleSystem:
         self.n_unk = rc.n_nodes - 1
         self.n_vsrc = len(rc.vsrc_p)
         self.n_aug = self.n_unk + self.n_vsrc
+        self._noi_nodes = list(getattr(rc, "noi_nodes", ()))
         self.vp = np.asarray(rc.vsrc_p, np.int64)
         self.vn = np.asarray(rc.vsrc_n, np.int64)
         self.ip = np.asarray(rc.isrc_p, np.int64)
@@ -137,6 +138,32 @@ class OracleSystem:
             self.vs_pos[1] = self._positions(np.where(vn, self.vn - 1, -1), np.where(vn, br, -1))
             self.vs_pos[2] = self._positions(np.where(vp, br, -1), np.where(vp, self.vp - 1, -1))
             self.vs_pos[3] = self._positions(np.where(vn, br, -1), np.where(vn, self.vn - 1, -1))
+        self.set_noi(getattr(self, "_noi_nodes", ()))
+
+    def set_noi(self, noi_nodes):
+        """NOI masks of _compute_noi_masks (solver_factories.py:37-137): residual
+        indices of the NOI nodes and the CSR positions of their rows, columns and
+        diagonals."""
+        self.noi = np.asarray(sorted(set(int(i) - 1 for i in noi_nodes)), np.int64)
+        rows = np.repeat(np.arange(self.n_aug), np.diff(self.indptr))
+        is_noi = np.zeros(self.n_aug, bool)
+        is_noi[self.noi] = True
+        hit = is_noi[rows] | is_noi[self.indices]
+        diag = hit & (rows == self.indices)
+        self.noi_zero = np.nonzero(hit & ~diag)[0]
+        self.noi_diag = np.nonzero(diag)[0]
+
+    def enforce_noi(self, csr, f):
+        """enforce_noi (solver_factories.py:775-782): J rows / columns of NOI
+        unknowns zeroed, their diagonal 1, their residual 0."""
+        if self.noi.size == 0:
+            return csr, f
+        csr = csr.copy()
+        f = f.copy()
+        csr[self.noi_zero] = 0.0
+        csr[self.noi_diag] = 1.0
+        f[self.noi] = 0.0
+        return csr, f
 
     def _positions(self, rows, cols):
         """compute_csr_stamp_positions (mna_builder.py:126-160)."""
@@ -279,12 +306,16 @@ def nr_solve(sys_: OracleSystem, X_init, vsrc_vals, isrc_vals=None, Q_prev=None,
                                                   Q_prev2, shunt_ref)
         res_tol = np.concatenate([np.maximum(maxc * reltol, floor_), np.full(n_v, vntol)])
         f_check = f if conv_mask is None else np.where(conv_mask, f, 0.0)
+        if sys_.noi.size:  # NOI rows leave the residual test (_build_augmented_conv_mask)
+            f_check = f_check.copy()
+            f_check[sys_.noi] = 0.0
         max_f = float(np.max(np.abs(f_check))) if len(f_check) else 0.0
         residual_converged = bool(np.all(np.abs(f_check) < res_tol))
-        if not (np.all(np.isfinite(csr)) and np.all(np.isfinite(f))):
+        csr, f_solve = sys_.enforce_noi(csr, f)
+        if not (np.all(np.isfinite(csr)) and np.all(np.isfinite(f_solve))):
             it += 1  # the iterate left the finite range: stop, not converged
             break
-        delta = sys_.solve(csr, -f)
+        delta = sys_.solve(csr, -f_solve)
         conv_delta = np.concatenate([delta[:n_unk] * nr_damping, delta[n_unk:]])
         X_ref = X[1:]
         tol = np.maximum(np.abs(X_ref) * reltol, delta_abs_tol)

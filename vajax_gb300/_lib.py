@@ -31,6 +31,9 @@ SIGNATURES = {
     "vgb_circuit_add_group": (C.c_int, [vp, C.c_int, C.c_int, i32p, f64p, C.c_int, i32p, f64p, f64p, C.c_double]),
     "vgb_circuit_set_sources": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, f64p]),
     "vgb_circuit_set_internal_nodes": (C.c_int, [vp, C.c_int, i32p]),
+    "vgb_circuit_set_noi_nodes": (C.c_int, [vp, C.c_int, i32p]),
+    "vgb_set_tuning": (C.c_int, [vp, C.c_int, C.c_int]),
+    "vgb_get_tuning": (C.c_int, [vp, C.c_int, i32p]),
     "vgb_circuit_analyze": (C.c_int, [vp]),
     "vgb_profile": (C.c_int, [vp, C.c_int, f64p]),
     "vgb_solver_order": (C.c_int, [vp, i32p, i32p]),

@@ -124,6 +124,14 @@ class ResolvedGroup:
         return m
 
 
+def is_noi_node(name: str) -> bool:
+    """A device internal node that the Newton update holds fixed: PSP103's
+    noise-correlation node, named ``NOI`` in its Verilog-A source and ``node4``
+    in the reference's collapsed node naming (engine.py:1486-1496,
+    full_mna.py:360-369)."""
+    return name.upper() == "NOI" or name == "node4"
+
+
 @dataclass
 class ResolvedCircuit:
     node_names: Dict[str, int]
@@ -140,6 +148,7 @@ class ResolvedCircuit:
     isources: List[Source]
     internal_nodes: List[int]
     temperature: float
+    noi_nodes: List[int] = field(default_factory=list)
 
     def source_tables(self, current: bool = False):
         srcs = self.isources if current else self.vsources
@@ -205,6 +214,7 @@ class Circuit:
         n_ext = len(names) + 1
         next_node = n_ext
         internal: List[int] = []
+        noi: List[int] = []
         by_model: Dict[str, List[Instance]] = {}
         for inst in self.instances:
             by_model.setdefault(inst.model, []).append(inst)
@@ -220,6 +230,8 @@ class Circuit:
                 for t in range(len(info.terminals), nn):  # internal nodes
                     node_map[t, d] = next_node
                     internal.append(next_node)
+                    if is_noi_node(info.nodes[t]):
+                        noi.append(next_node)
                     next_node += 1
             npar = len(info.user_params)
             vals = np.empty((npar, len(insts)))
@@ -250,4 +262,5 @@ class Circuit:
             isrc_names=[s.name for s in iss],
             isrc_p=np.asarray([node_names[s.p] for s in iss], np.int32),
             isrc_n=np.asarray([node_names[s.n] for s in iss], np.int32),
-            vsources=list(vs), isources=list(iss), internal_nodes=internal, temperature=self.temperature)
+            vsources=list(vs), isources=list(iss), internal_nodes=internal, temperature=self.temperature,
+            noi_nodes=noi)

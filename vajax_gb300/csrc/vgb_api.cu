@@ -103,6 +103,11 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
         assemble(c, X, vs, is, Qp, dQp, Qp2, k, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p,
                  c.d_maxc.p, c.d_fres.p, s);
         launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
+        if (!c.noi_res.empty()) {  // enforce_noi of solver_factories.py:775-782, before the solve
+            launch_noi_enforce(c.d_noi_zero.p, (int)c.noi_zero.size(), c.d_noi_diag.p, c.d_noi_res.p,
+                               (int)c.noi_res.size(), c.d_csr_vals.p, c.d_rhs.p, s);
+            c.launches += 1;
+        }
         if (prof) VGB_CUDA(cudaEventRecord(c.ev[2], s));
         const bool fp32 = c.solver_kind == 1;
         if (c.solver_kind == 2) {
@@ -283,8 +288,71 @@ int vgb_circuit_set_internal_nodes(void* h, int n, const int* node_idx) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
-        VGB_REQUIRE(!c->finalized, "circuit already finalized");
+        VGB_REQUIRE(!c->analyzed, "circuit already analysed");
+        VGB_REQUIRE(n >= 0 && (n == 0 || node_idx), "node_idx is required");
         c->internal_idx.assign(node_idx, node_idx + n);
+    });
+}
+
+int vgb_circuit_set_noi_nodes(void* h, int n, const int* node_idx) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(!c->analyzed, "circuit already analysed");
+        VGB_REQUIRE(n >= 0 && (n == 0 || node_idx), "node_idx is required");
+        c->noi_idx.assign(node_idx, node_idx + n);
+    });
+}
+
+int vgb_set_tuning(void* h, int knob, int value) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        switch (knob) {
+            case VGB_TUNE_FACTOR_CTAS_PER_SM: {
+                VGB_REQUIRE(value >= 1 && value <= 4, "factorisation CTAs per SM must be 1..4");
+                if (value == c->tune_factor_ctas) return;
+                c->tune_factor_ctas = value;
+                SparseLU& L = c->lu;
+                if (!c->analyzed || L.task_type.empty()) return;
+                // the host list schedule simulates one worker per CTA
+                schedule_tasks(L, (c->finalized ? sm_count() : 150) * value);
+                if (c->finalized) {
+                    VGB_CUDA(cudaStreamSynchronize(c->stream));
+                    L.d_task_type.upload(L.task_type);
+                    L.d_task_front.upload(L.task_front);
+                    L.d_task_i.upload(L.task_i);
+                    L.d_task_j.upload(L.task_j);
+                    L.d_task_k.upload(L.task_k);
+                }
+                return;
+            }
+            case VGB_TUNE_SOLVE_CTAS_PER_SM:
+                VGB_REQUIRE(value >= 1 && value <= 8, "tree-solve CTAs per SM must be 1..8");
+                c->tune_solve_ctas = value;
+                return;
+            case VGB_TUNE_EVAL_BLOCK:
+                VGB_REQUIRE(value >= 32 && value <= EVAL_BLOCK_MAX && value % 32 == 0,
+                            "evaluation block must be a multiple of 32 in 32..256");
+                c->tune_eval_block = value;
+                return;
+            default:
+                throw Error(VGB_ERR_INVALID, "unknown tuning knob " + std::to_string(knob));
+        }
+    });
+}
+
+int vgb_get_tuning(void* h, int knob, int* value) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        VGB_REQUIRE(value, "value is required");
+        switch (knob) {
+            case VGB_TUNE_FACTOR_CTAS_PER_SM: *value = c->tune_factor_ctas; return;
+            case VGB_TUNE_SOLVE_CTAS_PER_SM: *value = c->tune_solve_ctas; return;
+            case VGB_TUNE_EVAL_BLOCK: *value = c->tune_eval_block; return;
+            default: throw Error(VGB_ERR_INVALID, "unknown tuning knob " + std::to_string(knob));
+        }
     });
 }
 
@@ -428,6 +496,11 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->d_vsrc_p.upload(c->vsrc_p);
         c->d_vsrc_n.upload(c->vsrc_n);
         c->d_conv_mask.upload(c->conv_mask);
+        if (!c->noi_res.empty()) {
+            c->d_noi_zero.upload(c->noi_zero.empty() ? std::vector<int>{0} : c->noi_zero);
+            c->d_noi_diag.upload(c->noi_diag);
+            c->d_noi_res.upload(c->noi_res);
+        }
         c->d_heavy_csr.upload(c->heavy_csr.empty() ? std::vector<int>{0} : c->heavy_csr);
         c->d_heavy_row.upload(c->heavy_row.empty() ? std::vector<int>{0} : c->heavy_row);
         {

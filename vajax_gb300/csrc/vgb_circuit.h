@@ -139,6 +139,7 @@ struct SparseLU {
     std::vector<int> fr_tile0;                        // first tile of the front in the tile arrays
     long long n_tiles = 0;
     double sched_makespan_ns = 0;                     // simulated factorisation time of the task schedule
+    int sched_slots = 600;                            // workers of the list-schedule simulation
     std::vector<long long> tasm_ptr;                  // per tile: A entries (slot, tile-local position)
     std::vector<int> tasm_e, tasm_pos;
     std::vector<long long> tch_ptr;                   // per tile: child blocks {child, r0, r1, c0, c1}
@@ -192,6 +193,10 @@ struct Circuit {
     std::vector<int> diag_pos;
     std::vector<int> vs_pos[4];      // b_p, b_n, bt_p, bt_n
     std::vector<int> internal_idx;   // circuit indices of internal device nodes (residual mask)
+    std::vector<int> noi_idx;        // circuit indices of NOI nodes (held fixed by the Newton update)
+    // NOI enforcement before each Newton solve: CSR positions set to 0 (NOI rows and
+    // columns off the diagonal), to 1 (NOI diagonals), and the NOI rows of the RHS
+    std::vector<int> noi_zero, noi_diag, noi_res;
 
     // gather lists
     std::vector<int> csr_src_ptr, csr_src;
@@ -200,7 +205,7 @@ struct Circuit {
     std::vector<int> res_src_ptr, res_src, rq_src;
     std::vector<int> nb_ptr, nb_idx;   // node row -> vsource branch incidence (signed index: +k+1 / -(k+1))
     std::vector<int> ni_ptr, ni_idx;   // node row -> isource incidence (signed)
-    std::vector<unsigned char> conv_mask;  // [n_aug] 1 = checked in the residual test
+    std::vector<unsigned char> conv_mask;  // [n_aug] 1 = checked in the residual test, 0 = internal, 2 = NOI
     std::vector<int> heavy_csr, heavy_row; // items whose gather list is longer than HEAVY_LIST
     DevBuf<int> d_heavy_csr, d_heavy_row;
     // chunks of the heavy lists (HEAVY_CHUNK entries each, in list order) and each item's chunk range
@@ -212,6 +217,7 @@ struct Circuit {
     DevBuf<int> d_csr_src_ptr, d_csr_src, d_res_src_ptr, d_res_src, d_rq_src;
     DevBuf<double> d_csr_const;
     DevBuf<unsigned char> d_csr_diag, d_conv_mask;
+    DevBuf<int> d_noi_zero, d_noi_diag, d_noi_res;
     DevBuf<int> d_nb_ptr, d_nb_idx, d_ni_ptr, d_ni_idx, d_vsrc_p, d_vsrc_n;
     DevBuf<int> d_indptr, d_indices;
     DevBuf<double> d_contrib;
@@ -229,6 +235,10 @@ struct Circuit {
     double phase_ms[5] = {0, 0, 0, 0, 0};   // eval, assemble, factor, solve, update
     long long phase_calls = 0;
     long long launches = 0;                  // kernels launched by this handle
+    // launch shapes picked by the autotuner (vgb_set_tuning)
+    int tune_factor_ctas = 4;  // factorisation CTAs per SM (1..4)
+    int tune_solve_ctas = 4;   // tree-solve CTAs per SM (1..8)
+    int tune_eval_block = 64;  // device-evaluation threads per block (32..256)
     DevBuf<double> d_zeros, d_floor;  // defaults for omitted "previous state" vectors
     double floor_value = -1.0;
     bool analyzed = false;            // host-side pattern + symbolic built
@@ -239,5 +249,9 @@ struct Circuit {
 // Host-side construction (vgb_host.cpp)
 void build_pattern(Circuit& c);
 void build_sparse_symbolic(Circuit& c);
+// Streaming multiprocessors of the current device (vgb_frontal.cu).
+int sm_count();
+// Re-order the factorisation task list for `slots` concurrent workers.
+void schedule_tasks(SparseLU& L, int slots);
 
 } // namespace vgb

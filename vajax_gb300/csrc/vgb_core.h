@@ -12,7 +12,7 @@ struct Coeffs {
 inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
     for (auto& g : c.groups)
         if (g.n_dev) {
-            g.me->launch(g.args(c.d_contrib.p), X, c0, s);
+            g.me->launch(g.args(c.d_contrib.p), X, c0, c.tune_eval_block, s);
             c.launches++;
         }
 }

@@ -45,11 +45,13 @@ struct ParamReader {
 };
 
 // Device evaluation is FP64-pipe bound: small blocks spread the instances over
-// every SM instead of packing them onto a few.
+// every SM instead of packing them onto a few.  The block size is a launch
+// parameter (default 64) that the autotuner may change; EVAL_BLOCK_MAX bounds it.
 constexpr int EVAL_BLOCK = 64;
+constexpr int EVAL_BLOCK_MAX = 256;
 
 template <class M>
-__global__ void __launch_bounds__(EVAL_BLOCK) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
+__global__ void __launch_bounds__(EVAL_BLOCK_MAX) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n_dev) return;
@@ -102,15 +104,15 @@ struct ModelEntry {
     int nn, nj, np;
     const int* jrow;
     const int* jcol;
-    void (*launch)(const GroupArgs&, const double* X, double c0, cudaStream_t s);
+    void (*launch)(const GroupArgs&, const double* X, double c0, int block, cudaStream_t s);
     void (*launch_raw)(const GroupArgs&, const double* X, double* out, cudaStream_t s);
 };
 
 template <class M>
-void launch_eval(const GroupArgs& g, const double* X, double c0, cudaStream_t s)
+void launch_eval(const GroupArgs& g, const double* X, double c0, int block, cudaStream_t s)
 {
     if (g.n_dev == 0) return;
-    eval_kernel<M><<<ceil_div(g.n_dev, EVAL_BLOCK), EVAL_BLOCK, 0, s>>>(g, X, c0);
+    eval_kernel<M><<<ceil_div(g.n_dev, block), block, 0, s>>>(g, X, c0);
 }
 
 template <class M>

@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
 // host launchers
 // ---------------------------------------------------------------------------
 
-static int sm_count() {
+int sm_count() {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -849,7 +849,8 @@ static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, L.n_tiles * sizeof(int), s));
     MFArgs a = mf_args(c, A);
     a.epoch = L.epoch;
-    const int blocks = std::min(sm_count() * MF_CTAS_PER_SM, std::max(a.n_tasks, 1));
+    const int blocks = std::min(sm_count() * std::min(std::max(c.tune_factor_ctas, 1), MF_CTAS_PER_SM),
+                                std::max(a.n_tasks, 1));
     mf_factor_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool);
     VGB_CUDA(cudaGetLastError());
 }
@@ -900,7 +901,7 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
         VGB_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         cur = smem;
     }
-    const int blocks = std::min(sm_count() * 4, L.nsn);
+    const int blocks = std::min(sm_count() * std::max(c.tune_solve_ctas, 1), L.nsn);
     a.order = L.d_fwd_order.p;
     a.counter_small = L.d_counters.p + 4;
     mf_fwd_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool, rhsM, y, cv);

@@ -161,6 +161,30 @@ void build_pattern(Circuit& c) {
     c.conv_mask.assign(n_aug, 1);
     for (int idx : c.internal_idx)
         if (idx > 0 && idx - 1 < n_unk) c.conv_mask[idx - 1] = 0;
+    // NOI rows and columns (solver_factories.py:107-135 builds the same position lists)
+    c.noi_zero.clear();
+    c.noi_diag.clear();
+    c.noi_res.clear();
+    {
+        std::vector<char> is_noi(n_aug, 0);
+        for (int idx : c.noi_idx) {
+            VGB_REQUIRE(idx > 0 && idx - 1 < n_unk, "NOI node index out of range");
+            is_noi[idx - 1] = 1;
+        }
+        for (int r = 0; r < n_aug; ++r) {
+            if (is_noi[r]) {
+                c.conv_mask[r] = 2;
+                c.noi_res.push_back(r);
+            }
+            for (int e = c.indptr[r]; e < c.indptr[r + 1]; ++e) {
+                const int col = c.indices[e];
+                if (!is_noi[r] && !is_noi[col]) continue;
+                if (col == r) c.noi_diag.push_back(e);
+                else c.noi_zero.push_back(e);
+            }
+        }
+        VGB_REQUIRE(c.noi_diag.size() == c.noi_res.size(), "NOI node without a diagonal entry");
+    }
 
     // long gather lists (supply rails) are reduced by a block each
     c.heavy_csr.clear();
@@ -250,14 +274,14 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
 
 // Order the factorisation tasks for the persistent kernel, whose CTAs claim
 // tasks in list order and then wait for their inputs.  A list schedule
-// (highest bottom level first, simulated on SCHED_SLOTS workers with rough
+// (highest bottom level first, simulated on `slots` workers, one per CTA, with rough
 // per-task costs) puts each task where it is expected to become ready, so
 // CTAs do not park behind one front's chain of dependent tiles while
 // independent subtrees wait further down the list.  Start order is a
 // topological order, which keeps every wait on an earlier task.
-constexpr int SCHED_SLOTS = 600;
-
-static void schedule_tasks(SparseLU& L) {
+void schedule_tasks(SparseLU& L, int slots) {
+    VGB_REQUIRE(slots >= 1, "schedule needs at least one worker");
+    L.sched_slots = slots;
     const int nt = (int)L.task_type.size();
     if (nt == 0) return;
     const int ns = L.nsn;
@@ -358,7 +382,7 @@ static void schedule_tasks(SparseLU& L) {
         if (npred[t] == 0) ready.push({bl[t], t});
     std::vector<int> order;
     order.reserve(nt);
-    int idle = SCHED_SLOTS;
+    int idle = slots;
     double now = 0.0;
     while ((int)order.size() < nt) {
         while (idle > 0 && !ready.empty()) {
@@ -619,7 +643,7 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
         }
     }
     VGB_REQUIRE(ntile < (1LL << 31) && L.task_type.size() < (1ULL << 31), "too many factorisation tasks");
-    schedule_tasks(L);
+    schedule_tasks(L, L.sched_slots);
     // first-touch assembly of each tile of a large front: its A entries
     // (tile-local position r + c * FRONT_TILE_LD) and the blocks of each
     // child's contribution that land in it, in child order

@@ -71,8 +71,10 @@ __device__ __forceinline__ void finish_row(const AssembleArgs& a, int r, double 
         tol = a.vntol;
     }
     a.f[r] = fn;
-    if (!isfinite(fn)) atomicOr(&a.st->nonfinite, 1);
-    if (a.conv_mask[r]) {
+    // NOI rows (mask 2) are replaced by an identity row before the solve, so their
+    // residual (a 1e40 conductance in PSP103) neither stops nor enters the test
+    if (a.conv_mask[r] != 2 && !isfinite(fn)) atomicOr(&a.st->nonfinite, 1);
+    if (a.conv_mask[r] == 1) {
         double af = fabs(fn);
         if (!(af < tol)) atomicAnd(&a.st->res_ok, 0);
         atomic_max_nonneg(&a.st->max_f, af != af ? INFINITY : af);
@@ -346,6 +348,21 @@ void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp
 // ---------------------------------------------------------------------------
 // small vector kernels
 // ---------------------------------------------------------------------------
+
+// NOI constraint (solver_factories.py:775-782): rows and columns of NOI unknowns
+// zeroed, their diagonal set to 1 and their RHS to 0, so delta[NOI] = 0.
+__global__ void noi_enforce_kernel(const int* zero, int nz, const int* diag, const int* res, int nn, double* csr,
+                                   double* rhs) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nz) csr[zero[t]] = 0.0;
+    else if (t < nz + nn) csr[diag[t - nz]] = 1.0;
+    else if (t < nz + 2 * nn) rhs[res[t - nz - nn]] = 0.0;
+}
+void launch_noi_enforce(const int* zero, int nz, const int* diag, const int* res, int nn, double* csr, double* rhs,
+                        cudaStream_t s) {
+    const int total = nz + 2 * nn;
+    if (total) noi_enforce_kernel<<<ceil_div(total, 256), 256, 0, s>>>(zero, nz, diag, res, nn, csr, rhs);
+}
 
 __global__ void negate_kernel(const double* in, double* out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

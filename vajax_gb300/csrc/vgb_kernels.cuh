@@ -57,6 +57,8 @@ void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp
 
 // misc vector kernels
 void launch_negate(const double* in, double* out, int n, cudaStream_t s);
+void launch_noi_enforce(const int* zero, int nz, const int* diag, const int* res, int nn, double* csr, double* rhs,
+                        cudaStream_t s);
 void launch_vsrc_current(const double* fres, const int* vsrc_p, double* I, int n_vsrc, cudaStream_t s);
 void launch_eval_sources(const Sources& src, int n, double t, double* out, cudaStream_t s);
 // dQdt = c0 Q + c1 Q_prev + d1 dQdt_prev + c2 Q_prev2 (solver_factories.py:715-720)

@@ -56,6 +56,9 @@ class SimulationOptions:
     dc_node_limit_itl: int = 100
     # extension: per-node initial conditions used with icmode='uic'
     ic: Dict[str, float] = field(default_factory=dict)
+    # extension: tune launch shapes and the factorisation schedule on the GPU in
+    # prepare() (vajax_gb300.autotune); "cache" reuses earlier results per pattern
+    autotune: str = "off"  # "off" | "on" | "cache"
 
 
 @dataclass
@@ -169,8 +172,23 @@ class CircuitEngine:
                 prec = 2  # small circuits: dense LU with partial pivoting, as the reference's dense path
             self.device = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 3),
                                         gmin=self.options.gmin)
+            if self.options.autotune != "off":
+                self.tune()
         self._prepared = True
         return self
+
+    def tune(self, reps: int = 3):
+        """Autotune the device circuit's launch shapes at the initial guess
+        (extension; results do not depend on the knobs)."""
+        import torch
+
+        from vajax_gb300.autotune import autotune, default_cache_path
+        X = np.zeros(self.rc.n_nodes + len(self.rc.vsources))
+        X[: self.rc.n_nodes] = self.initial_guess()
+        use_cache = self.options.autotune == "cache"
+        self.tuning = autotune(self.device, torch.as_tensor(X, device="cuda"), self.rc.source_values(0.0),
+                               reps=reps, cache=default_cache_path() if use_cache else None, use_cache=use_cache)
+        return self.tuning
 
     # initial state (full_mna.py:694-745 mid-rail, :874-957 DC / uic)
     def _vdd_value(self) -> float:
@@ -194,6 +212,8 @@ class CircuitEngine:
         for s, p, n in zip(rc.vsources, rc.vsrc_p, rc.vsrc_n):
             if n == 0 and p > 0:
                 V[p] = s.dc_value()
+        for idx in getattr(rc, "noi_nodes", ()):  # NOI nodes start at 0 V (full_mna.py:734-739)
+            V[idx] = 0.0
         return V
 
     def initial_guess(self) -> np.ndarray:

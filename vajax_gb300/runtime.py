@@ -70,6 +70,10 @@ class DeviceCircuit:
             if rc.internal_nodes:
                 inn = np.asarray(rc.internal_nodes, np.int32)
                 self._check(self.lib.vgb_circuit_set_internal_nodes(h, len(inn), _ip(inn)))
+            noi = getattr(rc, "noi_nodes", None)
+            if noi:
+                nn = np.asarray(noi, np.int32)
+                self._check(self.lib.vgb_circuit_set_noi_nodes(h, len(nn), _ip(nn)))
             self._check(self.lib.vgb_circuit_analyze(h))
             if device:
                 self._check(self.lib.vgb_circuit_finalize(h, gmin, precision, refine_sweeps))
@@ -97,6 +101,20 @@ class DeviceCircuit:
         """0: FP64 LU; 1: FP32 LU + FP64-residual refinement."""
         self._check(self.lib.vgb_set_precision(self.h, int(precision), int(refine_sweeps)))
         self.precision = int(precision)
+
+    TUNING_KNOBS = {"factor_ctas_per_sm": 0, "solve_ctas_per_sm": 1, "eval_block": 2}
+
+    def set_tuning(self, knob: str, value: int):
+        """Launch shape or schedule knob (see vgb_set_tuning)."""
+        self._check(self.lib.vgb_set_tuning(self.h, self.TUNING_KNOBS[knob], int(value)))
+
+    def tuning(self) -> Dict[str, int]:
+        out = {}
+        for name, k in self.TUNING_KNOBS.items():
+            v = C.c_int()
+            self._check(self.lib.vgb_get_tuning(self.h, k, C.byref(v)))
+            out[name] = v.value
+        return out
 
     def close(self):
         if self.h is not None:
