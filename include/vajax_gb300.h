@@ -88,7 +88,7 @@ int vgb_circuit_set_noi_nodes(void* h, int n, const int* node_idx);
  * sparse solve is a library call (solver_factories.py:895-922, cuDSS).
  *   VGB_TUNE_FACTOR_CTAS_PER_SM  1..4 persistent factorisation CTAs per SM; the
  *                                task list is re-scheduled for that many workers
- *   VGB_TUNE_SOLVE_CTAS_PER_SM   1..8 tree-solve CTAs per SM
+ *   VGB_TUNE_SOLVE_CTAS_PER_SM   1..4 tree-solve CTAs per SM
  *   VGB_TUNE_EVAL_BLOCK          32..256 (multiple of 32) device-evaluation threads
  *                                per block
  * Defaults: 4, 4, 64.  Not thread-safe against work in flight on other streams. */

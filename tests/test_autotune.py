@@ -27,12 +27,12 @@ def test_coordinate_descent_picks_the_fastest_value_per_phase():
 
     def measure():
         f = {2: 3.0, 3: 2.0, 4: 2.5}[state["factor_ctas_per_sm"]]
-        s = {2: 1.0, 4: 1.0, 8: 0.5}[state["solve_ctas_per_sm"]]
+        s = {1: 1.0, 2: 1.0, 4: 0.5}[state["solve_ctas_per_sm"]]
         e = {32: 0.9, 64: 0.8, 128: 0.7, 256: 0.95}[state["eval_block"]]
         return {"factor_ms": f, "solve_ms": s, "eval_ms": e, "assemble_ms": 0.1}
 
     chosen, timings = coordinate_descent(set_knob, measure, dict(state))
-    assert chosen == {"factor_ctas_per_sm": 3, "solve_ctas_per_sm": 8, "eval_block": 128}
+    assert chosen == {"factor_ctas_per_sm": 3, "solve_ctas_per_sm": 4, "eval_block": 128}
     assert state == chosen
     assert set(timings) == {k[0] for k in KNOBS}
     assert timings["factor_ctas_per_sm"] == {2: 3.0, 3: 2.0, 4: 2.5}

@@ -30,7 +30,7 @@ import numpy as np
 # knob, candidate values, phase of the profile it drives
 KNOBS: Tuple[Tuple[str, Sequence[int], str], ...] = (
     ("factor_ctas_per_sm", (2, 3, 4), "factor_ms"),
-    ("solve_ctas_per_sm", (2, 4, 8), "solve_ms"),
+    ("solve_ctas_per_sm", (1, 2, 4), "solve_ms"),
     ("eval_block", (32, 64, 128, 256), "eval_ms"),
 )
 

@@ -328,7 +328,7 @@ int vgb_set_tuning(void* h, int knob, int value) {
                 return;
             }
             case VGB_TUNE_SOLVE_CTAS_PER_SM:
-                VGB_REQUIRE(value >= 1 && value <= 8, "tree-solve CTAs per SM must be 1..8");
+                VGB_REQUIRE(value >= 1 && value <= 4, "tree-solve CTAs per SM must be 1..4");
                 c->tune_solve_ctas = value;
                 return;
             case VGB_TUNE_EVAL_BLOCK:

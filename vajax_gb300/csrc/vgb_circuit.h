@@ -237,7 +237,7 @@ struct Circuit {
     long long launches = 0;                  // kernels launched by this handle
     // launch shapes picked by the autotuner (vgb_set_tuning)
     int tune_factor_ctas = 4;  // factorisation CTAs per SM (1..4)
-    int tune_solve_ctas = 4;   // tree-solve CTAs per SM (1..8)
+    int tune_solve_ctas = 4;   // tree-solve CTAs per SM (1..4)
     int tune_eval_block = 64;  // device-evaluation threads per block (32..256)
     DevBuf<double> d_zeros, d_floor;  // defaults for omitted "previous state" vectors
     double floor_value = -1.0;

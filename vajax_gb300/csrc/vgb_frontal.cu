@@ -253,50 +253,54 @@ __device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, i
 }
 
 // Pivot of step p (checked, replaced by 1e-30 and flagged when zero) and its
-// reciprocal; called by the warp that owns column p after its last update.
+// reciprocal, in every lane of the warp that owns column p.
 template <typename T>
-__device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T* rinv) {
+__device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T& r) {
     T piv = __shfl_sync(0xffffffffu, col, p);
     if (piv == (T)0 || !isfinite((double)piv)) {
         piv = (T)1e-30;
         if (lane == p) col = piv;
         if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
     }
-    const T r = (T)1 / piv;
-    if (lane == 0) *rinv = r;
+    r = (T)1 / piv;
 }
+
+// The elimination steps below exchange the step's pivot column (or row) through a
+// double-buffered slot of `xch` (step s uses xch[32 (s & 1) ...]), so one block
+// barrier per step suffices: a warp can only overwrite a slot two steps later, after
+// the barrier that every reader of that slot has passed.
 
 // LU without pivoting of the leading n x n block of a tile.  lane = row; warp
 // g owns columns g, g + 4, ... in registers.  The owner of column p + 1
-// updates that column first and forms the next pivot's reciprocal while the
-// other warps finish step p, which keeps the FP64 division off the chain of
-// dependent steps.
+// updates that column first and forms the next pivot's reciprocal (kept in its
+// registers) while the other warps finish step p, which keeps the FP64
+// division off the chain of dependent steps.
 template <typename T>
 __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
-    T* rinv = xch + 32;
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = t[lane + (g + NWARP * q) * LD];
-    if (g == 0 && n > 0) next_pivot<T>(a[0], 0, lane, err, rinv);
-    __syncthreads();
+    T r = (T)0;  // reciprocal of the current pivot, valid in the warp that owns its column
+    if (g == 0 && n > 0) next_pivot<T>(a[0], 0, lane, err, r);
 #pragma unroll
     for (int p = 0; p < FRONT_TILE; ++p) {
         if (p < n) {
+            T* xb = xch + ((p & 1) << 5);
             if (g == (p & (NWARP - 1))) {
                 // owner of column p: multipliers L(:, p) for the other warps
                 const int qp = p / NWARP;
-                if (lane > p) a[qp] *= *rinv;
-                xch[lane] = a[qp];
+                if (lane > p) a[qp] *= r;
+                xb[lane] = a[qp];
             }
             __syncthreads();
-            const T l = xch[lane];
+            const T l = xb[lane];
             const int p1 = p + 1;
             if (p1 < n && g == (p1 & (NWARP - 1))) {
                 const int q1 = p1 / NWARP;
                 const T u = __shfl_sync(0xffffffffu, a[q1], p);
                 if (lane > p) a[q1] -= l * u;
-                next_pivot<T>(a[q1], p1, lane, err, rinv);
+                next_pivot<T>(a[q1], p1, lane, err, r);
             }
 #pragma unroll
             for (int q = 0; q < QPW; ++q) {
@@ -306,7 +310,6 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
                     if (c < n && lane > p) a[q] -= l * u;
                 }
             }
-            __syncthreads();
         }
     }
 #pragma unroll
@@ -319,7 +322,7 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
 template <typename T>
 __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
-    T* dinv = xch + 32;  // reciprocals of the diagonal, formed once in parallel
+    T* dinv = xch + 64;  // reciprocals of the diagonal, formed once in parallel
     if (threadIdx.x < n) dinv[threadIdx.x] = (T)1 / d[threadIdx.x + threadIdx.x * LD];
     T a[QPW];
 #pragma unroll
@@ -328,18 +331,18 @@ __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
 #pragma unroll
     for (int c = 0; c < FRONT_TILE; ++c) {
         if (c < n) {
+            T* xb = xch + ((c & 1) << 5);
             if (g == (c & (NWARP - 1))) {
                 a[c / NWARP] *= dinv[c];
-                xch[lane] = a[c / NWARP];
+                xb[lane] = a[c / NWARP];
             }
             __syncthreads();
-            const T xc = xch[lane];
+            const T xc = xb[lane];
 #pragma unroll
             for (int q = 0; q < QPW; ++q) {
                 const int c2 = g + NWARP * q;
                 if (c2 > c && c2 < n) a[q] -= xc * d[c + c2 * LD];
             }
-            __syncthreads();
         }
     }
 #pragma unroll
@@ -358,15 +361,15 @@ __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch) {
 #pragma unroll
     for (int r = 0; r < FRONT_TILE; ++r) {
         if (r < n) {
-            if (g == (r & (NWARP - 1))) xch[lane] = a[r / NWARP];  // row r is final
+            T* xb = xch + ((r & 1) << 5);
+            if (g == (r & (NWARP - 1))) xb[lane] = a[r / NWARP];  // row r is final
             __syncthreads();
-            const T yr = xch[lane];
+            const T yr = xb[lane];
 #pragma unroll
             for (int q = 0; q < QPW; ++q) {
                 const int r2 = g + NWARP * q;
                 if (r2 > r && r2 < n) a[q] -= d[r2 + r * LD] * yr;
             }
-            __syncthreads();
         }
     }
 #pragma unroll
