@@ -91,10 +91,18 @@ int vgb_circuit_set_noi_nodes(void* h, int n, const int* node_idx);
  *   VGB_TUNE_SOLVE_CTAS_PER_SM   1..4 tree-solve CTAs per SM
  *   VGB_TUNE_EVAL_BLOCK          32..256 (multiple of 32) device-evaluation threads
  *                                per block
- * Defaults: 4, 4, 64.  Not thread-safe against work in flight on other streams. */
+ *   VGB_TUNE_TRAN_GRAPH          1: transient sessions created afterwards run their
+ *                                whole step loop as one CUDA graph (device-side
+ *                                Newton test, BDF2 coefficients, predictor, LTE and
+ *                                step control; no host round-trip per Newton
+ *                                iteration or step); 0: host-driven loop, one status
+ *                                read-back per Newton iteration (per-phase profiling
+ *                                with vgb_profile always uses this loop)
+ * Defaults: 4, 4, 64, 1.  Not thread-safe against work in flight on other streams. */
 #define VGB_TUNE_FACTOR_CTAS_PER_SM 0
 #define VGB_TUNE_SOLVE_CTAS_PER_SM 1
 #define VGB_TUNE_EVAL_BLOCK 2
+#define VGB_TUNE_TRAN_GRAPH 3
 int vgb_set_tuning(void* h, int knob, int value);
 int vgb_get_tuning(void* h, int knob, int* value);
 

@@ -77,11 +77,13 @@ static double bits_to_double(unsigned long long b) {
     return d;
 }
 
-// Newton loop (solver_factories.py:526-725, while_loop mode).
-NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
-                        const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
-                        const NROpts& o, int max_iter, cudaStream_t s) {
-    NRResult r;
+// One Newton iteration on the device (solver_factories.py:230-325): evaluate,
+// assemble, enforce NOI, solve J delta = -f, reduce the convergence tests into
+// c.d_status and apply the update.  The coefficients come from c.d_coeffs.  No
+// host synchronisation: the eager loop below reads the status after it, and the
+// transient graph captures it as the body of a device while-loop.
+void nr_iteration(Circuit& c, double* X, const double* vs, const double* is, const double* Qp, const double* dQp,
+                  const double* Qp2, const double* floor_, const NROpts& o, cudaStream_t s, bool prof) {
     NRUpdateArgs u{};
     u.n_unk = c.n_unk;
     u.n_aug = c.n_aug;
@@ -94,36 +96,46 @@ NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, cons
     u.max_step = o.max_step;
     u.node_limit = o.node_limit;
     u.st = c.d_status.p;
+    if (prof) VGB_CUDA(cudaEventRecord(c.ev[0], s));
+    launch_status_reset(c.d_status.p, s);
+    eval_all(c, X, s);
+    if (prof) VGB_CUDA(cudaEventRecord(c.ev[1], s));
+    assemble(c, X, vs, is, Qp, dQp, Qp2, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p, c.d_maxc.p,
+             c.d_fres.p, s);
+    launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
+    if (!c.noi_res.empty()) {  // enforce_noi of solver_factories.py:775-782, before the solve
+        launch_noi_enforce(c.d_noi_zero.p, (int)c.noi_zero.size(), c.d_noi_diag.p, c.d_noi_res.p,
+                           (int)c.noi_res.size(), c.d_csr_vals.p, c.d_rhs.p, s);
+        c.launches += 1;
+    }
+    if (prof) VGB_CUDA(cudaEventRecord(c.ev[2], s));
+    const bool fp32 = c.solver_kind == 1;
+    if (c.solver_kind == 2) {
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
+        launch_dense_solve(c.n_aug, c.d_indptr.p, c.d_indices.p, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p,
+                           c.d_dense.p, &c.d_status.p->dev_err, s);
+    } else {
+        lu_factor(c, c.d_csr_vals.p, fp32, s);
+        if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
+        lu_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, fp32, c.refine_sweeps, s);
+    }
+    if (prof) VGB_CUDA(cudaEventRecord(c.ev[4], s));
+    launch_nr_reduce(u, s);
+    launch_nr_apply(u, s);
+    if (prof) VGB_CUDA(cudaEventRecord(c.ev[5], s));
+    c.launches += 4 + solve_launches(c);  // status reset, negate, reduce, apply + solver kernels
+}
+
+// Newton loop (solver_factories.py:526-725, while_loop mode), host-driven: one
+// 48-byte status read back per iteration.
+NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
+                        const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
+                        const NROpts& o, int max_iter, cudaStream_t s) {
+    NRResult r;
     const bool prof = c.profile;
+    set_coeffs(c, k, s);
     for (int it = 0; it < max_iter; ++it) {
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[0], s));
-        launch_status_reset(c.d_status.p, s);
-        eval_all(c, X, k.c0, s);
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[1], s));
-        assemble(c, X, vs, is, Qp, dQp, Qp2, k, floor_, o.reltol, o.vntol, c.d_csr_vals.p, c.d_f.p, c.d_Q.p,
-                 c.d_maxc.p, c.d_fres.p, s);
-        launch_negate(c.d_f.p, c.d_rhs.p, c.n_aug, s);
-        if (!c.noi_res.empty()) {  // enforce_noi of solver_factories.py:775-782, before the solve
-            launch_noi_enforce(c.d_noi_zero.p, (int)c.noi_zero.size(), c.d_noi_diag.p, c.d_noi_res.p,
-                               (int)c.noi_res.size(), c.d_csr_vals.p, c.d_rhs.p, s);
-            c.launches += 1;
-        }
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[2], s));
-        const bool fp32 = c.solver_kind == 1;
-        if (c.solver_kind == 2) {
-            if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
-            launch_dense_solve(c.n_aug, c.d_indptr.p, c.d_indices.p, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p,
-                               c.d_dense.p, &c.d_status.p->dev_err, s);
-        } else {
-            lu_factor(c, c.d_csr_vals.p, fp32, s);
-            if (prof) VGB_CUDA(cudaEventRecord(c.ev[3], s));
-            lu_solve(c, c.d_csr_vals.p, c.d_rhs.p, c.d_delta.p, fp32, c.refine_sweeps, s);
-        }
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[4], s));
-        launch_nr_reduce(u, s);
-        launch_nr_apply(u, s);
-        if (prof) VGB_CUDA(cudaEventRecord(c.ev[5], s));
-        c.launches += 4 + solve_launches(c);  // status reset, negate, reduce, apply + solver kernels
+        nr_iteration(c, X, vs, is, Qp, dQp, Qp2, floor_, o, s, prof);
         VGB_CUDA(cudaMemcpyAsync(c.h_status, c.d_status.p, sizeof(NRStatus), cudaMemcpyDeviceToHost, s));
         VGB_CUDA(cudaStreamSynchronize(s));
         if (prof) {
@@ -260,6 +272,7 @@ int vgb_circuit_set_sources(void* h, int is_current, int n, const int* kinds, co
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
+        c->config_epoch++;
         VGB_REQUIRE(n == (is_current ? c->n_isrc : c->n_vsrc), "source count mismatch");
         Sources& s = is_current ? c->isrc_wave : c->vsrc_wave;
         s.kind.assign(kinds, kinds + n);
@@ -308,6 +321,7 @@ int vgb_set_tuning(void* h, int knob, int value) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
         c = as_circuit(h);
+        c->config_epoch++;
         switch (knob) {
             case VGB_TUNE_FACTOR_CTAS_PER_SM: {
                 VGB_REQUIRE(value >= 1 && value <= 4, "factorisation CTAs per SM must be 1..4");
@@ -336,6 +350,10 @@ int vgb_set_tuning(void* h, int knob, int value) {
                             "evaluation block must be a multiple of 32 in 32..256");
                 c->tune_eval_block = value;
                 return;
+            case VGB_TUNE_TRAN_GRAPH:
+                VGB_REQUIRE(value == 0 || value == 1, "transient graph mode must be 0 or 1");
+                c->tran_graph = value;
+                return;
             default:
                 throw Error(VGB_ERR_INVALID, "unknown tuning knob " + std::to_string(knob));
         }
@@ -351,6 +369,7 @@ int vgb_get_tuning(void* h, int knob, int* value) {
             case VGB_TUNE_FACTOR_CTAS_PER_SM: *value = c->tune_factor_ctas; return;
             case VGB_TUNE_SOLVE_CTAS_PER_SM: *value = c->tune_solve_ctas; return;
             case VGB_TUNE_EVAL_BLOCK: *value = c->tune_eval_block; return;
+            case VGB_TUNE_TRAN_GRAPH: *value = c->tran_graph; return;
             default: throw Error(VGB_ERR_INVALID, "unknown tuning knob " + std::to_string(knob));
         }
     });
@@ -435,6 +454,7 @@ int vgb_set_shunt_ref(void* h, const double* ref) {
     return guarded(c, [&] {
         c = as_circuit(h);
         require_final(c);
+        c->config_epoch++;
         c->shunt_ref = ref;
     });
 }
@@ -444,6 +464,7 @@ int vgb_set_precision(void* h, int precision, int refine_sweeps) {
     return guarded(c, [&] {
         c = as_circuit(h);
         require_final(c);
+        c->config_epoch++;
         VGB_REQUIRE(precision >= 0 && precision <= 2,
                     "precision must be 0 (FP64), 1 (FP32+refinement) or 2 (dense FP64, small circuits)");
         VGB_REQUIRE(refine_sweeps >= 0 && refine_sweeps <= 3, "refine_sweeps must be in [0, 3]");
@@ -496,6 +517,7 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
         c->d_vsrc_p.upload(c->vsrc_p);
         c->d_vsrc_n.upload(c->vsrc_n);
         c->d_conv_mask.upload(c->conv_mask);
+        c->d_coeffs.upload(std::vector<double>(8, 0.0));
         if (!c->noi_res.empty()) {
             c->d_noi_zero.upload(c->noi_zero.empty() ? std::vector<int>{0} : c->noi_zero);
             c->d_noi_diag.upload(c->noi_diag);
@@ -681,9 +703,10 @@ int vgb_build_system(void* h, const double* X, const double* vsrc_vals, const do
         k.c2 = coeffs[3];
         k.gshunt = coeffs[4];
         const double* z = dv.zeros;
+        set_coeffs(*c, k, s);
         launch_status_reset(c->d_status.p, s);
         build_system(*c, X, vsrc_vals ? vsrc_vals : z, isrc_vals ? isrc_vals : z, Q_prev ? Q_prev : z,
-                     dQdt_prev ? dQdt_prev : z, Q_prev2 ? Q_prev2 : z, k, dv.floor_abstol, 1e-3, 1e-6,
+                     dQdt_prev ? dQdt_prev : z, Q_prev2 ? Q_prev2 : z, dv.floor_abstol, 1e-3, 1e-6,
                      csr_vals ? csr_vals : c->d_csr_vals.p, f ? f : c->d_f.p, Q ? Q : c->d_Q.p,
                      maxc ? maxc : c->d_maxc.p, fres ? fres : c->d_fres.p, s);
         VGB_CUDA(cudaGetLastError());
@@ -751,13 +774,13 @@ int vgb_nr_solve(void* h, double* X, const double* vsrc_vals, const double* isrc
                              max_iter, s);
         // post-convergence rebuild for Q, I_vsource, max_res_contrib (solver_factories.py:689-713)
         launch_status_reset(c->d_status.p, s);
-        build_system(*c, X, vs, is, Qp, dQp, Qp2, k, dv.floor_abstol, o.reltol, o.vntol, c->d_csr_vals.p,
+        build_system(*c, X, vs, is, Qp, dQp, Qp2, dv.floor_abstol, o.reltol, o.vntol, c->d_csr_vals.p,
                      c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
         if (Q_out) VGB_CUDA(cudaMemcpyAsync(Q_out, c->d_Q.p, c->n_unk * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if (maxc_out)
             VGB_CUDA(cudaMemcpyAsync(maxc_out, c->d_maxc.p, c->n_unk * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if (I_vsrc) launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, I_vsrc, c->n_vsrc, s);
-        if (dQdt_out) launch_dqdt(c->d_Q.p, Qp, dQp, Qp2, k.c0, k.c1, k.d1, k.c2, dQdt_out, c->n_unk, s);
+        if (dQdt_out) launch_dqdt(c->d_Q.p, Qp, dQp, Qp2, c->d_coeffs.p, dQdt_out, c->n_unk, s);
         VGB_CUDA(cudaStreamSynchronize(s));
         if (iterations) *iterations = r.iterations;
         if (converged) *converged = r.converged ? 1 : 0;

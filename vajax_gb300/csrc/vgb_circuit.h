@@ -218,6 +218,7 @@ struct Circuit {
     DevBuf<double> d_csr_const;
     DevBuf<unsigned char> d_csr_diag, d_conv_mask;
     DevBuf<int> d_noi_zero, d_noi_diag, d_noi_res;
+    DevBuf<double> d_coeffs;  // Newton coefficients {c0, c1, d1, c2, gshunt} read by the kernels
     DevBuf<int> d_nb_ptr, d_nb_idx, d_ni_ptr, d_ni_idx, d_vsrc_p, d_vsrc_n;
     DevBuf<int> d_indptr, d_indices;
     DevBuf<double> d_contrib;
@@ -239,6 +240,10 @@ struct Circuit {
     int tune_factor_ctas = 4;  // factorisation CTAs per SM (1..4)
     int tune_solve_ctas = 4;   // tree-solve CTAs per SM (1..4)
     int tune_eval_block = 64;  // device-evaluation threads per block (32..256)
+    int tran_graph = 1;        // transient sessions run as a device graph (1) or a host-driven loop (0)
+    // bumped whenever buffers or launch shapes that a captured transient graph
+    // refers to may have changed (tuning, precision, sources, shunt reference)
+    int config_epoch = 0;
     DevBuf<double> d_zeros, d_floor;  // defaults for omitted "previous state" vectors
     double floor_value = -1.0;
     bool analyzed = false;            // host-side pattern + symbolic built
@@ -251,6 +256,8 @@ void build_pattern(Circuit& c);
 void build_sparse_symbolic(Circuit& c);
 // Streaming multiprocessors of the current device (vgb_frontal.cu).
 int sm_count();
+// Host-side set-up of the factor/solve launches, done before a stream capture.
+void mf_prepare_capture(Circuit& c);
 // Re-order the factorisation task list for `slots` concurrent workers.
 void schedule_tasks(SparseLU& L, int slots);
 

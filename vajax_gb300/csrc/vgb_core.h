@@ -9,10 +9,17 @@ struct Coeffs {
     double c0 = 0, c1 = 0, d1 = 0, c2 = 0, gshunt = 0;
 };
 
-inline void eval_all(Circuit& c, const double* X, double c0, cudaStream_t s) {
+// Newton coefficients into device memory (every kernel below reads them there).
+inline void set_coeffs(Circuit& c, const Coeffs& k, cudaStream_t s) {
+    launch_set_coeffs(c.d_coeffs.p, k.c0, k.c1, k.d1, k.c2, k.gshunt, s);
+    c.launches++;
+}
+
+// Device evaluation of every group with the coefficients in c.d_coeffs.
+inline void eval_all(Circuit& c, const double* X, cudaStream_t s) {
     for (auto& g : c.groups)
         if (g.n_dev) {
-            g.me->launch(g.args(c.d_contrib.p), X, c0, c.tune_eval_block, s);
+            g.me->launch(g.args(c.d_contrib.p), X, c.d_coeffs.p, c.tune_eval_block, s);
             c.launches++;
         }
 }
@@ -28,23 +35,22 @@ inline long long solve_launches(const Circuit& c) {
 }
 
 inline void assemble(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
-                     const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
-                     double reltol, double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
-                     cudaStream_t s);
+                     const double* dQp, const double* Qp2, const double* res_tol_floor, double reltol, double vntol,
+                     double* csr, double* f, double* Q, double* maxc, double* fres, cudaStream_t s);
 
-// build_system: eval + assemble (+ residual check into d_status)
+// build_system: eval + assemble (+ residual check into d_status), with the
+// Newton coefficients already in c.d_coeffs (set_coeffs)
 inline void build_system(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
-                         const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
-                         double reltol, double vntol, double* csr, double* f, double* Q, double* maxc,
-                         double* fres, cudaStream_t s) {
-    eval_all(c, X, k.c0, s);
-    assemble(c, X, vs, is, Qp, dQp, Qp2, k, res_tol_floor, reltol, vntol, csr, f, Q, maxc, fres, s);
+                         const double* dQp, const double* Qp2, const double* res_tol_floor, double reltol,
+                         double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
+                         cudaStream_t s) {
+    eval_all(c, X, s);
+    assemble(c, X, vs, is, Qp, dQp, Qp2, res_tol_floor, reltol, vntol, csr, f, Q, maxc, fres, s);
 }
 
 inline void assemble(Circuit& c, const double* X, const double* vs, const double* is, const double* Qp,
-                     const double* dQp, const double* Qp2, const Coeffs& k, const double* res_tol_floor,
-                     double reltol, double vntol, double* csr, double* f, double* Q, double* maxc, double* fres,
-                     cudaStream_t s) {
+                     const double* dQp, const double* Qp2, const double* res_tol_floor, double reltol, double vntol,
+                     double* csr, double* f, double* Q, double* maxc, double* fres, cudaStream_t s) {
     c.launches += 1 + ((c.heavy_csr.size() + c.heavy_row.size()) ? 2 : 0);
     AssembleArgs a{};
     a.nnz = c.nnz;
@@ -71,12 +77,8 @@ inline void assemble(Circuit& c, const double* X, const double* vs, const double
     a.Q_prev = Qp;
     a.dQdt_prev = dQp;
     a.Q_prev2 = Qp2;
-    a.c0 = k.c0;
-    a.c1 = k.c1;
-    a.d1 = k.d1;
-    a.c2 = k.c2;
-    a.gdiag = c.gmin + k.gshunt;
-    a.gshunt = k.gshunt;
+    a.k = c.d_coeffs.p;
+    a.gmin = c.gmin;
     a.shunt_ref = c.shunt_ref;
     a.res_tol_floor = res_tol_floor;
     a.reltol = reltol;
@@ -129,6 +131,8 @@ struct DefaultVecs {
     const double* floor_abstol;   // [n_unk] residual tolerance floor = abstol
 };
 
+void nr_iteration(Circuit& c, double* X, const double* vs, const double* is, const double* Qp, const double* dQp,
+                  const double* Qp2, const double* floor_, const NROpts& o, cudaStream_t s, bool prof);
 NRResult nr_loop(Circuit& c, double* X, const double* vs, const double* is, const double* Qp,
                  const double* dQp, const double* Qp2, const double* floor_, const Coeffs& k,
                  const NROpts& o, int max_iter, cudaStream_t s);

@@ -51,10 +51,12 @@ constexpr int EVAL_BLOCK = 64;
 constexpr int EVAL_BLOCK_MAX = 256;
 
 template <class M>
-__global__ void __launch_bounds__(EVAL_BLOCK_MAX) eval_kernel(GroupArgs g, const double* __restrict__ X, double c0)
+__global__ void __launch_bounds__(EVAL_BLOCK_MAX) eval_kernel(GroupArgs g, const double* __restrict__ X,
+                                                              const double* __restrict__ kdev)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n_dev) return;
+    const double c0 = __ldg(kdev);  // Newton coefficient c0, in device memory
     const double* Xr = X;
     if (g.batch_stride_x) Xr = X + (long long)(i / g.inst_per_replica) * g.batch_stride_x;
     double V[M::NN];
@@ -104,15 +106,15 @@ struct ModelEntry {
     int nn, nj, np;
     const int* jrow;
     const int* jcol;
-    void (*launch)(const GroupArgs&, const double* X, double c0, int block, cudaStream_t s);
+    void (*launch)(const GroupArgs&, const double* X, const double* kdev, int block, cudaStream_t s);
     void (*launch_raw)(const GroupArgs&, const double* X, double* out, cudaStream_t s);
 };
 
 template <class M>
-void launch_eval(const GroupArgs& g, const double* X, double c0, int block, cudaStream_t s)
+void launch_eval(const GroupArgs& g, const double* X, const double* kdev, int block, cudaStream_t s)
 {
     if (g.n_dev == 0) return;
-    eval_kernel<M><<<ceil_div(g.n_dev, block), block, 0, s>>>(g, X, c0);
+    eval_kernel<M><<<ceil_div(g.n_dev, block), block, 0, s>>>(g, X, kdev);
 }
 
 template <class M>

@@ -846,12 +846,14 @@ template <typename T>
 static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     SparseLU& L = c.lu;
     const int smem = MF_SMEM_ELEMS * (int)sizeof(T);
-    L.epoch++;
+    // flags start at 0 and a finished front is marked 1 (a fixed epoch): every launch
+    // resets them, so the launch replays unchanged inside a captured graph
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
+    VGB_CUDA(cudaMemsetAsync(L.d_mf_flags.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_count.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
     if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, L.n_tiles * sizeof(int), s));
     MFArgs a = mf_args(c, A);
-    a.epoch = L.epoch;
+    a.epoch = 1;
     const int blocks = std::min(sm_count() * std::min(std::max(c.tune_factor_ctas, 1), MF_CTAS_PER_SM),
                                 std::max(a.n_tasks, 1));
     mf_factor_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool);
@@ -864,14 +866,41 @@ void mf_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
     else mf_factor_t<double>(c, A, c.lu.d_pool64.p, s);
 }
 
+// bwd: z and x_tail (m) plus the partial sums of U12 x_tail (at most max(4 w, 128) <= 4 m + 128)
+template <typename T>
+static size_t mf_solve_smem(const SparseLU& L) {
+    return (size_t)(5 * std::max<long long>(L.mf_max_m, 1) + MF_THREADS) * sizeof(T);
+}
+
+// Opt the solve kernels in to more than 48 KB of dynamic shared memory (once per size).
+template <typename T>
+static void mf_solve_attributes(size_t smem) {
+    static size_t smem_set[2] = {0, 0};
+    size_t& cur = smem_set[sizeof(T) == 4 ? 0 : 1];
+    if (smem > 48 * 1024 && smem > cur) {
+        VGB_REQUIRE(smem <= 200 * 1024, "front too large for the solve kernels' shared memory");
+        VGB_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        VGB_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cur = smem;
+    }
+}
+
+// Everything the solve launches need set up outside a stream capture.
+void mf_prepare_capture(Circuit& c) {
+    (void)sm_count();
+    if (c.lu.nsn == 0) return;
+    mf_solve_attributes<double>(mf_solve_smem<double>(c.lu));
+    mf_solve_attributes<float>(mf_solve_smem<float>(c.lu));
+}
+
 template <typename T>
 void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream_t s) {
     SparseLU& L = c.lu;
     if (L.nsn == 0) return;
     const T* pool = std::is_same<T, float>::value ? (const T*)L.d_pool32.p : (const T*)L.d_pool64.p;
     T* cv = std::is_same<T, float>::value ? (T*)L.d_cv32.p : (T*)L.d_cv64.p;
-    L.epoch++;
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(int), s));
+    VGB_CUDA(cudaMemsetAsync(L.d_mf_flags.p + 2 * (size_t)L.nsn, 0, 2 * (size_t)L.nsn * sizeof(int), s));
     MFSolveArgs a{};
     a.ns = L.nsn;
     a.fr_ptr = L.d_fr_ptr.p;
@@ -892,18 +921,10 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.counter = L.d_counters.p + 1;
     a.abort_flag = L.d_counters.p + 3;
     a.err = &c.d_status.p->dev_err;
-    a.epoch = L.epoch;
+    a.epoch = 1;
     a.spin_limit = 1u << 22;
-    // bwd: z and x_tail (m) plus the partial sums of U12 x_tail (at most max(4 w, 128) <= 4 m + 128)
-    const size_t smem = (size_t)(5 * std::max<long long>(L.mf_max_m, 1) + MF_THREADS) * sizeof(T);
-    static size_t smem_set[2] = {0, 0};
-    size_t& cur = smem_set[sizeof(T) == 4 ? 0 : 1];
-    if (smem > 48 * 1024 && smem > cur) {
-        VGB_REQUIRE(smem <= 200 * 1024, "front too large for the solve kernels' shared memory");
-        VGB_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        VGB_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        cur = smem;
-    }
+    const size_t smem = mf_solve_smem<T>(L);
+    mf_solve_attributes<T>(smem);
     const int blocks = std::min(sm_count() * std::max(c.tune_solve_ctas, 1), L.nsn);
     a.order = L.d_fwd_order.p;
     a.counter_small = L.d_counters.p + 4;

@@ -59,9 +59,9 @@ __device__ __forceinline__ void finish_row(const AssembleArgs& a, int r, double 
             int k = a.nb_idx[e];
             fr += k > 0 ? a.X[a.n_nodes + k - 1] : -a.X[a.n_nodes - k - 1];
         }
-        fn = fr + a.c0 * q + a.c1 * a.Q_prev[r] + a.d1 * a.dQdt_prev[r] + a.c2 * a.Q_prev2[r] +
-             a.gdiag * a.X[r + 1];
-        if (a.shunt_ref) fn -= a.gshunt * a.shunt_ref[r];
+        const double c0 = a.k[0], c1 = a.k[1], d1 = a.k[2], c2 = a.k[3], gshunt = a.k[4];
+        fn = fr + c0 * q + c1 * a.Q_prev[r] + d1 * a.dQdt_prev[r] + c2 * a.Q_prev2[r] + (a.gmin + gshunt) * a.X[r + 1];
+        if (a.shunt_ref) fn -= gshunt * a.shunt_ref[r];
         a.Q[r] = q;
         a.maxc[r] = mc;
         tol = fmax(mc * a.reltol, a.res_tol_floor[r]);
@@ -92,7 +92,7 @@ __global__ void assemble_kernel(AssembleArgs a) {
         if (e1 - e0 > HEAVY_LIST) return;
         double s = 0.0;
         for (int e = e0; e < e1; ++e) s += a.contrib[a.csr_src[e]];
-        if (a.csr_diag[t]) s += a.gdiag;
+        if (a.csr_diag[t]) s += a.gmin + a.k[4];
         s += a.csr_const[t];
         a.csr_vals[t] = s;
         return;
@@ -163,7 +163,7 @@ __global__ void assemble_heavy_finish_kernel(AssembleArgs a) {
     }
     if (it < a.n_heavy_csr) {
         const int item = a.heavy_csr[it];
-        if (a.csr_diag[item]) s += a.gdiag;
+        if (a.csr_diag[item]) s += a.gmin + a.k[4];
         s += a.csr_const[item];
         a.csr_vals[item] = s;
     } else {
@@ -349,6 +349,20 @@ void lu_solve(Circuit& c, const double* A, const double* rhs, double* x, bool fp
 // small vector kernels
 // ---------------------------------------------------------------------------
 
+// Newton coefficients {c0, c1, d1, c2, gshunt} in device memory, where the
+// evaluation, assembly and dQ/dt kernels read them (a captured graph replays
+// kernels with frozen arguments, so values that change per step live here).
+__global__ void set_coeffs_kernel(double* k, double c0, double c1, double d1, double c2, double gshunt) {
+    k[0] = c0;
+    k[1] = c1;
+    k[2] = d1;
+    k[3] = c2;
+    k[4] = gshunt;
+}
+void launch_set_coeffs(double* kdev, double c0, double c1, double d1, double c2, double gshunt, cudaStream_t s) {
+    set_coeffs_kernel<<<1, 1, 0, s>>>(kdev, c0, c1, d1, c2, gshunt);
+}
+
 // NOI constraint (solver_factories.py:775-782): rows and columns of NOI unknowns
 // zeroed, their diagonal set to 1 and their RHS to 0, so delta[NOI] = 0.
 __global__ void noi_enforce_kernel(const int* zero, int nz, const int* diag, const int* res, int nn, double* csr,
@@ -420,14 +434,19 @@ __device__ double eval_source(int kind, const double* p, int cnt, double t) {
     return 0.0;
 }
 
+// t_dev (device memory) replaces t when given: the transient graph computes the time on the device
 __global__ void eval_sources_kernel(const int* kind, const int* off, const int* cnt, const double* data,
-                                    int n, double t, double* out) {
+                                    int n, double t, const double* t_dev, double* out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) out[k] = eval_source(kind[k], data + off[k], cnt[k], t);
+    if (k < n) out[k] = eval_source(kind[k], data + off[k], cnt[k], t_dev ? *t_dev : t);
 }
 void launch_eval_sources(const Sources& src, int n, double t, double* out, cudaStream_t s) {
     if (n) eval_sources_kernel<<<ceil_div(n, 128), 128, 0, s>>>(src.d_kind.p, src.d_off.p, src.d_cnt.p,
-                                                                src.d_data.p, n, t, out);
+                                                                src.d_data.p, n, t, nullptr, out);
+}
+void launch_eval_sources_dev(const Sources& src, int n, const double* t_dev, double* out, cudaStream_t s) {
+    if (n) eval_sources_kernel<<<ceil_div(n, 128), 128, 0, s>>>(src.d_kind.p, src.d_off.p, src.d_cnt.p,
+                                                                src.d_data.p, n, 0.0, t_dev, out);
 }
 
 } // namespace vgb

@@ -15,8 +15,8 @@ struct AssembleArgs {
     const double* X;
     const double* vsrc_vals; const double* isrc_vals;
     const double* Q_prev; const double* dQdt_prev; const double* Q_prev2;
-    double c0, c1, d1, c2, gdiag;
-    double gshunt; const double* shunt_ref;  // gshunt pulls node r towards shunt_ref[r] (NULL: ground)
+    const double* k;   // device Newton coefficients {c0, c1, d1, c2, gshunt}
+    double gmin; const double* shunt_ref;  // gshunt pulls node r towards shunt_ref[r] (NULL: ground)
     const double* res_tol_floor; double reltol, vntol;
     const unsigned char* conv_mask;
     double* csr_vals; double* f; double* Q; double* maxc; double* fres;
@@ -61,8 +61,10 @@ void launch_noi_enforce(const int* zero, int nz, const int* diag, const int* res
                         cudaStream_t s);
 void launch_vsrc_current(const double* fres, const int* vsrc_p, double* I, int n_vsrc, cudaStream_t s);
 void launch_eval_sources(const Sources& src, int n, double t, double* out, cudaStream_t s);
+void launch_eval_sources_dev(const Sources& src, int n, const double* t_dev, double* out, cudaStream_t s);
 // dQdt = c0 Q + c1 Q_prev + d1 dQdt_prev + c2 Q_prev2 (solver_factories.py:715-720)
-void launch_dqdt(const double* Q, const double* Qp, const double* dQp, const double* Qp2, double c0, double c1,
-                 double d1, double c2, double* out, int n, cudaStream_t s);
+void launch_set_coeffs(double* kdev, double c0, double c1, double d1, double c2, double gshunt, cudaStream_t s);
+void launch_dqdt(const double* Q, const double* Qp, const double* dQp, const double* Qp2, const double* kdev,
+                 double* out, int n, cudaStream_t s);
 
 } // namespace vgb

@@ -20,15 +20,15 @@ namespace vgb {
 // kernels
 // ---------------------------------------------------------------------------
 
-__global__ void dqdt_kernel(const double* Q, const double* Qp, const double* dQp, const double* Qp2, double c0,
-                            double c1, double d1, double c2, double* out, int n) {
+__global__ void dqdt_kernel(const double* Q, const double* Qp, const double* dQp, const double* Qp2,
+                            const double* k, double* out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = c0 * Q[i] + c1 * Qp[i] + d1 * dQp[i] + c2 * Qp2[i];
+    if (i < n) out[i] = k[0] * Q[i] + k[1] * Qp[i] + k[2] * dQp[i] + k[3] * Qp2[i];
 }
 
-void launch_dqdt(const double* Q, const double* Qp, const double* dQp, const double* Qp2, double c0, double c1,
-                 double d1, double c2, double* out, int n, cudaStream_t s) {
-    if (n) dqdt_kernel<<<ceil_div(n, 256), 256, 0, s>>>(Q, Qp, dQp, Qp2, c0, c1, d1, c2, out, n);
+void launch_dqdt(const double* Q, const double* Qp, const double* dQp, const double* Qp2, const double* kdev,
+                 double* out, int n, cudaStream_t s) {
+    if (n) dqdt_kernel<<<ceil_div(n, 256), 256, 0, s>>>(Q, Qp, dQp, Qp2, kdev, out, n);
 }
 
 // X_init (predictor, full_mna.py:1897-1911) and the historic NR tolerance
@@ -107,9 +107,10 @@ struct Pred {
     double err;
 };
 
-static Pred predictor_coeffs(const double dt_hist[4], int history_count, double new_dt, int max_order) {
-    int order = std::min(history_count - 1, max_order);
-    order = std::max(order, 0);
+__host__ __device__ inline Pred predictor_coeffs(const double dt_hist[4], int history_count, double new_dt,
+                                                 int max_order) {
+    int order = history_count - 1 < max_order ? history_count - 1 : max_order;
+    order = order > 0 ? order : 0;
     const double cum0 = 0.0, cum1 = dt_hist[0];
     (void)cum0;
     const double tau1 = -(new_dt + cum1) / new_dt;
@@ -119,7 +120,7 @@ static Pred predictor_coeffs(const double dt_hist[4], int history_count, double 
         p.a[0] = 1.0; p.a[1] = 0.0; p.a[2] = 0.0;
         p.err = 1.0;
     } else if (order == 1) {
-        const double r1 = new_dt / std::max(dt_hist[0], 1e-30);
+        const double r1 = new_dt / fmax(dt_hist[0], 1e-30);
         p.a[0] = 1.0 + r1; p.a[1] = -r1; p.a[2] = 0.0;
         p.err = -r1 * (1 + r1) / 2;
     } else {
@@ -127,15 +128,264 @@ static Pred predictor_coeffs(const double dt_hist[4], int history_count, double 
         double d0 = (tau0 - tau1) * (tau0 - tau2);
         double d1 = (tau1 - tau0) * (tau1 - tau2);
         double d2 = (tau2 - tau0) * (tau2 - tau1);
-        if (std::fabs(d0) < 1e-30) d0 = 1e-30;
-        if (std::fabs(d1) < 1e-30) d1 = 1e-30;
-        if (std::fabs(d2) < 1e-30) d2 = 1e-30;
+        if (fabs(d0) < 1e-30) d0 = 1e-30;
+        if (fabs(d1) < 1e-30) d1 = 1e-30;
+        if (fabs(d2) < 1e-30) d2 = 1e-30;
         p.a[0] = (0 - tau1) * (0 - tau2) / d0;
         p.a[1] = (0 - tau0) * (0 - tau2) / d1;
         p.a[2] = (0 - tau0) * (0 - tau1) / d2;
         p.err = -tau0 * tau1 * tau2 / 6;
     }
     return p;
+}
+
+
+// ---------------------------------------------------------------------------
+// Device-resident step loop (the transient graph).  The controller state of a
+// session lives in device memory; single-thread kernels do what the host loop
+// below does between launches: the step's integration and predictor
+// coefficients, the Newton convergence decision, the LTE step control
+// (full_mna.py:1851-2147, adaptive.py:94-339) and the commit parameters.  The
+// whole loop is one CUDA graph: an outer while-node over steps whose body holds
+// an inner while-node over Newton iterations.  Both loops are bounded on the
+// device (tran_itl iterations; guard_cap step attempts), whatever the inputs.
+// ---------------------------------------------------------------------------
+
+struct TranDev {
+    // configuration
+    double t_stop, max_dt, min_dt, lte_ratio, redo_factor, grow_factor, tran_ft, gshunt_init, gshunt_target;
+    int gshunt_steps, warmup_steps, max_consec, method, max_steps, tran_itl, fixed, fixed_n;
+    // controller state
+    double t, dt, dt_hist[4];
+    int head, history_count, warmup_count, consecutive, step_idx, fixed_i;
+    // the step in progress
+    double t_next, kl, pa[3];
+    int can_predict, slot0, slot1, slot2;
+    int nr_it, nr_conv;
+    // commit of the step, decided by the step-end kernel
+    int use_new, accept, zero_current, commit_row, commit_slot;
+    // statistics and loop control
+    long long total_nr;
+    int rejected, nr_fail_count, accepted_now, limit, guard, guard_cap, done, stop_reason;
+    double min_dt_used, max_dt_used;
+};
+
+enum { TRAN_STOP_NONE = 0, TRAN_STOP_TIMEOUT = 1, TRAN_STOP_GUARD = 2 };
+
+// Integration coefficients of the step (k = {c0, c1, d1, c2, gshunt}), predictor
+// weights and history slots; arms the Newton loop.
+__global__ void tran_step_begin_kernel(TranDev* T, double* k, cudaGraphConditionalHandle h_nr) {
+    const double dt_cur = T->dt;
+    const double inv = 1.0 / dt_cur;
+    double c0 = inv, c1 = -inv, d1 = 0.0, c2 = 0.0, gshunt = 0.0;
+    if (T->fixed) {
+        // constant-step coefficients (full_mna.py:1236-1253)
+        if (T->method == 1) { c0 = 2 * inv; c1 = -2 * inv; d1 = -1.0; }
+        else if (T->method == 2) { c0 = 1.5 * inv; c1 = -2.0 * inv; c2 = 0.5 * inv; }
+        T->t_next = ((double)T->fixed_i + 1.0) * dt_cur;
+    } else {
+        double err_integ;
+        if (T->method == 0) { err_integ = -0.5; }
+        else if (T->method == 1) { c0 = 2 * inv; c1 = -2 * inv; d1 = -1.0; err_integ = 1.0 / 24.0; }
+        else {
+            const double dt_prev = T->dt_hist[0];
+            const double w = dt_prev > 0 ? dt_cur / dt_prev : 1.0;
+            const double wp1 = 1.0 + w;
+            c0 = (1.0 + 2.0 * w) / (wp1 * dt_cur);
+            c1 = -wp1 / dt_cur;
+            c2 = (w * w) / (wp1 * dt_cur);
+            err_integ = -2.0 / 9.0;
+        }
+        T->t_next = T->t + dt_cur;
+        T->can_predict = (T->warmup_count >= T->warmup_steps && T->history_count >= 2) ? 1 : 0;
+        const Pred pr = predictor_coeffs(T->dt_hist, T->history_count, dt_cur, 2);
+        int order = T->history_count - 1 < 2 ? T->history_count - 1 : 2;
+        order = order > 0 ? order : 0;
+        T->pa[0] = pr.a[0];
+        T->pa[1] = order >= 1 ? pr.a[1] : 0.0;
+        T->pa[2] = order >= 2 ? pr.a[2] : 0.0;
+        T->slot0 = (T->head + 0) % 4;
+        T->slot1 = (T->head + 1) % 4;
+        T->slot2 = (T->head + 2) % 4;
+        const double ramp =
+            T->gshunt_steps > 0 ? fmin(fmax((double)T->step_idx / T->gshunt_steps, 0.0), 1.0) : 1.0;
+        gshunt = T->gshunt_init + ramp * (T->gshunt_target - T->gshunt_init);
+        T->kl = err_integ / (err_integ - pr.err);
+    }
+    k[0] = c0;
+    k[1] = c1;
+    k[2] = d1;
+    k[3] = c2;
+    k[4] = gshunt;
+    T->nr_it = 0;
+    T->nr_conv = 0;
+    cudaGraphSetConditional(h_nr, 1u);
+}
+
+// X_init from the predictor (adaptive), as predict_kernel with the device coefficients
+__global__ void tran_predict_kernel(int n_nodes, int n_x, int n_unk, const double* X, double* Xc, double* Vpred,
+                                    const double* hist, const TranDev* T, const double* hist_maxc, double reltol,
+                                    double abstol, double* floor_) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_nodes) {
+        const double vp = T->pa[0] * hist[(size_t)T->slot0 * n_nodes + i] +
+                          T->pa[1] * hist[(size_t)T->slot1 * n_nodes + i] +
+                          T->pa[2] * hist[(size_t)T->slot2 * n_nodes + i];
+        Vpred[i] = vp;
+        Xc[i] = T->can_predict ? vp : X[i];
+    } else if (i < n_x) {
+        Xc[i] = X[i];
+    }
+    if (i < n_unk) floor_[i] = hist_maxc ? fmax(hist_maxc[i] * reltol, abstol) : abstol;
+}
+
+__global__ void tran_copy_kernel(int n, const double* src, double* dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+// Newton convergence decision after one iteration (the host loop's test in nr_loop)
+__global__ void tran_nr_decide_kernel(TranDev* T, const NRStatus* S, cudaGraphConditionalHandle h_nr) {
+    const int i = T->nr_it;
+    bool stop = false;
+    if (S->dev_err & DEV_ERR_TIMEOUT) {
+        T->stop_reason = TRAN_STOP_TIMEOUT;
+        stop = true;
+    } else if (S->nonfinite) {
+        stop = true;  // the residual left the finite range: not converged
+    } else if (S->res_ok && (i == 0 || S->delta_ok)) {
+        T->nr_conv = 1;
+        stop = true;
+    }
+    T->nr_it = i + 1;
+    if (T->nr_it >= T->tran_itl) stop = true;
+    cudaGraphSetConditional(h_nr, stop ? 0u : 1u);
+}
+
+// LTE norm with the coefficient from the controller
+__global__ void tran_lte_kernel(int n_nodes, const double* Vnew, const double* Vpred, const double* Vmax,
+                                const TranDev* T, double reltol, double abstol, NRStatus* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double k = T->kl;
+    double v = 0.0;
+    if (i < n_nodes) {
+        const double lte = (Vnew[i] - Vpred[i]) * k;
+        const double vcur = fmax(fabs(Vnew[i]), fabs(Vpred[i]));
+        const double vs = fmax(Vmax[i], vcur);
+        const double tol = reltol * vs + abstol;
+        v = fabs(lte) / tol;
+        if (v != v) v = INFINITY;
+    }
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && i < n_nodes + 32)
+        atomicMax(&st->lte_norm, (unsigned long long)__double_as_longlong(v));
+}
+
+// Accept / reject and the next step size (the host loop's controller), then the
+// loop condition of the step graph.
+__global__ void tran_step_end_kernel(TranDev* T, const NRStatus* S, double* tdev, cudaGraphConditionalHandle h_out) {
+    T->total_nr += T->nr_it;
+    const bool nr_failed = !T->nr_conv;
+    if (nr_failed) T->nr_fail_count++;
+    if (T->fixed) {
+        const int i = T->fixed_i;
+        T->use_new = 1;
+        T->accept = 1;
+        T->zero_current = 0;
+        T->commit_row = i + 1;
+        T->commit_slot = (i + 1) % 4;
+        tdev[i + 1] = T->t_next;
+        T->fixed_i = i + 1;
+        T->step_idx = i + 2;
+        T->accepted_now++;
+        if (T->fixed_i >= T->fixed_n) T->done = 1;
+    } else {
+        const double dt_cur = T->dt;
+        const double lte_norm = __longlong_as_double((long long)S->lte_norm);
+        const int lte_order = T->history_count - 1 < 2 ? T->history_count - 1 : 2;
+        double factor = pow(T->lte_ratio / fmax(lte_norm, 1e-10), 1.0 / (lte_order + 1));
+        factor = fmin(fmax(factor, 0.1), T->grow_factor);
+        const double dt_lte = dt_cur * factor;
+        const bool at_min_dt = dt_cur <= T->min_dt;
+        const bool nr_failed_at_min = nr_failed && at_min_dt;
+        const bool lte_reject = (dt_cur / dt_lte > T->redo_factor) && T->can_predict && !nr_failed;
+        const bool nr_reject = nr_failed && !at_min_dt;
+        const bool force_accept = T->consecutive >= T->max_consec;
+        const bool reject = (lte_reject || nr_reject) && !force_accept;
+        const bool accept = !reject;
+        T->consecutive = accept ? 0 : (lte_reject ? T->consecutive + 1 : T->consecutive);
+        const double dt_from_lte = T->can_predict ? dt_lte : dt_cur;
+        const double dt_nr_halved = fmax(dt_cur * T->tran_ft, T->min_dt);
+        const double last_good = T->history_count > 0 ? T->dt_hist[0] : T->min_dt * 16.0;
+        const double dt_recovery = fmax(last_good / 8.0, T->min_dt * 2.0);
+        double new_dt = nr_failed ? (at_min_dt ? dt_recovery : dt_nr_halved) : dt_from_lte;
+        new_dt = fmin(fmax(new_dt, T->min_dt), T->max_dt);
+        new_dt = fmin(new_dt, T->t_stop - T->t_next);
+        const bool use_new = accept && !nr_failed_at_min;
+        const int new_head = use_new ? (T->head + 3) % 4 : T->head;
+        T->use_new = use_new ? 1 : 0;
+        T->accept = accept ? 1 : 0;
+        T->zero_current = nr_failed_at_min ? 1 : 0;
+        T->commit_row = T->step_idx;
+        T->commit_slot = new_head;
+        if (use_new) {
+            T->head = new_head;
+            for (int q = 3; q > 0; --q) T->dt_hist[q] = T->dt_hist[q - 1];
+            T->dt_hist[0] = dt_cur;
+            T->history_count = T->history_count + 1 < 4 ? T->history_count + 1 : 4;
+            T->warmup_count++;
+        }
+        if (accept) {
+            tdev[T->step_idx] = T->t_next;
+            T->t = T->t_next;
+            T->step_idx++;
+            T->accepted_now++;
+            T->min_dt_used = fmin(T->min_dt_used, dt_cur);
+            T->max_dt_used = fmax(T->max_dt_used, dt_cur);
+        }
+        if (reject) T->rejected++;
+        T->dt = new_dt;
+        if (!(T->t < T->t_stop && T->step_idx < T->max_steps)) T->done = 1;
+    }
+    T->guard++;
+    if (!T->done && T->guard >= T->guard_cap) T->stop_reason = TRAN_STOP_GUARD;
+    const bool more = !T->done && T->stop_reason == TRAN_STOP_NONE && !(T->limit > 0 && T->accepted_now >= T->limit);
+    cudaGraphSetConditional(h_out, more ? 1u : 0u);
+}
+
+// Accept / reject commit (full_mna.py:2078-2147) with the controller's decision
+__global__ void tran_commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, int n_vsrc, int nvo, const TranDev* T,
+                                   const double* Xc, double* X, const double* Q, double* Qp, const double* dQ,
+                                   double* dQp, double* Qp2, double* hist, double* Vmax, const double* maxc,
+                                   double* hist_maxc, const double* Ivs, double* Vout, double* Iout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int use_new = T->use_new, accept = T->accept;
+    if (use_new) {
+        if (i < n_x) X[i] = Xc[i];
+        if (i < n_unk) {
+            Qp2[i] = Qp[i];
+            Qp[i] = Q[i];
+            dQp[i] = dQ[i];
+            hist_maxc[i] = fmax(hist_maxc[i], maxc[i]);
+        }
+        if (i < n_nodes) {
+            hist[(size_t)T->commit_slot * n_nodes + i] = Xc[i];
+            Vmax[i] = fmax(Vmax[i], fabs(Xc[i]));
+        }
+    }
+    if (accept) {
+        const size_t row = (size_t)T->commit_row;
+        if (i < n_ext) Vout[row * n_ext + i] = use_new ? Xc[i] : X[i];
+        if (i < n_vsrc) Iout[row * nvo + i] = T->zero_current ? 0.0 : Ivs[i];
+    }
+}
+
+// Arms a run of the step graph: at most `limit` accepted steps (0: no limit).
+__global__ void tran_arm_kernel(TranDev* T, int limit) {
+    T->limit = limit;
+    T->accepted_now = 0;
+    T->guard = 0;
+    T->stop_reason = TRAN_STOP_NONE;
 }
 
 // ---------------------------------------------------------------------------
@@ -164,12 +414,194 @@ struct TranSession {
     double device_ms = 0;
     long long launches0 = 0;
     bool done = false;
+    // the step loop as one CUDA graph (used unless the circuit disables it or profiles phases)
+    DevBuf<TranDev> d_td;
+    TranDev* h_td = nullptr;  // pinned
+    DevBuf<double> tdev;      // accepted step times, written by the device controller
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_epoch = -1;
+    long long per_iter_launches = 0, per_step_launches = 0;
 
     void setup(Circuit* cc, const double* cfg, const double* X0, const double* Q0, const double* I0,
                const double* maxc0);
     int advance(int max_accepted);
+    int advance_graph(int max_accepted);
+    void build_graph();
+    void release_graph();
     int n_x() const { return c->n_nodes + c->n_vsrc; }
+    ~TranSession() {
+        release_graph();
+        if (h_td) cudaFreeHost(h_td);
+    }
 };
+
+void TranSession::release_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+}
+
+// Capture the step loop: outer while-node (steps) { step begin, sources, initial
+// guess, inner while-node (Newton iterations) { nr_iteration, decision },
+// post-Newton rebuild, LTE, step end, commit }.
+void TranSession::build_graph() {
+    release_graph();
+    cudaStream_t s = c->stream;
+    const int n_nodes = c->n_nodes, n_unk = c->n_unk, n_vsrc = c->n_vsrc;
+    const int nx = n_x();
+    const int nvo = std::max(n_vsrc, 1);
+    const int tb = 256;
+    const int grid_x = ceil_div(std::max(nx, 1), tb);
+    VGB_CUDA(cudaStreamSynchronize(s));
+    mf_prepare_capture(*c);
+    const DefaultVecs dv = defaults_for(*c, abstol, s);
+    VGB_CUDA(cudaStreamSynchronize(s));
+    const double* fl = fixed ? dv.floor_abstol : floor_.p;
+    TranDev* T = d_td.p;
+    cudaStream_t cs1 = nullptr, cs2 = nullptr;
+    VGB_CUDA(cudaStreamCreateWithFlags(&cs1, cudaStreamNonBlocking));
+    VGB_CUDA(cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking));
+    const long long l0 = c->launches;
+    bool cap1 = false, cap2 = false;
+    try {
+        VGB_CUDA(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle h_out, h_nr;
+        VGB_CUDA(cudaGraphConditionalHandleCreate(&h_out, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams po = {};
+        po.type = cudaGraphNodeTypeConditional;
+        po.conditional.handle = h_out;
+        po.conditional.type = cudaGraphCondTypeWhile;
+        po.conditional.size = 1;
+        cudaGraphNode_t n_out;
+        VGB_CUDA(cudaGraphAddNode(&n_out, graph, nullptr, nullptr, 0, &po));
+        cudaGraph_t body = po.conditional.phGraph_out[0];
+        VGB_CUDA(cudaGraphConditionalHandleCreate(&h_nr, body, 0, 0));
+        // step begin: coefficients, sources at t_next, initial Newton guess
+        VGB_CUDA(cudaStreamBeginCaptureToGraph(cs1, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        cap1 = true;
+        tran_step_begin_kernel<<<1, 1, 0, cs1>>>(T, c->d_coeffs.p, h_nr);
+        launch_eval_sources_dev(c->vsrc_wave, n_vsrc, &T->t_next, vs.p, cs1);
+        launch_eval_sources_dev(c->isrc_wave, c->n_isrc, &T->t_next, is.p, cs1);
+        if (fixed)
+            tran_copy_kernel<<<grid_x, tb, 0, cs1>>>(nx, X.p, Xc.p);
+        else
+            tran_predict_kernel<<<grid_x, tb, 0, cs1>>>(n_nodes, nx, n_unk, X.p, Xc.p, Vpred.p, hist.p, T, hmaxc.p,
+                                                        reltol, abstol, floor_.p);
+        c->launches += 2 + (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0);
+        // the Newton loop: a while-node nested in the step body
+        cudaStreamCaptureStatus cst;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        VGB_CUDA(cudaStreamGetCaptureInfo(cs1, &cst, nullptr, nullptr, &deps, nullptr, &nd));
+        cudaGraphNodeParams pn = {};
+        pn.type = cudaGraphNodeTypeConditional;
+        pn.conditional.handle = h_nr;
+        pn.conditional.type = cudaGraphCondTypeWhile;
+        pn.conditional.size = 1;
+        cudaGraphNode_t n_nr;
+        VGB_CUDA(cudaGraphAddNode(&n_nr, body, deps, nullptr, nd, &pn));
+        cudaGraph_t nr_body = pn.conditional.phGraph_out[0];
+        VGB_CUDA(cudaStreamUpdateCaptureDependencies(cs1, &n_nr, nullptr, 1, cudaStreamSetCaptureDependencies));
+        // post-Newton rebuild (solver_factories.py:689-713), LTE, step control, commit
+        launch_status_reset(c->d_status.p, cs1);
+        build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, fl, reltol, vntol, c->d_csr_vals.p, c->d_f.p,
+                     c->d_Q.p, c->d_maxc.p, c->d_fres.p, cs1);
+        launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, cs1);
+        launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, cs1);
+        if (!fixed)
+            tran_lte_kernel<<<ceil_div(n_nodes, tb), tb, 0, cs1>>>(n_nodes, Xc.p, Vpred.p, Vmax.p, T, reltol, abstol,
+                                                                  c->d_status.p);
+        tran_step_end_kernel<<<1, 1, 0, cs1>>>(T, c->d_status.p, tdev.p, h_out);
+        tran_commit_kernel<<<grid_x, tb, 0, cs1>>>(n_nodes, nx, n_unk, n_ext, n_vsrc, nvo, T, Xc.p, X.p, c->d_Q.p,
+                                                   Qp.p, dQn.p, dQp.p, Qp2.p, hist.p, Vmax.p, c->d_maxc.p, hmaxc.p,
+                                                   Ivs.p, Vout.p, Iout.p);
+        c->launches += 1 + (n_vsrc ? 1 : 0) + (n_unk ? 1 : 0) + (fixed ? 0 : 1) + 2;
+        VGB_CUDA(cudaGetLastError());
+        cap1 = false;
+        VGB_CUDA(cudaStreamEndCapture(cs1, &body));
+        per_step_launches = c->launches - l0;
+        // one Newton iteration and its convergence decision
+        const long long l1 = c->launches;
+        VGB_CUDA(cudaStreamBeginCaptureToGraph(cs2, nr_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        cap2 = true;
+        nr_iteration(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, fl, o, cs2, false);
+        tran_nr_decide_kernel<<<1, 1, 0, cs2>>>(T, c->d_status.p, h_nr);
+        VGB_CUDA(cudaGetLastError());
+        cap2 = false;
+        VGB_CUDA(cudaStreamEndCapture(cs2, &nr_body));
+        per_iter_launches = c->launches - l1 + 1;
+        VGB_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        if (cap1) cudaStreamEndCapture(cs1, &g);
+        if (cap2) cudaStreamEndCapture(cs2, &g);
+        cudaStreamDestroy(cs1);
+        cudaStreamDestroy(cs2);
+        c->launches = l0;
+        release_graph();
+        throw;
+    }
+    cudaStreamDestroy(cs1);
+    cudaStreamDestroy(cs2);
+    c->launches = l0;  // captures launch nothing; advance_graph counts the replays
+    graph_epoch = c->config_epoch;
+}
+
+// One run of the step graph: the host controller state goes down, the graph
+// runs until `max_accepted` more steps are accepted (0: to the end), the state
+// comes back.  One synchronisation per call, none per step or Newton iteration.
+int TranSession::advance_graph(int max_accepted) {
+    cudaStream_t s = c->stream;
+    if (!gexec || graph_epoch != c->config_epoch) build_graph();
+    TranDev& h = *h_td;
+    h = TranDev{};
+    h.t_stop = t_stop; h.max_dt = max_dt; h.min_dt = min_dt; h.lte_ratio = lte_ratio; h.redo_factor = redo_factor;
+    h.grow_factor = grow_factor; h.tran_ft = tran_ft; h.gshunt_init = gshunt_init; h.gshunt_target = gshunt_target;
+    h.gshunt_steps = gshunt_steps; h.warmup_steps = warmup_steps; h.max_consec = max_consec; h.method = method;
+    h.max_steps = max_steps; h.tran_itl = tran_itl; h.fixed = fixed ? 1 : 0; h.fixed_n = fixed_n;
+    h.t = t; h.dt = dt;
+    for (int q = 0; q < 4; ++q) h.dt_hist[q] = dt_hist[q];
+    h.head = head; h.history_count = history_count; h.warmup_count = warmup_count; h.consecutive = consecutive;
+    h.step_idx = step_idx; h.fixed_i = fixed_i;
+    h.total_nr = total_nr; h.rejected = rejected; h.nr_fail_count = nr_fail_count;
+    h.min_dt_used = min_dt_used; h.max_dt_used = max_dt_used;
+    h.limit = max_accepted;
+    h.guard_cap = 16 * max_steps + 1000;  // step attempts of one run, a bound the controller never reaches
+    VGB_CUDA(cudaMemcpyAsync(d_td.p, h_td, sizeof(TranDev), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemsetAsync(&c->d_status.p->dev_err, 0, sizeof(int), s));
+    const int step0 = step_idx;
+    cudaEvent_t ev0, ev1;
+    VGB_CUDA(cudaEventCreate(&ev0));
+    VGB_CUDA(cudaEventCreate(&ev1));
+    VGB_CUDA(cudaEventRecord(ev0, s));
+    VGB_CUDA(cudaGraphLaunch(gexec, s));
+    VGB_CUDA(cudaEventRecord(ev1, s));
+    VGB_CUDA(cudaMemcpyAsync(h_td, d_td.p, sizeof(TranDev), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    VGB_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    device_ms += ms;
+    const TranDev& d = *h_td;
+    c->launches += 1 + (d.total_nr - total_nr) * per_iter_launches + (long long)d.guard * per_step_launches;
+    if (d.step_idx > step0)
+        VGB_CUDA(cudaMemcpy(tout.data() + step0, tdev.p + step0, (size_t)(d.step_idx - step0) * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+    t = d.t; dt = d.dt;
+    for (int q = 0; q < 4; ++q) dt_hist[q] = d.dt_hist[q];
+    head = d.head; history_count = d.history_count; warmup_count = d.warmup_count; consecutive = d.consecutive;
+    step_idx = d.step_idx; fixed_i = d.fixed_i;
+    total_nr = d.total_nr; rejected = d.rejected; nr_fail_count = d.nr_fail_count;
+    min_dt_used = d.min_dt_used; max_dt_used = d.max_dt_used;
+    done = d.done != 0;
+    if (d.stop_reason == TRAN_STOP_TIMEOUT) throw Error(VGB_ERR_TIMEOUT, "sparse LU dependency wait timed out");
+    if (d.stop_reason == TRAN_STOP_GUARD)
+        throw Error(VGB_ERR_STATE, "transient step loop reached its bound on step attempts");
+    return d.accepted_now;
+}
 
 void TranSession::setup(Circuit* cc, const double* cfg, const double* X0, const double* Q0, const double* I0,
                         const double* maxc0) {
@@ -237,12 +669,19 @@ void TranSession::setup(Circuit* cc, const double* cfg, const double* X0, const 
         fixed_n = std::min((int)(t_stop / dt), max_steps - 1);
         if (fixed_n < 1) fixed_n = 1;
     }
+    // device controller state of the step graph
+    d_td.alloc(1);
+    VGB_CUDA(cudaMallocHost((void**)&h_td, sizeof(TranDev)));
+    tdev.alloc(max_steps);
+    tdev.zero(s);
+    VGB_CUDA(cudaStreamSynchronize(s));
     launches0 = c->launches;
 }
 
 // Run until max_accepted more steps are accepted (0 = to the end of the run).
 int TranSession::advance(int max_accepted) {
     if (done) return 0;
+    if (c->tran_graph && !c->profile) return advance_graph(max_accepted);
     cudaStream_t s = c->stream;
     const int n_nodes = c->n_nodes, n_unk = c->n_unk, n_vsrc = c->n_vsrc;
     const int nx = n_x();
@@ -275,10 +714,10 @@ int TranSession::advance(int max_accepted) {
             total_nr += r.iterations;
             if (!r.converged) nr_fail_count++;
             launch_status_reset(c->d_status.p, s);
-            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, k, dv.floor_abstol, reltol, vntol,
+            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, dv.floor_abstol, reltol, vntol,
                          c->d_csr_vals.p, c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
             launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
-            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, k.c0, k.c1, k.d1, k.c2, dQn.p, n_unk, s);
+            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, s);
             const int slot = ((i + 1) % 4);
             commit_kernel<<<grid_x, tb, 0, s>>>(n_nodes, nx, n_unk, n_ext, n_vsrc, 1, 1, 0, Xc.p, X.p,
                                                  c->d_Q.p, Qp.p, dQn.p, dQp.p, Qp2.p, hist.p + (size_t)slot * n_nodes,
@@ -328,10 +767,10 @@ int TranSession::advance(int max_accepted) {
             total_nr += r.iterations;
             // post-NR rebuild (solver_factories.py:689-713) + LTE
             launch_status_reset(c->d_status.p, s);
-            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, k, floor_.p, reltol, vntol, c->d_csr_vals.p,
+            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, floor_.p, reltol, vntol, c->d_csr_vals.p,
                          c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
             launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
-            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, k.c0, k.c1, k.d1, k.c2, dQn.p, n_unk, s);
+            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, s);
             const double kl = err_integ / (err_integ - pr.err);
             lte_kernel<<<ceil_div(n_nodes, tb), tb, 0, s>>>(n_nodes, Xc.p, Vpred.p, Vmax.p, kl, reltol, abstol,
                                                              c->d_status.p);

@@ -108,6 +108,11 @@ class DeviceCircuit:
         """Launch shape or schedule knob (see vgb_set_tuning)."""
         self._check(self.lib.vgb_set_tuning(self.h, self.TUNING_KNOBS[knob], int(value)))
 
+    def set_transient_graph(self, on: bool):
+        """Transient sessions created afterwards run their step loop as one CUDA
+        graph (True, the default) or as the host-driven loop (False)."""
+        self._check(self.lib.vgb_set_tuning(self.h, 3, 1 if on else 0))
+
     def tuning(self) -> Dict[str, int]:
         out = {}
         for name, k in self.TUNING_KNOBS.items():
