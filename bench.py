@@ -582,7 +582,8 @@ def run_serving(args):
     sampler = ClockSampler(gpu_index(local))
     sampler.start()
     torch.cuda.synchronize()
-    srv = serve(jobs, arrivals, slots=args.slots, precision=args.precision, max_batch=args.max_batch)
+    srv = serve(jobs, arrivals, slots=args.slots, precision=args.precision, max_batch=args.max_batch,
+                transient_graph=args.serving_graph == "on")
     torch.cuda.synchronize()
     clocks = sampler.stop()
     st = srv.stats()
@@ -595,7 +596,7 @@ def run_serving(args):
     for j in seq_jobs:
         a = time.perf_counter()
         try:
-            run_group([j], precision="fp64")
+            run_group([j], precision="fp64", transient_graph=True)  # the faster form for one job alone
             iters += j.newton_iters
         except RuntimeError as e:
             j.error = str(e)
@@ -617,7 +618,9 @@ def run_serving(args):
            "config": {"workload": SERVING["workload"], "jobs": n, "arrival_rate_per_s": SERVING["rate"],
                       "ring_stages": SERVING["ring_stages"], "network_transistors": [200, args.max_transistors],
                       "slots": args.slots, "max_batch": args.max_batch, "precision": args.precision,
-                      "seed": SERVING["seed"], "l2": "inputs and fronts of concurrent jobs exceed L2"},
+                      "seed": SERVING["seed"], "l2": "inputs and fronts of concurrent jobs exceed L2",
+                      "served_step_loop": "cuda_graph" if args.serving_graph == "on" else "host_driven",
+                      "sequential_step_loop": "cuda_graph"},
            "p50_latency_s": st.get("p50_s"), "p99_latency_s": st.get("p99_s"), "jobs_per_s": st.get("jobs_per_s"),
            "groups": st.get("groups"), "mean_group": st.get("mean_group"), "failed": st.get("failed"),
            "failed_jobs": [(j.job_id, j.error) for j in srv.results() if j.error],
@@ -721,6 +724,8 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")
     ap.add_argument("--max-transistors", type=int, default=SERVING["network_transistors"][1],
                     help="serving: largest gate network in the stream")
+    ap.add_argument("--serving-graph", choices=["on", "off"], default="off",
+                    help="serving: served sessions run the CUDA-graph step loop (default: host-driven loop)")
     ap.add_argument("--autotune", choices=["on", "off"], default="on",
                     help="tune launch shapes and the factorisation schedule before the run (outside the timing)")
     ap.add_argument("--reference-budget", type=float, default=150.0, help="seconds of timed CPU work, reference arm")

@@ -10,7 +10,10 @@ one batched circuit (disjoint copies in one system, one launch per kernel
 for the whole group): DC operating point, then the transient advanced in
 slices of ``slice_steps`` accepted steps.  Groups overlap on the device, and
 new jobs keep being admitted while earlier ones finish and free their slot
-and memory.
+and memory.  Sessions use the host-driven step loop by default
+(``transient_graph=False``): its per-iteration synchronisations are where the
+other groups' kernels interleave, and on the job stream of the benchmark it
+serves about twice the solves/s of one-graph-per-slice sessions.
 
 A job in a group of one gives bit-for-bit the result it gives alone (every
 kernel sums in a fixed order).  A job in a larger group shares the group's
@@ -85,7 +88,8 @@ def estimate_footprint(info: Dict[str, int], precision: str = "fp64") -> int:
     return int(val * info["front_storage"] + 8 * (3 * info["contrib_slots"] + 2 * nnz) + 8 * 40 * n + (1 << 20))
 
 
-def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, reserve=None):
+def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, reserve=None,
+              transient_graph: bool = False):
     """DC operating point + transient of a group of same-pattern jobs as one
     batched circuit.  Fills each job's result; returns the reserved bytes."""
     from vajax_gb300.corners import concat_circuits
@@ -106,6 +110,7 @@ def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, r
     if reserve is not None:
         reserve(footprint)
     eng.prepare(t_stop=lead.t_stop, dt=lead.dt, max_steps=lead.max_steps)
+    eng.device.set_transient_graph(transient_graph)
     t_adm = time.perf_counter()
     try:
         X0, Q0, I0, maxc0, ok = eng.initial_state()
@@ -135,8 +140,9 @@ def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, r
 
 class Server:
     def __init__(self, slots: int = 8, hbm_budget: int = 64 << 30, precision: str = "fp64", slice_steps: int = 50,
-                 max_batch: int = 64):
+                 max_batch: int = 64, transient_graph: bool = False):
         self.slots = slots
+        self.transient_graph = transient_graph
         self.hbm_budget = hbm_budget
         self.precision = precision
         self.slice_steps = slice_steps
@@ -216,7 +222,7 @@ class Server:
             reserved[0] = nbytes
 
         try:
-            run_group(group, self.precision, self.slice_steps, reserve)
+            run_group(group, self.precision, self.slice_steps, reserve, self.transient_graph)
         except Exception as e:  # a failing group reports, the server carries on
             for j in group:
                 j.error = f"{type(e).__name__}: {e}"
@@ -249,10 +255,10 @@ class Server:
 
 
 def serve(jobs: List[Job], arrivals: List[float], slots: int = 8, precision: str = "fp64", max_batch: int = 64,
-          hbm_budget: int = 64 << 30, slice_steps: int = 50) -> Server:
+          hbm_budget: int = 64 << 30, slice_steps: int = 50, transient_graph: bool = False) -> Server:
     """Submit `jobs` at the given arrival offsets (seconds) to a fresh server and wait for all of them."""
     srv = Server(slots=slots, precision=precision, max_batch=max_batch, hbm_budget=hbm_budget,
-                 slice_steps=slice_steps).start()
+                 slice_steps=slice_steps, transient_graph=transient_graph).start()
     t0 = time.perf_counter()
     for j, a in sorted(zip(jobs, arrivals), key=lambda p: p[1]):
         delay = a - (time.perf_counter() - t0)
