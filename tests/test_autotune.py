@@ -93,3 +93,34 @@ def test_knobs_change_no_result_bit_and_tuner_runs(cuda, tmp_path):
     again = autotune(dc, torch.as_tensor(X, device=cuda), rc.source_values(0.0), reps=2, cache=cache)
     assert again["cached"] and again["tuning"] == out["tuning"]
     assert np.array_equal(newton3(), ref)
+
+
+def test_tuning_knobs_validate_on_the_host():
+    """vgb_set_tuning / vgb_get_tuning on an analysed host-only circuit: valid values
+    stick, invalid ones return an error status and change nothing."""
+    from vajax_gb300.generators import random_gate_network
+    from vajax_gb300.runtime import DeviceCircuit
+    c, _ = random_gate_network(n_gates=120, depth=6, n_inputs=8, seed=5)
+    dc = DeviceCircuit(c.resolve(), device=False)
+    assert dc.tuning() == {"factor_ctas_per_sm": 4, "solve_ctas_per_sm": 4, "eval_block": 64}
+    dc.set_tuning("eval_block", 128)
+    dc.set_tuning("solve_ctas_per_sm", 1)
+    assert dc.tuning()["eval_block"] == 128 and dc.tuning()["solve_ctas_per_sm"] == 1
+    for knob, bad in (("eval_block", 48), ("eval_block", 512), ("solve_ctas_per_sm", 0), ("solve_ctas_per_sm", 5),
+                      ("factor_ctas_per_sm", 0), ("factor_ctas_per_sm", 5)):
+        before = dc.tuning()
+        with pytest.raises(Exception):
+            dc.set_tuning(knob, bad)
+        assert dc.tuning() == before
+    # changing the factorisation CTAs re-schedules the task list on the host; the
+    # schedule stays a topological order of the same tasks
+    n_tasks = dc.solver_info()["tasks"]
+    dc.set_tuning("factor_ctas_per_sm", 2)
+    assert dc.solver_info()["tasks"] == n_tasks
+    dc.set_transient_graph(False)
+    dc.set_transient_graph(True)
+    with pytest.raises(Exception):
+        dc._check(dc.lib.vgb_set_tuning(dc.h, 3, 2))
+    with pytest.raises(Exception):
+        dc._check(dc.lib.vgb_set_tuning(dc.h, 99, 1))
+    dc.close()
