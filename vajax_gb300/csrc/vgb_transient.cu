@@ -67,7 +67,7 @@ __global__ void lte_kernel(int n_nodes, const double* Vnew, const double* Vpred,
 }
 
 // Accept / reject commit (full_mna.py:2078-2147).
-__global__ void commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, int n_vsrc, int use_new, int accept,
+__device__ __forceinline__ void commit_kernel_body(int n_nodes, int n_x, int n_unk, int n_ext, int n_vsrc, int use_new, int accept,
                               int zero_current, const double* Xc, double* X, const double* Q, double* Qp,
                               const double* dQ, double* dQp, double* Qp2, double* hist_slot, double* Vmax,
                               const double* maxc, double* hist_maxc, const double* Ivs, double* Vout_row,
@@ -90,6 +90,15 @@ __global__ void commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, int n_
         if (i < n_ext) Vout_row[i] = use_new ? Xc[i] : X[i];
         if (i < n_vsrc) Iout_row[i] = zero_current ? 0.0 : Ivs[i];
     }
+}
+
+__global__ void commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, int n_vsrc, int use_new, int accept,
+                              int zero_current, const double* Xc, double* X, const double* Q, double* Qp,
+                              const double* dQ, double* dQp, double* Qp2, double* hist_slot, double* Vmax,
+                              const double* maxc, double* hist_maxc, const double* Ivs, double* Vout_row,
+                              double* Iout_row) {
+    commit_kernel_body(n_nodes, n_x, n_unk, n_ext, n_vsrc, use_new, accept, zero_current, Xc, X, Q, Qp, dQ, dQp, Qp2,
+                       hist_slot, Vmax, maxc, hist_maxc, Ivs, Vout_row, Iout_row);
 }
 
 static double bits_to_double(unsigned long long b) {
@@ -151,88 +160,182 @@ __host__ __device__ inline Pred predictor_coeffs(const double dt_hist[4], int hi
 // device (tran_itl iterations; guard_cap step attempts), whatever the inputs.
 // ---------------------------------------------------------------------------
 
+// ---------------------------------------------------------------------------
+// Step controller (full_mna.py:1236-1253 fixed coefficients, :1851-1891 BDF2
+// coefficients, :1984-2147 LTE control and commit; adaptive.py:94-339).  One
+// implementation for both step loops: the host-driven loop calls it on the
+// session and the transient graph calls it from one-thread kernels on the
+// device state.  S is either; both carry the same field names.
+// ---------------------------------------------------------------------------
+
+struct StepPlan {
+    double k[5];  // c0, c1, d1, c2, gshunt
+    double t_next, kl, pa[3];
+    int can_predict, slot[3];
+};
+
+struct StepCommit {
+    int use_new, accept, zero_current, row, slot;
+};
+
+template <class S>
+__host__ __device__ inline StepPlan ctl_plan(const S& s) {
+    StepPlan p{};
+    const double dt_cur = s.dt;
+    const double inv = 1.0 / dt_cur;
+    p.k[0] = inv;
+    p.k[1] = -inv;
+    if (s.fixed) {
+        if (s.method == 1) { p.k[0] = 2 * inv; p.k[1] = -2 * inv; p.k[2] = -1.0; }
+        else if (s.method == 2) { p.k[0] = 1.5 * inv; p.k[1] = -2.0 * inv; p.k[3] = 0.5 * inv; }
+        p.t_next = ((double)s.fixed_i + 1.0) * dt_cur;
+        return p;
+    }
+    double err_integ;
+    if (s.method == 0) {
+        err_integ = -0.5;
+    } else if (s.method == 1) {
+        p.k[0] = 2 * inv; p.k[1] = -2 * inv; p.k[2] = -1.0;
+        err_integ = 1.0 / 24.0;
+    } else {
+        const double dt_prev = s.dt_hist[0];
+        const double w = dt_prev > 0 ? dt_cur / dt_prev : 1.0;
+        const double wp1 = 1.0 + w;
+        p.k[0] = (1.0 + 2.0 * w) / (wp1 * dt_cur);
+        p.k[1] = -wp1 / dt_cur;
+        p.k[3] = (w * w) / (wp1 * dt_cur);
+        err_integ = -2.0 / 9.0;
+    }
+    p.t_next = s.t + dt_cur;
+    p.can_predict = (s.warmup_count >= s.warmup_steps && s.history_count >= 2) ? 1 : 0;
+    const Pred pr = predictor_coeffs(s.dt_hist, s.history_count, dt_cur, 2);
+    int order = s.history_count - 1 < 2 ? s.history_count - 1 : 2;
+    order = order > 0 ? order : 0;
+    p.pa[0] = pr.a[0];
+    p.pa[1] = order >= 1 ? pr.a[1] : 0.0;
+    p.pa[2] = order >= 2 ? pr.a[2] : 0.0;
+    for (int q = 0; q < 3; ++q) p.slot[q] = (s.head + q) % 4;
+    const double ramp = s.gshunt_steps > 0 ? fmin(fmax((double)s.step_idx / s.gshunt_steps, 0.0), 1.0) : 1.0;
+    p.k[4] = s.gshunt_init + ramp * (s.gshunt_target - s.gshunt_init);
+    p.kl = err_integ / (err_integ - pr.err);
+    return p;
+}
+
+// Accept / reject, next dt, history update and the commit of the step; writes
+// the accepted time into tout.  Returns the commit parameters.
+template <class S>
+__host__ __device__ inline StepCommit ctl_finish(S& s, const StepPlan& p, double lte_norm, int nr_iters,
+                                                 bool converged, double* tout) {
+    StepCommit m{};
+    s.total_nr += nr_iters;
+    const bool nr_failed = !converged;
+    if (nr_failed) s.nr_fail_count++;
+    if (s.fixed) {
+        const int i = s.fixed_i;
+        m.use_new = 1; m.accept = 1; m.zero_current = 0; m.row = i + 1; m.slot = (i + 1) % 4;
+        tout[i + 1] = p.t_next;
+        s.fixed_i = i + 1;
+        s.step_idx = s.fixed_i + 1;
+        if (s.fixed_i >= s.fixed_n) s.done = true;
+        return m;
+    }
+    const double dt_cur = s.dt;
+    const int lte_order = s.history_count - 1 < 2 ? s.history_count - 1 : 2;
+    double factor = pow(s.lte_ratio / fmax(lte_norm, 1e-10), 1.0 / (lte_order + 1));
+    factor = fmin(fmax(factor, 0.1), s.grow_factor);
+    const double dt_lte = dt_cur * factor;
+    const bool at_min_dt = dt_cur <= s.min_dt;
+    const bool nr_failed_at_min = nr_failed && at_min_dt;
+    const bool lte_reject = (dt_cur / dt_lte > s.redo_factor) && p.can_predict && converged;
+    const bool nr_reject = nr_failed && !at_min_dt;
+    const bool force_accept = s.consecutive >= s.max_consec;
+    const bool reject = (lte_reject || nr_reject) && !force_accept;
+    const bool accept = !reject;
+    s.consecutive = accept ? 0 : (lte_reject ? s.consecutive + 1 : s.consecutive);
+    const double dt_from_lte = p.can_predict ? dt_lte : dt_cur;
+    const double dt_nr_halved = fmax(dt_cur * s.tran_ft, s.min_dt);
+    const double last_good = s.history_count > 0 ? s.dt_hist[0] : s.min_dt * 16.0;
+    const double dt_recovery = fmax(last_good / 8.0, s.min_dt * 2.0);
+    double new_dt = nr_failed ? (at_min_dt ? dt_recovery : dt_nr_halved) : dt_from_lte;
+    new_dt = fmin(fmax(new_dt, s.min_dt), s.max_dt);
+    new_dt = fmin(new_dt, s.t_stop - p.t_next);
+    const bool use_new = accept && !nr_failed_at_min;
+    const int new_head = use_new ? (s.head + 3) % 4 : s.head;
+    m.use_new = use_new ? 1 : 0;
+    m.accept = accept ? 1 : 0;
+    m.zero_current = nr_failed_at_min ? 1 : 0;
+    m.row = s.step_idx;
+    m.slot = new_head;
+    if (use_new) {
+        s.head = new_head;
+        for (int q = 3; q > 0; --q) s.dt_hist[q] = s.dt_hist[q - 1];
+        s.dt_hist[0] = dt_cur;
+        s.history_count = s.history_count + 1 < 4 ? s.history_count + 1 : 4;
+        s.warmup_count++;
+    }
+    if (accept) {
+        tout[s.step_idx] = p.t_next;
+        s.t = p.t_next;
+        s.step_idx++;
+        s.min_dt_used = fmin(s.min_dt_used, dt_cur);
+        s.max_dt_used = fmax(s.max_dt_used, dt_cur);
+    }
+    if (reject) s.rejected++;
+    s.dt = new_dt;
+    if (!(s.t < s.t_stop && s.step_idx < s.max_steps)) s.done = true;
+    return m;
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident step loop (the transient graph).  The controller state of a
+// session lives in device memory; one-thread kernels run ctl_plan, the Newton
+// convergence decision and ctl_finish between the batched kernels.  The whole
+// loop is one CUDA graph: an outer while-node over steps whose body holds an
+// inner while-node over Newton iterations.  Both loops are bounded on the
+// device (tran_itl iterations; guard_cap step attempts), whatever the inputs.
+// ---------------------------------------------------------------------------
+
 struct TranDev {
-    // configuration
+    // configuration (field names as in TranSession, for ctl_plan / ctl_finish)
     double t_stop, max_dt, min_dt, lte_ratio, redo_factor, grow_factor, tran_ft, gshunt_init, gshunt_target;
     int gshunt_steps, warmup_steps, max_consec, method, max_steps, tran_itl, fixed, fixed_n;
     // controller state
     double t, dt, dt_hist[4];
     int head, history_count, warmup_count, consecutive, step_idx, fixed_i;
-    // the step in progress
-    double t_next, kl, pa[3];
-    int can_predict, slot0, slot1, slot2;
-    int nr_it, nr_conv;
-    // commit of the step, decided by the step-end kernel
-    int use_new, accept, zero_current, commit_row, commit_slot;
-    // statistics and loop control
     long long total_nr;
-    int rejected, nr_fail_count, accepted_now, limit, guard, guard_cap, done, stop_reason;
+    int rejected, nr_fail_count, done;
     double min_dt_used, max_dt_used;
+    // the step in progress
+    StepPlan plan;
+    StepCommit commit;
+    int nr_it, nr_conv;
+    // loop control of one run
+    int accepted_now, limit, guard, guard_cap, stop_reason;
 };
 
 enum { TRAN_STOP_NONE = 0, TRAN_STOP_TIMEOUT = 1, TRAN_STOP_GUARD = 2 };
 
-// Integration coefficients of the step (k = {c0, c1, d1, c2, gshunt}), predictor
-// weights and history slots; arms the Newton loop.
+// Plan of the step (coefficients into k); arms the Newton loop.
 __global__ void tran_step_begin_kernel(TranDev* T, double* k, cudaGraphConditionalHandle h_nr) {
-    const double dt_cur = T->dt;
-    const double inv = 1.0 / dt_cur;
-    double c0 = inv, c1 = -inv, d1 = 0.0, c2 = 0.0, gshunt = 0.0;
-    if (T->fixed) {
-        // constant-step coefficients (full_mna.py:1236-1253)
-        if (T->method == 1) { c0 = 2 * inv; c1 = -2 * inv; d1 = -1.0; }
-        else if (T->method == 2) { c0 = 1.5 * inv; c1 = -2.0 * inv; c2 = 0.5 * inv; }
-        T->t_next = ((double)T->fixed_i + 1.0) * dt_cur;
-    } else {
-        double err_integ;
-        if (T->method == 0) { err_integ = -0.5; }
-        else if (T->method == 1) { c0 = 2 * inv; c1 = -2 * inv; d1 = -1.0; err_integ = 1.0 / 24.0; }
-        else {
-            const double dt_prev = T->dt_hist[0];
-            const double w = dt_prev > 0 ? dt_cur / dt_prev : 1.0;
-            const double wp1 = 1.0 + w;
-            c0 = (1.0 + 2.0 * w) / (wp1 * dt_cur);
-            c1 = -wp1 / dt_cur;
-            c2 = (w * w) / (wp1 * dt_cur);
-            err_integ = -2.0 / 9.0;
-        }
-        T->t_next = T->t + dt_cur;
-        T->can_predict = (T->warmup_count >= T->warmup_steps && T->history_count >= 2) ? 1 : 0;
-        const Pred pr = predictor_coeffs(T->dt_hist, T->history_count, dt_cur, 2);
-        int order = T->history_count - 1 < 2 ? T->history_count - 1 : 2;
-        order = order > 0 ? order : 0;
-        T->pa[0] = pr.a[0];
-        T->pa[1] = order >= 1 ? pr.a[1] : 0.0;
-        T->pa[2] = order >= 2 ? pr.a[2] : 0.0;
-        T->slot0 = (T->head + 0) % 4;
-        T->slot1 = (T->head + 1) % 4;
-        T->slot2 = (T->head + 2) % 4;
-        const double ramp =
-            T->gshunt_steps > 0 ? fmin(fmax((double)T->step_idx / T->gshunt_steps, 0.0), 1.0) : 1.0;
-        gshunt = T->gshunt_init + ramp * (T->gshunt_target - T->gshunt_init);
-        T->kl = err_integ / (err_integ - pr.err);
-    }
-    k[0] = c0;
-    k[1] = c1;
-    k[2] = d1;
-    k[3] = c2;
-    k[4] = gshunt;
+    T->plan = ctl_plan(*T);
+    for (int q = 0; q < 5; ++q) k[q] = T->plan.k[q];
     T->nr_it = 0;
     T->nr_conv = 0;
     cudaGraphSetConditional(h_nr, 1u);
 }
 
-// X_init from the predictor (adaptive), as predict_kernel with the device coefficients
+// X_init from the predictor (adaptive): predict_kernel with the plan in device memory
 __global__ void tran_predict_kernel(int n_nodes, int n_x, int n_unk, const double* X, double* Xc, double* Vpred,
                                     const double* hist, const TranDev* T, const double* hist_maxc, double reltol,
                                     double abstol, double* floor_) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const StepPlan& p = T->plan;
     if (i < n_nodes) {
-        const double vp = T->pa[0] * hist[(size_t)T->slot0 * n_nodes + i] +
-                          T->pa[1] * hist[(size_t)T->slot1 * n_nodes + i] +
-                          T->pa[2] * hist[(size_t)T->slot2 * n_nodes + i];
+        const double vp = p.pa[0] * hist[(size_t)p.slot[0] * n_nodes + i] +
+                          p.pa[1] * hist[(size_t)p.slot[1] * n_nodes + i] +
+                          p.pa[2] * hist[(size_t)p.slot[2] * n_nodes + i];
         Vpred[i] = vp;
-        Xc[i] = T->can_predict ? vp : X[i];
+        Xc[i] = p.can_predict ? vp : X[i];
     } else if (i < n_x) {
         Xc[i] = X[i];
     }
@@ -262,11 +365,11 @@ __global__ void tran_nr_decide_kernel(TranDev* T, const NRStatus* S, cudaGraphCo
     cudaGraphSetConditional(h_nr, stop ? 0u : 1u);
 }
 
-// LTE norm with the coefficient from the controller
+// LTE norm: lte_kernel with the coefficient from the plan
 __global__ void tran_lte_kernel(int n_nodes, const double* Vnew, const double* Vpred, const double* Vmax,
                                 const TranDev* T, double reltol, double abstol, NRStatus* st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const double k = T->kl;
+    const double k = T->plan.kl;
     double v = 0.0;
     if (i < n_nodes) {
         const double lte = (Vnew[i] - Vpred[i]) * k;
@@ -281,72 +384,11 @@ __global__ void tran_lte_kernel(int n_nodes, const double* Vnew, const double* V
         atomicMax(&st->lte_norm, (unsigned long long)__double_as_longlong(v));
 }
 
-// Accept / reject and the next step size (the host loop's controller), then the
-// loop condition of the step graph.
+// ctl_finish on the device state, then the loop condition of the step graph.
 __global__ void tran_step_end_kernel(TranDev* T, const NRStatus* S, double* tdev, cudaGraphConditionalHandle h_out) {
-    T->total_nr += T->nr_it;
-    const bool nr_failed = !T->nr_conv;
-    if (nr_failed) T->nr_fail_count++;
-    if (T->fixed) {
-        const int i = T->fixed_i;
-        T->use_new = 1;
-        T->accept = 1;
-        T->zero_current = 0;
-        T->commit_row = i + 1;
-        T->commit_slot = (i + 1) % 4;
-        tdev[i + 1] = T->t_next;
-        T->fixed_i = i + 1;
-        T->step_idx = i + 2;
-        T->accepted_now++;
-        if (T->fixed_i >= T->fixed_n) T->done = 1;
-    } else {
-        const double dt_cur = T->dt;
-        const double lte_norm = __longlong_as_double((long long)S->lte_norm);
-        const int lte_order = T->history_count - 1 < 2 ? T->history_count - 1 : 2;
-        double factor = pow(T->lte_ratio / fmax(lte_norm, 1e-10), 1.0 / (lte_order + 1));
-        factor = fmin(fmax(factor, 0.1), T->grow_factor);
-        const double dt_lte = dt_cur * factor;
-        const bool at_min_dt = dt_cur <= T->min_dt;
-        const bool nr_failed_at_min = nr_failed && at_min_dt;
-        const bool lte_reject = (dt_cur / dt_lte > T->redo_factor) && T->can_predict && !nr_failed;
-        const bool nr_reject = nr_failed && !at_min_dt;
-        const bool force_accept = T->consecutive >= T->max_consec;
-        const bool reject = (lte_reject || nr_reject) && !force_accept;
-        const bool accept = !reject;
-        T->consecutive = accept ? 0 : (lte_reject ? T->consecutive + 1 : T->consecutive);
-        const double dt_from_lte = T->can_predict ? dt_lte : dt_cur;
-        const double dt_nr_halved = fmax(dt_cur * T->tran_ft, T->min_dt);
-        const double last_good = T->history_count > 0 ? T->dt_hist[0] : T->min_dt * 16.0;
-        const double dt_recovery = fmax(last_good / 8.0, T->min_dt * 2.0);
-        double new_dt = nr_failed ? (at_min_dt ? dt_recovery : dt_nr_halved) : dt_from_lte;
-        new_dt = fmin(fmax(new_dt, T->min_dt), T->max_dt);
-        new_dt = fmin(new_dt, T->t_stop - T->t_next);
-        const bool use_new = accept && !nr_failed_at_min;
-        const int new_head = use_new ? (T->head + 3) % 4 : T->head;
-        T->use_new = use_new ? 1 : 0;
-        T->accept = accept ? 1 : 0;
-        T->zero_current = nr_failed_at_min ? 1 : 0;
-        T->commit_row = T->step_idx;
-        T->commit_slot = new_head;
-        if (use_new) {
-            T->head = new_head;
-            for (int q = 3; q > 0; --q) T->dt_hist[q] = T->dt_hist[q - 1];
-            T->dt_hist[0] = dt_cur;
-            T->history_count = T->history_count + 1 < 4 ? T->history_count + 1 : 4;
-            T->warmup_count++;
-        }
-        if (accept) {
-            tdev[T->step_idx] = T->t_next;
-            T->t = T->t_next;
-            T->step_idx++;
-            T->accepted_now++;
-            T->min_dt_used = fmin(T->min_dt_used, dt_cur);
-            T->max_dt_used = fmax(T->max_dt_used, dt_cur);
-        }
-        if (reject) T->rejected++;
-        T->dt = new_dt;
-        if (!(T->t < T->t_stop && T->step_idx < T->max_steps)) T->done = 1;
-    }
+    const double lte_norm = __longlong_as_double((long long)S->lte_norm);
+    T->commit = ctl_finish(*T, T->plan, lte_norm, T->nr_it, T->nr_conv != 0, tdev);
+    T->accepted_now += T->commit.accept;
     T->guard++;
     if (!T->done && T->guard >= T->guard_cap) T->stop_reason = TRAN_STOP_GUARD;
     const bool more = !T->done && T->stop_reason == TRAN_STOP_NONE && !(T->limit > 0 && T->accepted_now >= T->limit);
@@ -358,26 +400,10 @@ __global__ void tran_commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, i
                                    const double* Xc, double* X, const double* Q, double* Qp, const double* dQ,
                                    double* dQp, double* Qp2, double* hist, double* Vmax, const double* maxc,
                                    double* hist_maxc, const double* Ivs, double* Vout, double* Iout) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int use_new = T->use_new, accept = T->accept;
-    if (use_new) {
-        if (i < n_x) X[i] = Xc[i];
-        if (i < n_unk) {
-            Qp2[i] = Qp[i];
-            Qp[i] = Q[i];
-            dQp[i] = dQ[i];
-            hist_maxc[i] = fmax(hist_maxc[i], maxc[i]);
-        }
-        if (i < n_nodes) {
-            hist[(size_t)T->commit_slot * n_nodes + i] = Xc[i];
-            Vmax[i] = fmax(Vmax[i], fabs(Xc[i]));
-        }
-    }
-    if (accept) {
-        const size_t row = (size_t)T->commit_row;
-        if (i < n_ext) Vout[row * n_ext + i] = use_new ? Xc[i] : X[i];
-        if (i < n_vsrc) Iout[row * nvo + i] = T->zero_current ? 0.0 : Ivs[i];
-    }
+    const StepCommit& m = T->commit;
+    commit_kernel_body(n_nodes, n_x, n_unk, n_ext, n_vsrc, m.use_new, m.accept, m.zero_current, Xc, X, Q, Qp, dQ,
+                       dQp, Qp2, hist + (size_t)m.slot * n_nodes, Vmax, maxc, hist_maxc, Ivs,
+                       Vout + (size_t)m.row * n_ext, Iout + (size_t)m.row * nvo);
 }
 
 // Arms a run of the step graph: at most `limit` accepted steps (0: no limit).
@@ -482,8 +508,8 @@ void TranSession::build_graph() {
         VGB_CUDA(cudaStreamBeginCaptureToGraph(cs1, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         cap1 = true;
         tran_step_begin_kernel<<<1, 1, 0, cs1>>>(T, c->d_coeffs.p, h_nr);
-        launch_eval_sources_dev(c->vsrc_wave, n_vsrc, &T->t_next, vs.p, cs1);
-        launch_eval_sources_dev(c->isrc_wave, c->n_isrc, &T->t_next, is.p, cs1);
+        launch_eval_sources_dev(c->vsrc_wave, n_vsrc, &T->plan.t_next, vs.p, cs1);
+        launch_eval_sources_dev(c->isrc_wave, c->n_isrc, &T->plan.t_next, is.p, cs1);
         if (fixed)
             tran_copy_kernel<<<grid_x, tb, 0, cs1>>>(nx, X.p, Xc.p);
         else
@@ -669,6 +695,8 @@ void TranSession::setup(Circuit* cc, const double* cfg, const double* X0, const 
         fixed_n = std::min((int)(t_stop / dt), max_steps - 1);
         if (fixed_n < 1) fixed_n = 1;
     }
+    // an adaptive run with nothing to do (t_stop = 0 or max_steps = 1) is done at once
+    done = !fixed && !(t < t_stop && step_idx < max_steps);
     // device controller state of the step graph
     d_td.alloc(1);
     VGB_CUDA(cudaMallocHost((void**)&h_td, sizeof(TranDev)));
@@ -696,138 +724,54 @@ int TranSession::advance(int max_accepted) {
     VGB_CUDA(cudaEventRecord(ev0, s));
     const auto limit_hit = [&]() { return max_accepted > 0 && accepted_now >= max_accepted; };
 
-    if (fixed) {
-        // constant-step coefficients (full_mna.py:1236-1253)
-        const double inv = 1.0 / dt;
+    // the host-driven loop: the same controller (ctl_plan / ctl_finish) on the host,
+    // one status read back per Newton iteration and one LTE read back per step
+    const DefaultVecs dv = defaults_for(*c, abstol, s);
+    while (!done && !limit_hit()) {
+        const StepPlan p = ctl_plan(*this);
         Coeffs k;
-        k.c0 = inv; k.c1 = -inv;
-        if (method == 1) { k.c0 = 2 * inv; k.c1 = -2 * inv; k.d1 = -1.0; }
-        else if (method == 2) { k.c0 = 1.5 * inv; k.c1 = -2.0 * inv; k.c2 = 0.5 * inv; }
-        DefaultVecs dv = defaults_for(*c, abstol, s);
-        while (fixed_i < fixed_n && !limit_hit()) {
-            const int i = fixed_i;
-            const double t_next = ((double)i + 1.0) * dt;
-            launch_eval_sources(c->vsrc_wave, n_vsrc, t_next, vs.p, s);
-            launch_eval_sources(c->isrc_wave, c->n_isrc, t_next, is.p, s);
+        k.c0 = p.k[0];
+        k.c1 = p.k[1];
+        k.d1 = p.k[2];
+        k.c2 = p.k[3];
+        k.gshunt = p.k[4];
+        launch_eval_sources(c->vsrc_wave, n_vsrc, p.t_next, vs.p, s);
+        launch_eval_sources(c->isrc_wave, c->n_isrc, p.t_next, is.p, s);
+        const double* fl = fixed ? dv.floor_abstol : floor_.p;
+        if (fixed) {
             VGB_CUDA(cudaMemcpyAsync(Xc.p, X.p, nx * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            NRResult r = nr_loop(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, dv.floor_abstol, k, o, tran_itl, s);
-            total_nr += r.iterations;
-            if (!r.converged) nr_fail_count++;
-            launch_status_reset(c->d_status.p, s);
-            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, dv.floor_abstol, reltol, vntol,
-                         c->d_csr_vals.p, c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
-            launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
-            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, s);
-            const int slot = ((i + 1) % 4);
-            commit_kernel<<<grid_x, tb, 0, s>>>(n_nodes, nx, n_unk, n_ext, n_vsrc, 1, 1, 0, Xc.p, X.p,
-                                                 c->d_Q.p, Qp.p, dQn.p, dQp.p, Qp2.p, hist.p + (size_t)slot * n_nodes,
-                                                 Vmax.p, c->d_maxc.p, hmaxc.p, Ivs.p,
-                                                 Vout.p + (size_t)(i + 1) * n_ext, Iout.p + (size_t)(i + 1) * nvo);
-            tout[i + 1] = t_next;
-            // sources (2), status reset, vsource current, dQ/dt, commit
-            c->launches += (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0) + 4;
-            fixed_i++;
-            accepted_now++;
+        } else {
+            const double* h0 = hist.p + (size_t)p.slot[0] * n_nodes;
+            const double* h1 = hist.p + (size_t)p.slot[1] * n_nodes;
+            const double* h2 = hist.p + (size_t)p.slot[2] * n_nodes;
+            predict_kernel<<<grid_x, tb, 0, s>>>(n_nodes, nx, n_unk, X.p, Xc.p, Vpred.p, h0, h1, h2, p.pa[0],
+                                                  p.pa[1], p.pa[2], p.can_predict, hmaxc.p, reltol, abstol, floor_.p);
+            c->launches += 1;
         }
-        step_idx = fixed_i + 1;
-        if (fixed_i >= fixed_n) done = true;
-    } else {
-        const int max_order = 2, max_history = 4;
-        while (t < t_stop && step_idx < max_steps && !limit_hit()) {
-            const double dt_cur = dt;
-            Coeffs k;
-            double err_integ;
-            const double inv = 1.0 / dt_cur;
-            if (method == 0) { k.c0 = inv; k.c1 = -inv; err_integ = -0.5; }
-            else if (method == 1) { k.c0 = 2 * inv; k.c1 = -2 * inv; k.d1 = -1.0; err_integ = 1.0 / 24.0; }
-            else {
-                const double dt_prev = dt_hist[0];
-                const double w = dt_prev > 0 ? dt_cur / dt_prev : 1.0;
-                const double wp1 = 1.0 + w;
-                k.c0 = (1.0 + 2.0 * w) / (wp1 * dt_cur);
-                k.c1 = -wp1 / dt_cur;
-                k.c2 = (w * w) / (wp1 * dt_cur);
-                err_integ = -2.0 / 9.0;
-            }
-            const double t_next = t + dt_cur;
-            launch_eval_sources(c->vsrc_wave, n_vsrc, t_next, vs.p, s);
-            launch_eval_sources(c->isrc_wave, c->n_isrc, t_next, is.p, s);
-            const bool can_predict = warmup_count >= warmup_steps && history_count >= 2;
-            const Pred pr = predictor_coeffs(dt_hist, history_count, dt_cur, max_order);
-            const int order = std::max(std::min(history_count - 1, max_order), 0);
-            double a0 = pr.a[0], a1 = order >= 1 ? pr.a[1] : 0.0, a2 = order >= 2 ? pr.a[2] : 0.0;
-            const double* h0 = hist.p + (size_t)((head + 0) % 4) * n_nodes;
-            const double* h1 = hist.p + (size_t)((head + 1) % 4) * n_nodes;
-            const double* h2 = hist.p + (size_t)((head + 2) % 4) * n_nodes;
-            predict_kernel<<<grid_x, tb, 0, s>>>(n_nodes, nx, n_unk, X.p, Xc.p, Vpred.p, h0, h1, h2, a0, a1, a2,
-                                                  can_predict ? 1 : 0, hmaxc.p, reltol, abstol, floor_.p);
-            double ramp = gshunt_steps > 0 ? std::min(std::max((double)step_idx / gshunt_steps, 0.0), 1.0) : 1.0;
-            k.gshunt = gshunt_init + ramp * (gshunt_target - gshunt_init);
-            NRResult r = nr_loop(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, floor_.p, k, o, tran_itl, s);
-            total_nr += r.iterations;
-            // post-NR rebuild (solver_factories.py:689-713) + LTE
-            launch_status_reset(c->d_status.p, s);
-            build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, floor_.p, reltol, vntol, c->d_csr_vals.p,
-                         c->d_f.p, c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
-            launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
-            launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, s);
-            const double kl = err_integ / (err_integ - pr.err);
-            lte_kernel<<<ceil_div(n_nodes, tb), tb, 0, s>>>(n_nodes, Xc.p, Vpred.p, Vmax.p, kl, reltol, abstol,
+        NRResult r = nr_loop(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, fl, k, o, tran_itl, s);
+        // post-NR rebuild (solver_factories.py:689-713), LTE
+        launch_status_reset(c->d_status.p, s);
+        build_system(*c, Xc.p, vs.p, is.p, Qp.p, dQp.p, Qp2.p, fl, reltol, vntol, c->d_csr_vals.p, c->d_f.p,
+                     c->d_Q.p, c->d_maxc.p, c->d_fres.p, s);
+        launch_vsrc_current(c->d_fres.p, c->d_vsrc_p.p, Ivs.p, n_vsrc, s);
+        launch_dqdt(c->d_Q.p, Qp.p, dQp.p, Qp2.p, c->d_coeffs.p, dQn.p, n_unk, s);
+        double lte_norm = 0.0;
+        if (!fixed) {
+            lte_kernel<<<ceil_div(n_nodes, tb), tb, 0, s>>>(n_nodes, Xc.p, Vpred.p, Vmax.p, p.kl, reltol, abstol,
                                                              c->d_status.p);
             VGB_CUDA(cudaMemcpyAsync(c->h_status, c->d_status.p, sizeof(NRStatus), cudaMemcpyDeviceToHost, s));
             VGB_CUDA(cudaStreamSynchronize(s));
-            const double lte_norm = bits_to_double(c->h_status->lte_norm);
-            const int lte_order = std::min(history_count - 1, max_order);
-            double factor = std::pow(lte_ratio / std::max(lte_norm, 1e-10), 1.0 / (lte_order + 1));
-            factor = std::min(std::max(factor, 0.1), grow_factor);
-            const double dt_lte = dt_cur * factor;
-
-            const bool nr_failed = !r.converged;
-            if (nr_failed) nr_fail_count++;
-            const bool at_min_dt = dt_cur <= min_dt;
-            const bool nr_failed_at_min = nr_failed && at_min_dt;
-            const bool lte_reject = (dt_cur / dt_lte > redo_factor) && can_predict && r.converged;
-            const bool nr_reject = nr_failed && !at_min_dt;
-            const bool force_accept = consecutive >= max_consec;
-            const bool reject = (lte_reject || nr_reject) && !force_accept;
-            const bool accept = !reject;
-            consecutive = accept ? 0 : (lte_reject ? consecutive + 1 : consecutive);
-            const double dt_from_lte = can_predict ? dt_lte : dt_cur;
-            const double dt_nr_halved = std::max(dt_cur * tran_ft, min_dt);
-            const double last_good = history_count > 0 ? dt_hist[0] : min_dt * 16.0;
-            const double dt_recovery = std::max(last_good / 8.0, min_dt * 2.0);
-            double new_dt = nr_failed ? (at_min_dt ? dt_recovery : dt_nr_halved) : dt_from_lte;
-            new_dt = std::min(std::max(new_dt, min_dt), max_dt);
-            new_dt = std::min(new_dt, t_stop - t_next);
-
-            const bool use_new = accept && !nr_failed_at_min;
-            int new_head = head;
-            if (use_new) new_head = (head + 3) % 4;
-            commit_kernel<<<grid_x, tb, 0, s>>>(
-                n_nodes, nx, n_unk, n_ext, n_vsrc, use_new ? 1 : 0, accept ? 1 : 0, nr_failed_at_min ? 1 : 0,
-                Xc.p, X.p, c->d_Q.p, Qp.p, dQn.p, dQp.p, Qp2.p, hist.p + (size_t)new_head * n_nodes, Vmax.p,
-                c->d_maxc.p, hmaxc.p, Ivs.p, Vout.p + (size_t)step_idx * n_ext, Iout.p + (size_t)step_idx * nvo);
-            // sources, predictor, status reset, vsource current, dQ/dt, LTE, commit
-            c->launches += (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0) + 6;
-            if (use_new) {
-                head = new_head;
-                for (int q = 3; q > 0; --q) dt_hist[q] = dt_hist[q - 1];
-                dt_hist[0] = dt_cur;
-                history_count = std::min(history_count + 1, max_history);
-                warmup_count++;
-            }
-            if (accept) {
-                tout[step_idx] = t_next;
-                t = t_next;
-                step_idx++;
-                accepted_now++;
-                min_dt_used = std::min(min_dt_used, dt_cur);
-                max_dt_used = std::max(max_dt_used, dt_cur);
-            }
-            if (reject) rejected++;
-            dt = new_dt;
+            lte_norm = bits_to_double(c->h_status->lte_norm);
+            c->launches += 1;
         }
-        if (!(t < t_stop && step_idx < max_steps)) done = true;
+        const StepCommit m = ctl_finish(*this, p, lte_norm, r.iterations, r.converged, tout.data());
+        commit_kernel<<<grid_x, tb, 0, s>>>(
+            n_nodes, nx, n_unk, n_ext, n_vsrc, m.use_new, m.accept, m.zero_current, Xc.p, X.p, c->d_Q.p, Qp.p,
+            dQn.p, dQp.p, Qp2.p, hist.p + (size_t)m.slot * n_nodes, Vmax.p, c->d_maxc.p, hmaxc.p, Ivs.p,
+            Vout.p + (size_t)m.row * n_ext, Iout.p + (size_t)m.row * nvo);
+        // sources, status reset, vsource current, dQ/dt, commit
+        c->launches += (n_vsrc ? 1 : 0) + (c->n_isrc ? 1 : 0) + 4;
+        accepted_now += m.accept;
     }
     VGB_CUDA(cudaEventRecord(ev1, s));
     VGB_CUDA(cudaEventSynchronize(ev1));
