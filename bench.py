@@ -275,6 +275,9 @@ def run_gb300(args):
         eng, nstats, depth = make_engine(args.gates, max_steps=W + K + prof_steps + 4, precision=args.precision,
                                          refine=args.refine)
     dev = eng.device
+    # the CUDA-graph step loop is the product path; ncu cannot profile the kernel nodes of a
+    # graph with conditional nodes, so profiling runs use the host-driven loop (same kernels)
+    dev.set_transient_graph(args.step_loop == "graph")
     info = dev.solver_info()
     tuning = eng.tune()["tuning"] if args.autotune == "on" else dev.tuning()
     t0 = time.perf_counter()
@@ -380,7 +383,8 @@ def run_gb300(args):
            "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32lu",
            "data": "synthetic (seeded generator)",
-           "config": {**workload_config(args, ring, nstats, depth, info, world, dc_s, eng), "tuning": tuning},
+           "config": {**workload_config(args, ring, nstats, depth, info, world, dc_s, eng), "tuning": tuning,
+                      "step_loop": "cuda_graph" if args.step_loop == "graph" else "host_driven"},
            "newton_iters_per_s": nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "instances": n_inst, "solves_per_s": n_inst * nr_iters / (dev_ms * 1e-3) if dev_ms > 0 else 0.0,
            "newton_iters": nr_iters, "rejected_steps": rejected, "host_wall_ms_per_step": wall_s * 1e3 / K,
@@ -724,6 +728,8 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")
     ap.add_argument("--max-transistors", type=int, default=SERVING["network_transistors"][1],
                     help="serving: largest gate network in the stream")
+    ap.add_argument("--step-loop", choices=["graph", "host"], default="graph",
+                    help="transient step loop: one CUDA graph (default) or host-driven (for ncu: same kernels)")
     ap.add_argument("--serving-graph", choices=["on", "off"], default="off",
                     help="serving: served sessions run the CUDA-graph step loop (default: host-driven loop)")
     ap.add_argument("--autotune", choices=["on", "off"], default="on",
