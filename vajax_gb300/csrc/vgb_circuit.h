@@ -159,7 +159,6 @@ struct SparseLU {
     DevBuf<int> d_f_col, d_f_arow, d_f_diag_e, d_l_col, d_l_arow, d_l_diag_e, d_l_ptr, d_l_e, d_l_x;
     DevBuf<int> d_pre_ptr, d_pre_e, d_pre_f;
     DevBuf<int> d_counters;  // work counters
-    int epoch = 0;
 };
 
 struct NRStatus {

@@ -25,6 +25,7 @@
 //
 // Front storage is dense column-major, F[i + j * m], in one pool.
 #include <cuda/atomic>
+#include <mutex>
 
 #include "vgb_kernels.cuh"
 
@@ -793,13 +794,12 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
 // ---------------------------------------------------------------------------
 
 int sm_count() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
+    static const int sms = [] {  // initialised once, thread-safe
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        sms = std::max(1, sms);
-    }
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return std::max(1, n);
+    }();
     return sms;
 }
 
@@ -873,9 +873,12 @@ static size_t mf_solve_smem(const SparseLU& L) {
 }
 
 // Opt the solve kernels in to more than 48 KB of dynamic shared memory (once per size).
+// Circuits on several host threads (the server) may get here at once: the cache is locked.
 template <typename T>
 static void mf_solve_attributes(size_t smem) {
+    static std::mutex mu;
     static size_t smem_set[2] = {0, 0};
+    std::lock_guard<std::mutex> lock(mu);
     size_t& cur = smem_set[sizeof(T) == 4 ? 0 : 1];
     if (smem > 48 * 1024 && smem > cur) {
         VGB_REQUIRE(smem <= 200 * 1024, "front too large for the solve kernels' shared memory");
