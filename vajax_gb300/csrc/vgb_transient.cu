@@ -447,6 +447,7 @@ struct TranSession {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int graph_epoch = -1;
+    bool graph_unavailable = false;  // capture or instantiation failed once: host-driven loop from then on
     long long per_iter_launches = 0, per_step_launches = 0;
 
     void setup(Circuit* cc, const double* cfg, const double* X0, const double* Q0, const double* I0,
@@ -709,7 +710,19 @@ void TranSession::setup(Circuit* cc, const double* cfg, const double* X0, const 
 // Run until max_accepted more steps are accepted (0 = to the end of the run).
 int TranSession::advance(int max_accepted) {
     if (done) return 0;
-    if (c->tran_graph && !c->profile) return advance_graph(max_accepted);
+    if (c->tran_graph && !c->profile && !graph_unavailable) {
+        try {
+            return advance_graph(max_accepted);
+        } catch (const Error&) {
+            // a failure while building the graph (no executable graph yet) leaves the device
+            // untouched: run the same kernels from the host loop instead; a failure during a
+            // run of the graph is the run's error
+            if (gexec) throw;
+            graph_unavailable = true;
+            (void)cudaGetLastError();  // clear the (non-sticky) error of the failed graph call
+            c->last_error.clear();
+        }
+    }
     cudaStream_t s = c->stream;
     const int n_nodes = c->n_nodes, n_unk = c->n_unk, n_vsrc = c->n_vsrc;
     const int nx = n_x();
