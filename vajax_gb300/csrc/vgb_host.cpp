@@ -237,11 +237,24 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
     for (int v = 0; v < n; ++v)
         if (state[v] == 0) pq.push({(int)adj[v].size(), v});
     std::vector<int> tmp;
+    int live = 0;
+    for (int v = 0; v < n; ++v) live += state[v] == 0;
     while (!pq.empty()) {
         auto [d, v] = pq.top();
         pq.pop();
         if (state[v] != 0 || d != (int)adj[v].size()) continue;
+        if (d == live - 1) {
+            // the smallest degree is the largest possible: the live vertices form a
+            // clique, which the (degree, index) queue would eliminate in index order
+            for (int u = 0; u < n; ++u)
+                if (state[u] == 0) {
+                    state[u] = 1;
+                    order.push_back(u);
+                }
+            break;
+        }
         state[v] = 1;
+        --live;
         order.push_back(v);
         std::vector<int> nb;
         nb.swap(adj[v]);
