@@ -9,6 +9,11 @@
 #include <numeric>
 #include <queue>
 #include <unordered_map>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 
 #include "vgb_circuit.h"
 
@@ -220,6 +225,68 @@ void build_pattern(Circuit& c) {
 // Minimum-degree ordering on a symmetric pattern.  Rows whose degree is far
 // above the average (supply rails) are set aside and ordered last, the usual
 // dense-row rule of approximate-minimum-degree codes.
+// Runs f(i) for i in [0, n) on a few worker threads (the calling thread takes
+// part); used for the independent neighbour merges of one elimination.
+class MergePool {
+public:
+    explicit MergePool(int threads) {
+        for (int t = 1; t < threads; ++t) workers_.emplace_back([this] { work(); });
+    }
+    ~MergePool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto& w : workers_) w.join();
+    }
+    int size() const { return (int)workers_.size() + 1; }
+    template <class F>
+    void run(int n, F&& f) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = [&f](int i) { f(i); };
+            n_ = n;
+            next_.store(0);
+            pending_ = (int)workers_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [this] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void drain() {
+        for (int i = next_.fetch_add(1); i < n_; i = next_.fetch_add(1)) job_(i);
+    }
+    void work() {
+        long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+            }
+            drain();
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::function<void(int)> job_;
+    std::atomic<int> next_{0};
+    int n_ = 0, pending_ = 0;
+    long long gen_ = 0;
+    bool stop_ = false;
+};
+
 static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> adj) {
     std::vector<int> order;
     order.reserve(n);
@@ -234,6 +301,8 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
     }
     using P = std::pair<int, int>;
     std::priority_queue<P, std::vector<P>, std::greater<P>> pq;
+    constexpr int MERGE_PAR_MIN = 96;  // neighbours of one elimination worth a parallel merge
+    MergePool pool(std::max(1, std::min(8, (int)std::thread::hardware_concurrency())));
     for (int v = 0; v < n; ++v)
         if (state[v] == 0) pq.push({(int)adj[v].size(), v});
     std::vector<int> tmp;
@@ -258,14 +327,24 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
         order.push_back(v);
         std::vector<int> nb;
         nb.swap(adj[v]);
-        for (int u : nb) {
+        // adj[u] := adj[u] | nb minus {u, v} for every neighbour u; the merges are
+        // independent, so large neighbourhoods are merged on the pool
+        auto merge = [&](int u, std::vector<int>& buf) {
             auto& au = adj[u];
-            tmp.clear();
-            std::set_union(au.begin(), au.end(), nb.begin(), nb.end(), std::back_inserter(tmp));
-            tmp.erase(std::remove_if(tmp.begin(), tmp.end(), [&](int w) { return w == u || w == v; }), tmp.end());
-            au.swap(tmp);
-            pq.push({(int)au.size(), u});
+            buf.clear();
+            std::set_union(au.begin(), au.end(), nb.begin(), nb.end(), std::back_inserter(buf));
+            buf.erase(std::remove_if(buf.begin(), buf.end(), [&](int w) { return w == u || w == v; }), buf.end());
+            au.swap(buf);
+        };
+        if ((int)nb.size() >= MERGE_PAR_MIN && pool.size() > 1) {
+            pool.run((int)nb.size(), [&](int q) {
+                thread_local std::vector<int> buf;
+                merge(nb[q], buf);
+            });
+        } else {
+            for (int u : nb) merge(u, tmp);
         }
+        for (int u : nb) pq.push({(int)adj[u].size(), u});
     }
     for (int v = 0; v < n; ++v)
         if (state[v] == 2) order.push_back(v);
