@@ -406,13 +406,6 @@ __global__ void tran_commit_kernel(int n_nodes, int n_x, int n_unk, int n_ext, i
                        Vout + (size_t)m.row * n_ext, Iout + (size_t)m.row * nvo);
 }
 
-// Arms a run of the step graph: at most `limit` accepted steps (0: no limit).
-__global__ void tran_arm_kernel(TranDev* T, int limit) {
-    T->limit = limit;
-    T->accepted_now = 0;
-    T->guard = 0;
-    T->stop_reason = TRAN_STOP_NONE;
-}
 
 // ---------------------------------------------------------------------------
 // Resumable transient session: configuration, device state and the host-side
