@@ -47,7 +47,7 @@ def _emulator():
     return lib, f64p
 
 
-def _case(circuit, c0):
+def _case(circuit, c0, factor_ctas=None):
     import scipy.sparse as sp
     import scipy.sparse.linalg as spl
 
@@ -57,6 +57,8 @@ def _case(circuit, c0):
     eng = CircuitEngine(circuit).parse()
     rc = eng.rc
     dc = DeviceCircuit(rc, device=False)
+    if factor_ctas is not None:  # the autotuner re-schedules the task list for this many CTAs per SM
+        dc.set_tuning("factor_ctas_per_sm", factor_ctas)
     S = OracleSystem(rc, {g.model: load_model(g.model) for g in rc.groups})
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
     X0[: rc.n_nodes] = eng.initial_guess()
@@ -87,3 +89,9 @@ def test_task_list_emulation_matches_sparse_lu(name):
     info = _case(c, c0=1e12)
     if name == "gates8000":
         assert info["max_front"] > 4 * 32  # several pivot and contribution tiles per large front
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 3])
+def test_rescheduled_task_lists_stay_valid(ctas):
+    """The list schedule recomputed for other CTA counts is still a valid order."""
+    _case(random_gate_network(n_gates=4000, seed=2)[0], c0=1e12, factor_ctas=ctas)
