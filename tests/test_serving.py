@@ -28,6 +28,44 @@ def test_job_keys_group_same_patterns():
     assert keys[0] == keys[1] != keys[2]
 
 
+def test_reservation_sized_before_device_allocation(monkeypatch):
+    # prepare() analyses once; the server's hook sees the analysed handle before finalize
+    from vajax_gb300 import runtime
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions
+    from vajax_gb300.serving import estimate_footprint
+    calls = []
+
+    def fake_finalize(self):
+        calls.append(("finalize", self.h is not None))
+        self.finalized = True
+
+    monkeypatch.setattr(runtime.DeviceCircuit, "finalize", fake_finalize)
+    job = _net_job(0, 3)
+    eng = CircuitEngine(job.make_circuit(), SimulationOptions(**job.options))
+    eng.parse()
+
+    def hook(dev):
+        calls.append(("sized", estimate_footprint(dev.solver_info())))
+
+    eng.prepare(t_stop=job.t_stop, dt=job.dt, max_steps=job.max_steps, on_analyzed=hook)
+    assert [c[0] for c in calls] == ["sized", "finalize"]
+    assert calls[0][1] > 0 and calls[1][1]
+    eng.device.close()
+
+    # a hook that refuses the job leaves nothing allocated and no handle open
+    seen = []
+
+    def refuse(dev):
+        seen.append(dev)
+        raise MemoryError("over budget")
+
+    eng2 = CircuitEngine(job.make_circuit(), SimulationOptions(**job.options))
+    with pytest.raises(MemoryError):
+        eng2.prepare(t_stop=job.t_stop, dt=job.dt, max_steps=job.max_steps, on_analyzed=refuse)
+    assert eng2.device is None and seen[0].h is None
+    assert [c[0] for c in calls] == ["sized", "finalize"]
+
+
 @pytest.mark.gpu
 def test_served_results_match_alone(cuda):
     from vajax_gb300.serving import serve

@@ -147,8 +147,13 @@ class CircuitEngine:
 
     def prepare(self, *, t_stop: Optional[float] = None, dt: Optional[float] = None,
                 adaptive_config: Optional[AdaptiveConfig] = None, max_steps: Optional[int] = None,
-                temperature: Optional[float] = None):
-        """t_stop / dt default to the netlist's first ``tran`` analysis (stop=, step=)."""
+                temperature: Optional[float] = None, on_analyzed=None):
+        """t_stop / dt default to the netlist's first ``tran`` analysis (stop=, step=).
+
+        ``on_analyzed(device_circuit)``, if given, is called once the host
+        analysis is done and before any device memory is allocated: a server
+        sizes its HBM reservation there from ``solver_info()`` without
+        analysing the circuit twice."""
         from vajax_gb300.runtime import DeviceCircuit
         if t_stop is None or dt is None:
             from vajax_gb300.netlist import evaluate
@@ -170,8 +175,16 @@ class CircuitEngine:
             prec = {"fp64": 0, "fp32": 1, "mixed": 1}[self.precision]
             if self.rc.n_nodes - 1 + len(self.rc.vsources) <= DENSE_MAX:
                 prec = 2  # small circuits: dense LU with partial pivoting, as the reference's dense path
-            self.device = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 3),
-                                        gmin=self.options.gmin)
+            dev = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 3),
+                                gmin=self.options.gmin, device=False)
+            try:
+                if on_analyzed is not None:
+                    on_analyzed(dev)
+                dev.finalize()
+            except BaseException:
+                dev.close()
+                raise
+            self.device = dev
             if self.options.autotune != "off":
                 self.tune()
         self._prepared = True

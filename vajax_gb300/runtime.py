@@ -35,12 +35,16 @@ def _ptr(t) -> Optional[int]:
 
 class DeviceCircuit:
     """``device=False`` stops after the host-side analysis (pattern, maps,
-    symbolic factorisation), which needs no GPU."""
+    symbolic factorisation), which needs no GPU; ``finalize()`` later allocates
+    and uploads the device side of the same handle."""
 
     def __init__(self, rc: ResolvedCircuit, precision: int = 0, refine_sweeps: int = 3, gmin: float = 1e-12,
                  device: bool = True):
         self.rc = rc
         self.precision = precision
+        self._refine_sweeps = refine_sweeps
+        self._gmin = gmin
+        self.finalized = False
         self.lib = _lib.load()
         h = C.c_void_p()
         vp_ = np.ascontiguousarray(rc.vsrc_p, np.int32)
@@ -76,7 +80,7 @@ class DeviceCircuit:
                 self._check(self.lib.vgb_circuit_set_noi_nodes(h, len(nn), _ip(nn)))
             self._check(self.lib.vgb_circuit_analyze(h))
             if device:
-                self._check(self.lib.vgb_circuit_finalize(h, gmin, precision, refine_sweeps))
+                self.finalize()
         except Exception:
             self.lib.vgb_circuit_destroy(h)
             self.h = None
@@ -91,6 +95,14 @@ class DeviceCircuit:
 
     def _check(self, code):
         _lib.check(code, self.h)
+
+    def finalize(self):
+        """Allocate and upload the device side after a ``device=False``
+        construction (the analysis is not repeated)."""
+        if self.finalized:
+            raise RuntimeError("circuit already finalized")
+        self._check(self.lib.vgb_circuit_finalize(self.h, self._gmin, self.precision, self._refine_sweeps))
+        self.finalized = True
 
     def set_shunt_ref(self, ref=None):
         """ref: torch CUDA float64 tensor [n_nodes-1] the gshunt term pulls towards, or None (ground)."""

@@ -94,7 +94,6 @@ def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, r
     batched circuit.  Fills each job's result; returns the reserved bytes."""
     from vajax_gb300.corners import concat_circuits
     from vajax_gb300.engine import CircuitEngine, SimulationOptions, TransientResult
-    from vajax_gb300.runtime import DeviceCircuit
     lead = jobs[0]
     circuits = [j.circuit if j.circuit is not None else j.make_circuit() for j in jobs]
     single = len(jobs) == 1
@@ -104,12 +103,16 @@ def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, r
         opts["ic"] = {f"j{k}.{n}": v for k in range(len(jobs)) for n, v in lead.options["ic"].items()}
     eng = CircuitEngine(circuit, SimulationOptions(**opts), precision=precision)
     eng.parse()
-    host = DeviceCircuit(eng.rc, device=False)
-    footprint = estimate_footprint(host.solver_info(), precision)
-    host.close()
-    if reserve is not None:
-        reserve(footprint)
-    eng.prepare(t_stop=lead.t_stop, dt=lead.dt, max_steps=lead.max_steps)
+    sized = [0]
+
+    def admit(dev):
+        # the reservation is sized from the host analysis, before any device allocation
+        sized[0] = estimate_footprint(dev.solver_info(), precision)
+        if reserve is not None:
+            reserve(sized[0])
+
+    eng.prepare(t_stop=lead.t_stop, dt=lead.dt, max_steps=lead.max_steps, on_analyzed=admit)
+    footprint = sized[0]
     eng.device.set_transient_graph(transient_graph)
     t_adm = time.perf_counter()
     try:
