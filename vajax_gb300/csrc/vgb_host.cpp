@@ -287,6 +287,109 @@ private:
     bool stop_ = false;
 };
 
+// The dense tail of the elimination: once the live graph is small and dense,
+// each vertex's neighbour set is a bit row over the live vertices, numbered in
+// increasing index order so that the (degree, index) rule picks the same
+// vertex, and a merge is a word-wise OR.  Rows are renumbered narrower each
+// time the live count halves.  Appends to `order` exactly what the list form
+// would.
+constexpr int MD_IDX_BITS = 14;
+constexpr int BITSET_MAX = 1 << MD_IDX_BITS;  // live vertices of the bit-row form (rows of at most 32 MB)
+
+static void min_degree_bitset_tail(int n, std::vector<std::vector<int>>& adj, std::vector<char>& state, int live,
+                                   std::vector<int>& order) {
+    // key = degree << 14 | local index (both below 2^14): the smallest key is the
+    // (degree, index) rule's pick
+    constexpr int IDX_BITS = MD_IDX_BITS;
+    constexpr uint32_t GONE = 0xffffffffu;
+    std::vector<int> glob;
+    glob.reserve(live);
+    std::vector<int> loc(n, -1);
+    for (int u = 0; u < n; ++u)
+        if (state[u] == 0) {
+            loc[u] = (int)glob.size();
+            glob.push_back(u);
+        }
+    int L = (int)glob.size(), W = (L + 63) / 64;
+    std::vector<uint64_t> rows((size_t)L * W, 0);
+    std::vector<uint32_t> key(L);
+    for (int a = 0; a < L; ++a) {
+        uint64_t* r = rows.data() + (size_t)a * W;
+        for (int u : adj[glob[a]]) {
+            const int b = loc[u];
+            r[b >> 6] |= 1ull << (b & 63);
+        }
+        key[a] = ((uint32_t)adj[glob[a]].size() << IDX_BITS) | (uint32_t)a;
+        std::vector<int>().swap(adj[glob[a]]);
+    }
+    std::vector<int> nb;
+    while (live > 0) {
+        if (2 * live <= L && live >= 128) {
+            std::vector<int> nl(L, -1);
+            int L2 = 0;
+            for (int b = 0; b < L; ++b)
+                if (key[b] != GONE) nl[b] = L2++;
+            const int W2 = (L2 + 63) / 64;
+            std::vector<uint64_t> r2((size_t)L2 * W2, 0);
+            std::vector<int> g2(L2);
+            std::vector<uint32_t> k2(L2);
+            for (int b = 0; b < L; ++b) {
+                if (key[b] == GONE) continue;
+                const uint64_t* rb = rows.data() + (size_t)b * W;
+                uint64_t* o = r2.data() + (size_t)nl[b] * W2;
+                for (int w = 0; w < W; ++w)
+                    for (uint64_t m = rb[w]; m; m &= m - 1) {
+                        const int x = nl[w * 64 + __builtin_ctzll(m)];
+                        o[x >> 6] |= 1ull << (x & 63);
+                    }
+                g2[nl[b]] = glob[b];
+                k2[nl[b]] = (key[b] >> IDX_BITS << IDX_BITS) | (uint32_t)nl[b];
+            }
+            rows.swap(r2);
+            glob.swap(g2);
+            key.swap(k2);
+            L = L2;
+            W = W2;
+        }
+        uint32_t kmin = GONE;
+        for (int b = 0; b < L; ++b) kmin = std::min(kmin, key[b]);
+        const int a = (int)(kmin & ((1u << IDX_BITS) - 1)), d = (int)(kmin >> IDX_BITS);
+        if (d == live - 1) {
+            for (int b = 0; b < L; ++b)
+                if (key[b] != GONE) order.push_back(glob[b]);
+            break;
+        }
+        key[a] = GONE;
+        --live;
+        order.push_back(glob[a]);
+        const uint64_t* ra = rows.data() + (size_t)a * W;
+        int wlo = 0, whi = W;
+        while (wlo < W && !ra[wlo]) ++wlo;
+        while (whi > wlo && !ra[whi - 1]) --whi;
+        nb.clear();
+        for (int w = wlo; w < whi; ++w)
+            for (uint64_t m = ra[w]; m; m &= m - 1) nb.push_back(w * 64 + __builtin_ctzll(m));
+        // row b := row b | row a minus {a, b}.  a is in row b and b is in row a,
+        // so the new degree is deg(b) + |row a \ row b| - 2.
+        for (int b : nb) {
+            uint64_t* rb = rows.data() + (size_t)b * W;
+            int c = (int)(key[b] >> IDX_BITS);
+            for (int w = wlo; w < whi; ++w) {
+                const uint64_t x = ra[w] & ~rb[w];
+                if (x) {
+                    c += __builtin_popcountll(x);
+                    rb[w] |= x;
+                }
+            }
+            rb[b >> 6] &= ~(1ull << (b & 63));
+            rb[a >> 6] &= ~(1ull << (a & 63));
+            key[b] = ((uint32_t)(c - 2) << IDX_BITS) | (uint32_t)b;
+        }
+    }
+    for (int u = 0; u < n; ++u)
+        if (state[u] == 0) state[u] = 1;
+}
+
 static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> adj) {
     std::vector<int> order;
     order.reserve(n);
@@ -307,8 +410,18 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
         if (state[v] == 0) pq.push({(int)adj[v].size(), v});
     std::vector<int> tmp;
     int live = 0;
-    for (int v = 0; v < n; ++v) live += state[v] == 0;
+    long long tot = 0;  // sum of the live vertices' degrees
+    for (int v = 0; v < n; ++v)
+        if (state[v] == 0) {
+            ++live;
+            tot += (long long)adj[v].size();
+        }
     while (!pq.empty()) {
+        if (live <= BITSET_MAX && tot * 64 >= (long long)live * live) {
+            // bit rows are now smaller than the lists and far faster to merge
+            min_degree_bitset_tail(n, adj, state, live, order);
+            break;
+        }
         auto [d, v] = pq.top();
         pq.pop();
         if (state[v] != 0 || d != (int)adj[v].size()) continue;
@@ -327,6 +440,8 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
         order.push_back(v);
         std::vector<int> nb;
         nb.swap(adj[v]);
+        tot -= (long long)nb.size();
+        for (int u : nb) tot -= (long long)adj[u].size();
         // adj[u] := adj[u] | nb minus {u, v} for every neighbour u; the merges are
         // independent, so large neighbourhoods are merged on the pool
         auto merge = [&](int u, std::vector<int>& buf) {
@@ -344,7 +459,10 @@ static std::vector<int> min_degree_order(int n, std::vector<std::vector<int>> ad
         } else {
             for (int u : nb) merge(u, tmp);
         }
-        for (int u : nb) pq.push({(int)adj[u].size(), u});
+        for (int u : nb) {
+            tot += (long long)adj[u].size();
+            pq.push({(int)adj[u].size(), u});
+        }
     }
     for (int v = 0; v < n; ++v)
         if (state[v] == 2) order.push_back(v);
