@@ -187,7 +187,6 @@ struct Circuit {
 
     // CSR pattern of the augmented Jacobian (reference layout)
     std::vector<int> indptr, indices;
-    std::vector<long long> unique_linear;
     int nnz = 0;
     std::vector<int> diag_pos;
     std::vector<int> vs_pos[4];      // b_p, b_n, bt_p, bt_n

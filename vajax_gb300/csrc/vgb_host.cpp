@@ -19,55 +19,64 @@
 
 namespace vgb {
 
-static int find_pos(const std::vector<long long>& ul, long long key) {
-    auto it = std::lower_bound(ul.begin(), ul.end(), key);
-    if (it == ul.end() || *it != key) return -1;
-    return (int)(it - ul.begin());
+// Position of entry (r, col) in the CSR pattern, or -1.
+static int csr_find(const Circuit& c, int r, int col) {
+    const int* lo = c.indices.data() + c.indptr[r];
+    const int* hi = c.indices.data() + c.indptr[r + 1];
+    const int* it = std::lower_bound(lo, hi, col);
+    return (it == hi || *it != col) ? -1 : (int)(it - c.indices.data());
 }
 
 void build_pattern(Circuit& c) {
     const int n_unk = c.n_unk, n_aug = c.n_aug;
-    const long long N = n_aug;
-    std::vector<long long> lin;
-    size_t est = (size_t)n_unk + 4 * (size_t)c.n_vsrc;
-    for (auto& g : c.groups) est += (size_t)g.n_dev * g.nj;
-    lin.reserve(est);
+    // The reference sorts and de-duplicates the linear ids row * n + col of all
+    // COO entries (full_mna.py:421-513).  Bucketing the entries by row and
+    // sorting each row's columns gives the same sorted unique set in linear
+    // time plus short per-row sorts.
     bool masked = false;
-    // device Jacobian entries (mna_builder.py:44-118, masked pairs -> (0,0) as in mna.py:mask_coo_matrix)
-    for (auto& g : c.groups) {
-        for (int i = 0; i < g.n_dev; ++i) {
-            for (int k = 0; k < g.nj; ++k) {
-                int r = g.node_map[(size_t)g.me->jrow[k] * g.n_dev + i];
-                int col = g.node_map[(size_t)g.me->jcol[k] * g.n_dev + i];
-                if (r > 0 && col > 0) lin.push_back((long long)(r - 1) * N + (col - 1));
-                else masked = true;
-            }
+    auto for_each_entry = [&](auto&& emit) {
+        // device Jacobian entries (mna_builder.py:44-118, masked pairs -> (0,0) as in mna.py:mask_coo_matrix)
+        for (auto& g : c.groups)
+            for (int i = 0; i < g.n_dev; ++i)
+                for (int k = 0; k < g.nj; ++k) {
+                    const int r = g.node_map[(size_t)g.me->jrow[k] * g.n_dev + i];
+                    const int col = g.node_map[(size_t)g.me->jcol[k] * g.n_dev + i];
+                    if (r > 0 && col > 0) emit(r - 1, col - 1);
+                    else masked = true;
+                }
+        // vsource incidence (mna.py:build_vsource_incidence_coo); invalid terminals -> (0,0)
+        for (int k = 0; k < c.n_vsrc; ++k) {
+            const int p = c.vsrc_p[k], n = c.vsrc_n[k], b = n_unk + k;
+            if (p > 0) { emit(p - 1, b); emit(b, p - 1); }
+            else masked = true;
+            if (n > 0) { emit(n - 1, b); emit(b, n - 1); }
+            else masked = true;
         }
+        // node diagonals (mna.py:assemble_sparse_jacobian)
+        for (int i = 0; i < n_unk; ++i) emit(i, i);
+    };
+    std::vector<long long> rstart(n_aug + 1, 0);
+    for_each_entry([&](int r, int) { rstart[r + 1]++; });
+    const bool add_origin = masked && n_aug > 0;
+    if (add_origin) rstart[1]++;
+    for (int r = 0; r < n_aug; ++r) rstart[r + 1] += rstart[r];
+    std::vector<int> cols((size_t)rstart[n_aug]);
+    {
+        std::vector<long long> fill(rstart.begin(), rstart.end() - 1);
+        for_each_entry([&](int r, int col) { cols[fill[r]++] = col; });
+        if (add_origin) cols[fill[0]++] = 0;
     }
-    // vsource incidence (mna.py:build_vsource_incidence_coo); invalid terminals -> (0,0)
-    for (int k = 0; k < c.n_vsrc; ++k) {
-        int p = c.vsrc_p[k], n = c.vsrc_n[k];
-        long long b = n_unk + k;
-        if (p > 0) { lin.push_back((long long)(p - 1) * N + b); lin.push_back(b * N + (p - 1)); }
-        else masked = true;
-        if (n > 0) { lin.push_back((long long)(n - 1) * N + b); lin.push_back(b * N + (n - 1)); }
-        else masked = true;
-    }
-    // node diagonals (mna.py:assemble_sparse_jacobian)
-    for (int i = 0; i < n_unk; ++i) lin.push_back((long long)i * N + i);
-    if (masked && n_aug > 0) lin.push_back(0);
-    std::sort(lin.begin(), lin.end());
-    lin.erase(std::unique(lin.begin(), lin.end()), lin.end());
-    c.unique_linear = lin;
-    c.nnz = (int)lin.size();
     c.indptr.assign(n_aug + 1, 0);
-    c.indices.resize(c.nnz);
-    for (int e = 0; e < c.nnz; ++e) {
-        int r = (int)(lin[e] / N);
-        c.indices[e] = (int)(lin[e] % N);
-        c.indptr[r + 1]++;
+    c.indices.clear();
+    for (int r = 0; r < n_aug; ++r) {
+        auto lo = cols.begin() + rstart[r], hi = cols.begin() + rstart[r + 1];
+        std::sort(lo, hi);
+        hi = std::unique(lo, hi);
+        c.indices.insert(c.indices.end(), lo, hi);
+        c.indptr[r + 1] = (int)c.indices.size();
     }
-    for (int r = 0; r < n_aug; ++r) c.indptr[r + 1] += c.indptr[r];
+    c.nnz = (int)c.indices.size();
+    std::vector<int>().swap(cols);
 
     // stamp positions (mna_builder.py:126-160)
     long long base = 0;
@@ -79,7 +88,7 @@ void build_pattern(Circuit& c) {
             for (int k = 0; k < g.nj; ++k) {
                 int r = g.node_map[(size_t)g.me->jrow[k] * g.n_dev + i];
                 int col = g.node_map[(size_t)g.me->jcol[k] * g.n_dev + i];
-                if (r > 0 && col > 0) g.csr_pos[(size_t)i * g.nj + k] = find_pos(lin, (long long)(r - 1) * N + (col - 1));
+                if (r > 0 && col > 0) g.csr_pos[(size_t)i * g.nj + k] = csr_find(c, r - 1, col - 1);
             }
     }
     c.n_contrib = base;
@@ -87,14 +96,14 @@ void build_pattern(Circuit& c) {
 
     // diagonal positions (mna_builder.py:163-184): every node diagonal exists
     c.diag_pos.resize(n_unk);
-    for (int i = 0; i < n_unk; ++i) c.diag_pos[i] = find_pos(lin, (long long)i * N + i);
+    for (int i = 0; i < n_unk; ++i) c.diag_pos[i] = csr_find(c, i, i);
     // vsource positions (mna_builder.py:187-255)
     for (auto& v : c.vs_pos) v.assign(c.n_vsrc, -1);
     for (int k = 0; k < c.n_vsrc; ++k) {
         int p = c.vsrc_p[k], n = c.vsrc_n[k];
-        long long b = n_unk + k;
-        if (p > 0) { c.vs_pos[0][k] = find_pos(lin, (long long)(p - 1) * N + b); c.vs_pos[2][k] = find_pos(lin, b * N + (p - 1)); }
-        if (n > 0) { c.vs_pos[1][k] = find_pos(lin, (long long)(n - 1) * N + b); c.vs_pos[3][k] = find_pos(lin, b * N + (n - 1)); }
+        int b = n_unk + k;
+        if (p > 0) { c.vs_pos[0][k] = csr_find(c, p - 1, b); c.vs_pos[2][k] = csr_find(c, b, p - 1); }
+        if (n > 0) { c.vs_pos[1][k] = csr_find(c, n - 1, b); c.vs_pos[3][k] = csr_find(c, b, n - 1); }
     }
 
     // gather lists for the CSR values
