@@ -132,6 +132,47 @@ def is_noi_node(name: str) -> bool:
     return name.upper() == "NOI" or name == "node4"
 
 
+def _fill_instance_params(info, insts, vals: np.ndarray) -> None:
+    """Write each instance's parameters over the model defaults in
+    ``vals[n_params, n_dev]``; a name given twice in one instance keeps its
+    last value.  Instances with the same parameter items (the common case:
+    a netlist reuses a few device cards) are written as one column slice per
+    distinct set; mostly distinct sets (corners) are gathered per column."""
+    index_of: Dict[str, int] = {}
+
+    def columns(items):
+        per = {}
+        for pname, v in items:
+            k = index_of.get(pname)
+            if k is None:
+                k = index_of[pname] = info.param_index(pname)
+            per[k] = float(v)
+        return per
+
+    by_items: Optional[Dict[tuple, List[int]]] = {}
+    try:
+        for d, inst in enumerate(insts):
+            if inst.params:
+                by_items.setdefault(tuple(inst.params.items()), []).append(d)
+    except TypeError:  # an unhashable parameter value
+        by_items = None
+    if by_items is not None and len(by_items) * 8 <= len(insts):
+        for items, ds in by_items.items():
+            for k, v in columns(items).items():
+                vals[k, ds] = v
+        return
+    col_dev: List[List[int]] = [[] for _ in range(vals.shape[0])]
+    col_val: List[List[float]] = [[] for _ in range(vals.shape[0])]
+    for d, inst in enumerate(insts):
+        if inst.params:
+            for k, v in columns(inst.params.items()).items():
+                col_dev[k].append(d)
+                col_val[k].append(v)
+    for k, ds in enumerate(col_dev):
+        if ds:
+            vals[k, ds] = col_val[k]
+
+
 @dataclass
 class ResolvedCircuit:
     node_names: Dict[str, int]
@@ -223,23 +264,28 @@ class Circuit:
             insts = by_model[model]
             info = model_info(model)
             nn = len(info.nodes)
-            node_map = np.zeros((nn, len(insts)), np.int32)
-            for d, inst in enumerate(insts):
-                for t, nname in enumerate(inst.nodes):
-                    node_map[t, d] = node_names[nname]
-                for t in range(len(info.terminals), nn):  # internal nodes
-                    node_map[t, d] = next_node
-                    internal.append(next_node)
-                    if is_noi_node(info.nodes[t]):
-                        noi.append(next_node)
-                    next_node += 1
+            n_dev = len(insts)
+            node_map = np.zeros((nn, n_dev), np.int32)
+            # terminals: rows of the node map, filled column-wise
+            n_used = max((len(inst.nodes) for inst in insts), default=0)
+            for t in range(n_used):
+                node_map[t] = [node_names[inst.nodes[t]] if t < len(inst.nodes) else 0 for inst in insts]
+            # internal nodes: numbered instance by instance, in model-node order
+            n_term = len(info.terminals)
+            n_int = nn - n_term
+            if n_int > 0 and n_dev:
+                ids = next_node + np.arange(n_dev * n_int, dtype=np.int64).reshape(n_dev, n_int)
+                node_map[n_term:] = ids.T
+                internal.extend(ids.ravel().tolist())
+                noi_cols = [j for j in range(n_int) if is_noi_node(info.nodes[n_term + j])]
+                if noi_cols:
+                    noi.extend(ids[:, noi_cols].ravel().tolist())
+                next_node += n_dev * n_int
             npar = len(info.user_params)
-            vals = np.empty((npar, len(insts)))
+            vals = np.empty((npar, n_dev))
             for k, pname in enumerate(info.user_params):
                 vals[k] = info.defaults[pname]
-            for d, inst in enumerate(insts):
-                for pname, v in inst.params.items():
-                    vals[info.param_index(pname), d] = float(v)
+            _fill_instance_params(info, insts, vals)
             varying = [k for k in range(npar) if len(insts) and np.any(vals[k] != vals[k, 0])]
             shared = vals[:, 0].copy() if len(insts) else np.array([info.defaults[p] for p in info.user_params])
             temps = [inst.temperature for inst in insts]
