@@ -22,7 +22,8 @@ struct Ctl {
 
 // cfg: the 22-value transient configuration (vgb_transient layout).  Attempt a
 // takes nr_iters[a], converged[a] and lte_norm[a].  Writes per attempt
-// plan[8a..8a+7] = c0, c1, d1, c2, gshunt, t_next, kl, can_predict and
+// plan[11a..11a+10] = c0, c1, d1, c2, gshunt, t_next, kl, can_predict and the
+// predictor weights of the three latest solutions (newest first), and
 // commit[2a..2a+1] = accept, use_new; times[max_steps] the accepted times;
 // summary = attempts, step_idx, rejected, total_nr, nr_failures, t, dt, done.
 // Returns 0, or 1 when the script ran out before the run was done.
@@ -56,10 +57,12 @@ extern "C" int ctl_replay(const double* cfg, int n_script, const int* nr_iters, 
     int a = 0;
     for (; !s.done && a < n_script; ++a) {
         const StepPlan p = ctl_plan(s);
-        for (int q = 0; q < 5; ++q) plan[8 * a + q] = p.k[q];
-        plan[8 * a + 5] = p.t_next;
-        plan[8 * a + 6] = p.kl;
-        plan[8 * a + 7] = p.can_predict;
+        double* o = plan + 11 * a;
+        for (int q = 0; q < 5; ++q) o[q] = p.k[q];
+        o[5] = p.t_next;
+        o[6] = p.kl;
+        o[7] = p.can_predict;
+        for (int q = 0; q < 3; ++q) o[8 + q] = p.pa[q];
         const StepCommit m = ctl_finish(s, p, lte_norm[a], nr_iters[a], converged[a] != 0, times);
         commit[2 * a] = m.accept;
         commit[2 * a + 1] = m.use_new;

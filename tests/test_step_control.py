@@ -77,7 +77,7 @@ FAIL_AT = {7, 30, 31, 32, 33, 34, 35, 90}
 
 
 def _oracle_run(monkeypatch, rc, S, cfg):
-    calls, norms, perr = [], [], []
+    calls, norms, perr, vhist, vpred = [], [], [], [], []
     nodes = [rc.node_names[f"n{k}"] for k in range(4)]
     tn = rc.node_names["tn"]
 
@@ -105,6 +105,8 @@ def _oracle_run(monkeypatch, rc, S, cfg):
     def rec_pred(*a, **k):
         r = real_pred(*a, **k)
         perr.append(r[1])
+        vhist.append(np.array(a[0]))
+        vpred.append(np.array(r[0]))
         return r
 
     monkeypatch.setattr(otr, "nr_solve", fake_nr)
@@ -112,7 +114,7 @@ def _oracle_run(monkeypatch, rc, S, cfg):
     monkeypatch.setattr(otr, "predict_voltage", rec_pred)
     X0 = np.zeros(rc.n_nodes + len(rc.vsources))
     o = otr.run_transient(S, cfg, X0)
-    return o, calls, norms, perr
+    return o, calls, norms, perr, vhist, vpred
 
 
 @pytest.mark.parametrize("method,fixed,min_dt,reltol", [
@@ -122,13 +124,13 @@ def _oracle_run(monkeypatch, rc, S, cfg):
 def test_controller_replays_oracle_decisions(monkeypatch, method, fixed, min_dt, reltol):
     rc, S = _system()
     cfg = _cfg(rc, method, fixed, min_dt, reltol)
-    o, calls, norms, perr = _oracle_run(monkeypatch, rc, S, cfg)
+    o, calls, norms, perr, vhist, vpred = _oracle_run(monkeypatch, rc, S, cfg)
     n = len(calls)
     iters = np.array([(2 + a % 5) if a not in FAIL_AT else int(cfg["tran_itl"]) for a in range(n)], np.int32)
     conv = np.array([0 if a in FAIL_AT else 1 for a in range(n)], np.int32)
     lte = np.asarray(norms if norms else [0.0] * n, np.float64)
     assert len(lte) == n
-    plan = np.zeros((n, 8))
+    plan = np.zeros((n, 11))
     commit = np.zeros((n, 2), np.int32)
     times = np.zeros(int(cfg["max_steps"]))
     summary = np.zeros(8)
@@ -145,6 +147,10 @@ def test_controller_replays_oracle_decisions(monkeypatch, method, fixed, min_dt,
         err_i = {0: -0.5, 1: 1.0 / 24.0, 2: -2.0 / 9.0}[method]
         kl = err_i / (err_i - np.asarray(perr))
         np.testing.assert_allclose(plan[:, 6], kl, rtol=1e-12)
+        # the predictor weights applied to the oracle's history (newest first) give its prediction
+        for a in range(n):
+            pred = plan[a, 8:11] @ vhist[a][:3]
+            np.testing.assert_allclose(pred, vpred[a], rtol=1e-12, atol=1e-15)
     steps = int(summary[1])
     assert steps == o["n_steps"]
     np.testing.assert_allclose(times[:steps], o["times"], rtol=1e-15, atol=0)
