@@ -76,3 +76,56 @@ extern "C" int gather_assemble(void* h, const double* const* rr, const double* c
         return 1;
     }
 }
+
+// The chunks of the long (supply-rail) gather lists: for every heavy item, its
+// chunks tile its list exactly, in order, none longer than HEAVY_CHUNK.
+// Returns the number of heavy items checked, or -1 after a failed check.
+extern "C" int heavy_chunks_check(void* h) {
+    try {
+        const Circuit& c = *static_cast<const Circuit*>(h);
+        const int n_items = (int)(c.heavy_csr.size() + c.heavy_row.size());
+        CHK((int)c.hitem_ptr.size() == n_items + 1 && c.hitem_ptr[0] == 0);
+        CHK(c.hitem_ptr[n_items] == (int)c.hchunk_item.size());
+        for (int it = 0; it < n_items; ++it) {
+            const bool is_csr = it < (int)c.heavy_csr.size();
+            const int item = is_csr ? c.heavy_csr[it] : c.heavy_row[it - c.heavy_csr.size()];
+            const int lo = is_csr ? c.csr_src_ptr[item] : c.res_src_ptr[item];
+            const int hi = is_csr ? c.csr_src_ptr[item + 1] : c.res_src_ptr[item + 1];
+            CHK(hi - lo > HEAVY_LIST);
+            int at = lo;
+            for (int k = c.hitem_ptr[it]; k < c.hitem_ptr[it + 1]; ++k) {
+                CHK(c.hchunk_item[k] == it && c.hchunk_lo[k] == at);
+                CHK(c.hchunk_hi[k] > at && c.hchunk_hi[k] - at <= HEAVY_CHUNK);
+                at = c.hchunk_hi[k];
+            }
+            CHK(at == hi);
+        }
+        // every list longer than HEAVY_LIST is a heavy item
+        int n_long = 0;
+        for (int e = 0; e < c.nnz; ++e) n_long += c.csr_src_ptr[e + 1] - c.csr_src_ptr[e] > HEAVY_LIST;
+        for (int r = 0; r < c.n_unk; ++r) n_long += c.res_src_ptr[r + 1] - c.res_src_ptr[r] > HEAVY_LIST;
+        CHK(n_long == n_items);
+        return n_items;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// The NOI position lists applied to (csr, f) as the enforcement kernel does:
+// listed CSR values zeroed, NOI diagonals set to 1, NOI residual rows zeroed.
+// The kernel writes all three lists at once, so the zeroed and the unit
+// positions must be disjoint (no entry written twice).
+extern "C" int noi_apply(void* h, double* csr, double* f) {
+    try {
+        const Circuit& c = *static_cast<const Circuit*>(h);
+        std::vector<char> hit(c.nnz, 0);
+        for (int e : c.noi_zero) { CHK(e >= 0 && e < c.nnz && !hit[e]); hit[e] = 1; }
+        for (int e : c.noi_diag) { CHK(e >= 0 && e < c.nnz && !hit[e]); hit[e] = 1; }
+        for (int e : c.noi_zero) { CHK(e >= 0 && e < c.nnz); csr[e] = 0.0; }
+        for (int e : c.noi_diag) { CHK(e >= 0 && e < c.nnz); csr[e] = 1.0; }
+        for (int r : c.noi_res) { CHK(r >= 0 && r < c.n_aug); f[r] = 0.0; }
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}

@@ -7,6 +7,10 @@ host through the lists of an analysed circuit, fed with the oracle's
 per-instance model outputs laid out as the evaluation kernel writes them.  The
 result must equal the oracle's own scatter-add assembly (mna_builder.py:
 759-1076): CSR values, resistive residual, charges and maximum contribution.
+Also checked: the fixed chunks that split the supply-rail lists for the block
+reduction tile each list exactly, and the NOI position lists (disjoint, as the
+enforcement kernel writes them at once) equal the oracle's enforce_noi
+(solver_factories.py:775-782).
 """
 
 import ctypes as C
@@ -46,6 +50,10 @@ def _lib():
     dpp, dp = C.POINTER(C.c_void_p), C.POINTER(C.c_double)
     lib.gather_assemble.restype = C.c_int
     lib.gather_assemble.argtypes = [C.c_void_p, dpp, dpp, dpp, dpp, C.c_double, C.c_double, dp, dp, dp, dp]
+    lib.heavy_chunks_check.restype = C.c_int
+    lib.heavy_chunks_check.argtypes = [C.c_void_p]
+    lib.noi_apply.restype = C.c_int
+    lib.noi_apply.argtypes = [C.c_void_p, dp, dp]
     return lib
 
 
@@ -87,4 +95,35 @@ def test_gathered_assembly_equals_oracle(name, c0):
     np.testing.assert_allclose(fres, ref_fres, rtol=1e-12, atol=1e-13 * np.abs(ref_fres).max())
     np.testing.assert_allclose(q, ref_q, rtol=1e-12, atol=1e-13 * max(np.abs(ref_q).max(), 1e-300))
     np.testing.assert_array_equal(maxc, ref_maxc)  # a maximum does not depend on the order
+    dc.close()
+
+
+def test_heavy_list_chunks_tile_the_lists():
+    """Supply-rail rows (lists longer than 64 slots) are summed in fixed chunks by a block reduction."""
+    eng = CircuitEngine(random_gate_network(n_gates=2000, seed=2)[0]).parse()
+    dc = DeviceCircuit(eng.rc, device=False)
+    n = _lib().heavy_chunks_check(dc.h)
+    assert n > 0, "no heavy lists, or a failed check (see stderr)"
+    dc.close()
+
+
+@pytest.mark.parametrize("name", ["ring7", "gates120"])
+def test_noi_positions_equal_oracle_enforcement(name):
+    eng = CircuitEngine(CASES[name]()).parse()
+    rc = eng.rc
+    # two circuit nodes held as NOI nodes (any node works for the position lists)
+    rc.noi_nodes = sorted(v for k, v in rc.node_names.items() if v > 0)[1:3]
+    dc = DeviceCircuit(rc, device=False)
+    S = OracleSystem(rc, {g.model: load_model(g.model) for g in rc.groups})
+    S.set_noi(rc.noi_nodes)
+    X = np.zeros(rc.n_nodes + len(rc.vsources))
+    X[: rc.n_nodes] = eng.initial_guess()
+    csr, f, *_ = S.build_system(X, rc.source_values(0.0), c0=1e12)
+    ref_csr, ref_f = S.enforce_noi(csr, f)
+    got_csr, got_f = csr.copy(), f.copy()
+    dp = C.POINTER(C.c_double)
+    assert _lib().noi_apply(dc.h, got_csr.ctypes.data_as(dp), got_f.ctypes.data_as(dp)) == 0
+    np.testing.assert_array_equal(got_csr, ref_csr)
+    np.testing.assert_array_equal(got_f, ref_f)
+    assert not np.array_equal(ref_csr, csr)
     dc.close()
