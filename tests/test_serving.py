@@ -66,6 +66,32 @@ def test_reservation_sized_before_device_allocation(monkeypatch):
     assert [c[0] for c in calls] == ["sized", "finalize"]
 
 
+def test_parse_reuses_a_resolve_at_the_analysis_temperature():
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions
+    job = _net_job(0, 3)
+    c = job.make_circuit()
+    c.temperature = SimulationOptions(**job.options).temp + 273.15
+    rc = c.resolve()
+    eng = CircuitEngine(c, SimulationOptions(**job.options)).parse(resolved=rc)
+    assert eng.rc is rc
+    # another analysis temperature: resolved again, at that temperature
+    hot = CircuitEngine(c, SimulationOptions(**job.options, temp=125.0)).parse(resolved=rc)
+    assert hot.rc is not rc and hot.rc.temperature == 125.0 + 273.15
+    assert hot.rc.node_names == rc.node_names
+
+
+def test_submit_keys_and_keeps_the_resolved_circuit():
+    from vajax_gb300.serving import Server
+    srv = Server()
+    ok, bad = _net_job(0, 3), _net_job(1, 3)
+    bad.options = dict(bad.options, not_an_option=1)
+    srv.submit(ok)
+    srv.submit(bad)  # invalid options are reported when the job runs, not at submission
+    assert ok.resolved is not None and ok.resolved.temperature == 27.0 + 273.15
+    assert bad.resolved is None
+    assert ok.key.split(":")[0] == bad.key.split(":")[0]  # same circuit pattern
+
+
 @pytest.mark.gpu
 def test_served_results_match_alone(cuda):
     from vajax_gb300.serving import serve

@@ -128,9 +128,15 @@ class CircuitEngine:
         self.dc_method = ""
 
     # parse: resolve node numbering and device groups (engine.py:421-486)
-    def parse(self):
+    def parse(self, resolved=None):
+        """Resolve the circuit at the analysis temperature.  ``resolved``: this
+        circuit already resolved by the caller; used when its temperature is
+        the analysis temperature, otherwise the circuit is resolved again."""
         self.circuit.temperature = self.options.temp + 273.15
-        self.rc = self.circuit.resolve()
+        if resolved is not None and resolved.temperature == self.circuit.temperature:
+            self.rc = resolved
+        else:
+            self.rc = self.circuit.resolve()
         self.node_names = dict(self.rc.node_names)
         self.num_nodes = self.rc.n_nodes
         return self

@@ -58,6 +58,7 @@ class Job:
     group_size: int = 1
     key: str = ""
     circuit: Any = None
+    resolved: Any = None
 
     @property
     def latency(self) -> float:
@@ -102,7 +103,9 @@ def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, r
     if not single and opts.get("ic"):
         opts["ic"] = {f"j{k}.{n}": v for k in range(len(jobs)) for n, v in lead.options["ic"].items()}
     eng = CircuitEngine(circuit, SimulationOptions(**opts), precision=precision)
-    eng.parse()
+    eng.parse(resolved=lead.resolved if single else None)
+    for j in jobs:
+        j.resolved = None  # held by the engine now (or not needed)
     sized = [0]
 
     def admit(dev):
@@ -162,9 +165,19 @@ class Server:
     # ---- client side -----------------------------------------------------
     def submit(self, job: Job):
         """Queue a job (its circuit is built and keyed by pattern here, on the caller's thread)."""
+        from vajax_gb300.engine import SimulationOptions
         job.arrival = time.perf_counter()
         job.circuit = job.make_circuit()
-        job.key = job_key(job, job.circuit.resolve())
+        try:
+            temp = SimulationOptions(**job.options).temp + 273.15
+        except TypeError:
+            temp = None  # invalid options: the job reports the error when it runs
+        if temp is not None:
+            # resolved at the analysis temperature, so that a group of one reuses it
+            job.circuit.temperature = temp
+        rc = job.circuit.resolve()
+        job.resolved = rc if temp is not None else None
+        job.key = job_key(job, rc)
         with self._lock:
             self._queue.append(job)
             self._lock.notify_all()
