@@ -115,3 +115,27 @@ def test_served_results_match_alone(cuda):
             assert err == 0.0, (served.job_id, err)
         else:
             assert err < 1e-6, (served.job_id, err)
+
+
+def test_group_resolves_at_the_analysis_temperature():
+    """Two jobs with temp=125 submitted to a server, then batched: every
+    instance of the concatenated circuit resolves at 398.15 K, as each job
+    does alone."""
+    from vajax_gb300.corners import concat_circuits
+    from vajax_gb300.serving import Server
+    opts = dict(tran_method="gear2", maxstep=0.4e-9 / 50, temp=125.0)
+    jobs = [Job(i, lambda s=s: random_gate_network(n_gates=20, depth=4, n_inputs=4, seed=s)[0], t_stop=0.1e-9,
+                dt=1e-12, max_steps=11, options=dict(opts)) for i, s in enumerate((4, 4))]
+    srv = Server()
+    for j in jobs:
+        srv.submit(j)
+    assert jobs[0].key == jobs[1].key
+    alone = jobs[0].resolved
+    assert alone is not None
+    for g in alone.groups:
+        temps = g.temperatures if g.temperatures is not None else np.full(g.n_dev, g.temp_shared)
+        assert np.allclose(temps, 398.15)
+    rc = concat_circuits([j.circuit for j in jobs]).resolve()
+    for g in rc.groups:
+        temps = g.temperatures if g.temperatures is not None else np.full(g.n_dev, g.temp_shared)
+        assert np.allclose(temps, 398.15)

@@ -173,7 +173,9 @@ class Server:
         except TypeError:
             temp = None  # invalid options: the job reports the error when it runs
         if temp is not None:
-            # resolved at the analysis temperature, so that a group of one reuses it
+            # The circuit carries the analysis temperature: a group of one reuses
+            # this resolution, and concat_circuits gives every instance of a
+            # batched group the same temperature the job has alone.
             job.circuit.temperature = temp
         rc = job.circuit.resolve()
         job.resolved = rc if temp is not None else None
@@ -216,6 +218,11 @@ class Server:
                     else:
                         rest.append(j)
                 self._queue = rest
+                if len(group) > 1:
+                    # a batched group is resolved anew as one circuit: drop the
+                    # per-job resolutions kept for groups of one
+                    for j in group:
+                        j.resolved = None
                 self._active += 1
                 self._groups.append(len(group))
             t = threading.Thread(target=self._run, args=(group,), daemon=True)
