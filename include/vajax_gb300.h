@@ -246,21 +246,31 @@ int vgb_tran_read(void* session, double* times, double* V_out, double* I_out, do
 int vgb_tran_state(void* session, double* X, double* Q);
 int vgb_tran_destroy(void* session);
 
-/* Dense solve of J x = rhs for a small circuit that allocates nothing: the
- * same system as vgb_linear_solve (device pointers csr_vals[nnz], rhs[n_aug],
- * x[n_aug]), solved by dense LU with partial pivoting in one CTA, with the
- * working matrix in a fixed file-scope device array of VGB_DENSE_STATIC_MAX^2
- * doubles (128 KB) instead of memory allocated per call.  Circuits with
- * n_aug > VGB_DENSE_STATIC_MAX are rejected with VGB_ERR_INVALID.
+/* Dense solve of J x = rhs for a small circuit that allocates nothing.
+ * For callers that may not allocate device memory while they run: an XLA
+ * custom-call handler (XLA's allocator already holds most of the GPU and
+ * hands the handler only its operand and result buffers), or a host that
+ * reserves all device memory for its own pool at start-up.  The caller passes
+ * every input and output; the working matrix is a fixed file-scope device
+ * array of VGB_DENSE_STATIC_MAX^2 doubles (128 KB), which every GPU that loads
+ * the library keeps until the process exits.
+ * Same system as vgb_linear_solve (device pointers csr_vals[nnz], rhs[n_aug],
+ * x[n_aug]), solved by dense LU with partial pivoting in one CTA.  Circuits
+ * with n_aug > VGB_DENSE_STATIC_MAX are rejected with VGB_ERR_INVALID.
+ * info (device int, may be NULL) receives 0, or 1 + the column of the first
+ * zero or non-finite pivot, which was replaced by 1e-30 (LAPACK getrf
+ * convention); it is written on the stream, so read it after the stream
+ * synchronises.  The call itself is asynchronous.
  * The first call on each device (with that device current) looks up the
- * array's address and loads the module: make it before any stream capture.
+ * array's address and loads the module; make that first call before any
+ * stream capture.  The cached address does not survive cudaDeviceReset.
  * Nothing in the array must start at zero.  Calls that overlap in time on one
  * device (other streams or threads) share the array and race: serialise them.
  * No counterpart in the reference (its dense path solves in JAX,
  * solver_factories.py:784-788). */
 #define VGB_DENSE_STATIC_MAX 128
 int vgb_linear_solve_dense_static(void* h, const double* csr_vals, const double* rhs, double* x,
-                                  vgb_stream_t stream);
+                                  int* info, vgb_stream_t stream);
 
 #ifdef __cplusplus
 }

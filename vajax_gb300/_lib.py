@@ -56,7 +56,7 @@ SIGNATURES = {
     "vgb_tran_read": (C.c_int, [vp, f64p, f64p, f64p, f64p]),
     "vgb_tran_state": (C.c_int, [vp, f64p, f64p]),
     "vgb_tran_destroy": (C.c_int, [vp]),
-    "vgb_linear_solve_dense_static": (C.c_int, [vp, vp, vp, vp, vp]),
+    "vgb_linear_solve_dense_static": (C.c_int, [vp, vp, vp, vp, vp, vp]),
 }
 
 

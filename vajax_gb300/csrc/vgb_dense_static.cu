@@ -1,13 +1,21 @@
 // Dense linear solve of a small circuit with no allocation: the working matrix
 // lives in a file-scope __device__ array instead of memory allocated per call.
 //
+// Some callers may not allocate device memory while they run: an XLA custom
+// call, whose buffers all come from XLA's own allocator that already holds
+// most of the GPU, or a host that reserves all device memory up front for its
+// own pool.  This entry point lets them solve small systems with only the
+// buffers they pass in.
+//
 // J x = rhs is scattered from the circuit's CSR values into a dense
 // column-major matrix in that array and solved by LU with partial pivoting in
 // one CTA.  The set-up (looking up the array's device address with
 // cudaGetSymbolAddress) runs once per device, on the first call made with that
-// device current.  Nothing in the array needs to start at zero: every call
-// writes all n x n entries before reading them.  Calls that overlap in time on
-// one device (other streams or host threads) share the array and race.
+// device current; the address is cached for the life of the process, so it
+// does not survive a cudaDeviceReset.  Nothing in the array needs to start at
+// zero: every call writes all n x n entries before reading them.  Calls that
+// overlap in time on one device (other streams or host threads) share the
+// array and race.
 #include <mutex>
 
 #include "vgb_core.h"
@@ -43,11 +51,12 @@ __global__ void __launch_bounds__(DENSE_THREADS) dense_static_solve_kernel(int n
                                                                          const int* __restrict__ indices,
                                                                          const double* __restrict__ vals,
                                                                          const double* __restrict__ rhs, double* x,
-                                                                         double* M, int* err) {
+                                                                         double* M, int* err, int* info) {
     __shared__ double b[VGB_DENSE_STATIC_MAX];
     __shared__ double r_val[DENSE_THREADS];
     __shared__ int r_idx[DENSE_THREADS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = DENSE_THREADS / 32;
+    int first_bad = 0;  // LAPACK getrf convention: 1 + column of the first zero or non-finite pivot
     for (int t = tid; t < n * n; t += DENSE_THREADS) M[t] = 0.0;
     for (int i = tid; i < n; i += DENSE_THREADS) b[i] = rhs[i];
     __syncthreads();
@@ -93,7 +102,8 @@ __global__ void __launch_bounds__(DENSE_THREADS) dense_static_solve_kernel(int n
             __syncthreads();
             if (tid == 0) {
                 M[k + k * n] = piv;
-                atomicOr(err, DEV_ERR_PIVOT);
+                if (err) atomicOr(err, DEV_ERR_PIVOT);
+                if (!first_bad) first_bad = k + 1;
             }
         }
         for (int i = k + 1 + tid; i < n; i += DENSE_THREADS) M[i + k * n] /= piv;
@@ -118,6 +128,7 @@ __global__ void __launch_bounds__(DENSE_THREADS) dense_static_solve_kernel(int n
         __syncthreads();
     }
     for (int i = tid; i < n; i += DENSE_THREADS) x[i] = b[i];
+    if (info && tid == 0) *info = first_bad;
 }
 
 }  // namespace
@@ -126,7 +137,7 @@ __global__ void __launch_bounds__(DENSE_THREADS) dense_static_solve_kernel(int n
 // (the per-circuit dense solver of small circuits).
 void launch_dense_solve(int n, const int* indptr, const int* indices, const double* vals, const double* rhs,
                         double* x, double* M, int* err, cudaStream_t s) {
-    if (n > 0) dense_static_solve_kernel<<<1, DENSE_THREADS, 0, s>>>(n, indptr, indices, vals, rhs, x, M, err);
+    if (n > 0) dense_static_solve_kernel<<<1, DENSE_THREADS, 0, s>>>(n, indptr, indices, vals, rhs, x, M, err, nullptr);
 }
 
 }  // namespace vgb
@@ -134,7 +145,7 @@ void launch_dense_solve(int n, const int* indptr, const int* indices, const doub
 using namespace vgb;
 
 extern "C" int vgb_linear_solve_dense_static(void* h, const double* csr_vals, const double* rhs, double* x,
-                                             vgb_stream_t stream) {
+                                             int* info, vgb_stream_t stream) {
     Circuit* c = static_cast<Circuit*>(h);
     if (!c) return VGB_ERR_INVALID;
     try {
@@ -144,11 +155,14 @@ extern "C" int vgb_linear_solve_dense_static(void* h, const double* csr_vals, co
             throw Error(VGB_ERR_INVALID, "vgb_linear_solve_dense_static: n_aug = " + std::to_string(c->n_aug) +
                                              " exceeds the static scratch limit of " +
                                              std::to_string(VGB_DENSE_STATIC_MAX) + " unknowns");
-        if (c->n_aug == 0) return VGB_OK;
-        double* M = scratch_for_current_device();
         cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+        if (c->n_aug == 0) {
+            if (info) VGB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+            return VGB_OK;
+        }
+        double* M = scratch_for_current_device();
         dense_static_solve_kernel<<<1, DENSE_THREADS, 0, s>>>(c->n_aug, c->d_indptr.p, c->d_indices.p, csr_vals, rhs,
-                                                              x, M, &c->d_status.p->dev_err);
+                                                              x, M, nullptr, info);
         VGB_CUDA(cudaGetLastError());
         c->launches += 1;
         return VGB_OK;
