@@ -14,7 +14,10 @@ instead of evaluating both sides of every branch the way the JAX backend's
 ``jnp.where`` does; phi nodes become assignments at the end of each
 predecessor block.  Opcode semantics are the reference's safe-math ones
 (``codegen/instruction.py``): divide-by-zero yields 0, ``sqrt`` clamps at 0,
-``ln``/``log`` clamp at 1e-300, ``ficast`` floors.
+``ln``/``log`` clamp at 1e-300, ``ficast`` floors.  Division, ``exp``,
+``ln``/``log`` and ``pow`` use the table-driven FP64 functions of
+``csrc/vgb_math.cuh``, which cost fewer FP64 instructions than the library's
+on GB300 (where FP64 issue is what bounds a device evaluation).
 """
 
 from __future__ import annotations
@@ -28,11 +31,11 @@ _BIN_INFIX = {"fadd": "+", "fsub": "-", "fmul": "*", "iadd": "+", "isub": "-", "
 _CMP = {"feq": "==", "fne": "!=", "flt": "<", "fle": "<=", "fgt": ">", "fge": ">=",
         "ieq": "==", "ine": "!=", "ilt": "<", "ile": "<=", "igt": ">", "ige": ">=",
         "beq": "==", "bne": "!="}
-_UN_FN = {"exp": "exp", "sin": "sin", "cos": "cos", "tan": "tan", "sinh": "sinh",
+_UN_FN = {"exp": "vgb_exp", "sin": "sin", "cos": "cos", "tan": "tan", "sinh": "sinh",
           "cosh": "cosh", "tanh": "tanh", "asin": "asin", "acos": "acos", "atan": "atan",
           "asinh": "asinh", "acosh": "acosh", "atanh": "atanh", "fabs": "fabs", "abs": "fabs",
           "floor": "floor", "ceil": "ceil"}
-_BIN_FN = {"pow": "pow", "fmin": "vgb_fmin", "fmax": "vgb_fmax", "atan2": "atan2", "hypot": "hypot"}
+_BIN_FN = {"pow": "vgb_pow", "fmin": "vgb_fmin", "fmax": "vgb_fmax", "atan2": "atan2", "hypot": "hypot"}
 
 
 def _cname(model_name: str) -> str:
@@ -265,13 +268,13 @@ def _expr(op: str, a: List[str]) -> str:
     if op == "fneg" or op == "ineg":
         return f"(-{a[0]})"
     if op == "fdiv":
-        return f"vgb_sdiv({a[0]}, {a[1]})"
+        return f"vgb_msdiv({a[0]}, {a[1]})"
     if op == "sqrt":
         return f"sqrt(fmax({a[0]}, 0.0))"
     if op == "ln":
-        return f"log(fmax({a[0]}, 1e-300))"
+        return f"vgb_log(fmax({a[0]}, 1e-300))"
     if op == "log":
-        return f"log10(fmax({a[0]}, 1e-300))"
+        return f"(vgb_log(fmax({a[0]}, 1e-300)) * VGB_INV_LN10)"
     if op == "frem":
         return f"vgb_fmod_floor({a[0]}, {a[1]})"
     if op == "select":
@@ -314,29 +317,45 @@ def load_model(path) -> dict:
         return json.load(fh)
 
 
-def emit_registry(models: Dict[str, dict]) -> str:
-    """Emit all models plus the kernel instantiations and a lookup table."""
-    parts = ['#include "vgb_eval.cuh"', "namespace vgb {"]
+def emit_header(models: Dict[str, dict]) -> str:
+    """The model structs, plus an X-macro VGB_MODEL_LIST(X) that expands
+    X(id, struct) for every model in model-table order, so that other
+    translation units (the batched engine) can dispatch on a model id."""
+    parts = ["#pragma once", '#include "vgb_eval.cuh"', '#include "vgb_math.cuh"', "namespace vgb {"]
     names = []
     for key, m in models.items():
         sname = f"Model_{_cname(key)}"
         parts.append(emit_model(m, sname))
-        names.append((key, sname))
+        names.append(sname)
+    parts.append("} // namespace vgb")
+    parts.append("#define VGB_MODEL_LIST(X) " + " ".join(f"X({i}, {n})" for i, n in enumerate(names)))
+    return "\n".join(parts) + "\n"
+
+
+def emit_registry(models: Dict[str, dict], header: str = "vgb_models_gen.cuh") -> str:
+    """The lookup table of the kernels of every model (models from `header`)."""
+    parts = [f'#include "{header}"', "namespace vgb {"]
     parts.append("const ModelEntry* model_table(int* count) {")
     parts.append("    static const ModelEntry table[] = {")
-    for key, sname in names:
-        parts.append(f'        make_model_entry<{sname}>("{key}"),')
+    for key in models:
+        parts.append(f'        make_model_entry<Model_{_cname(key)}>("{key}"),')
     parts.append("    };")
-    parts.append(f"    *count = {len(names)};")
+    parts.append(f"    *count = {len(models)};")
     parts.append("    return table;")
     parts.append("}")
     parts.append("} // namespace vgb")
     return "\n".join(parts)
 
 
-def write_generated(models_dir: Path, out_path: Path) -> List[str]:
+def write_generated(models_dir: Path, out_path: Path, header_path: Path | None = None) -> List[str]:
+    """Write the model structs to `header_path` (default: next to `out_path`,
+    vgb_models_gen.cuh) and the model table to `out_path`."""
     models = {}
     for p in sorted(models_dir.glob("*.json")):
         models[p.stem] = load_model(p)
-    out_path.write_text(emit_registry(models))
+    header_path = header_path or out_path.with_name("vgb_models_gen.cuh")
+    text = emit_header(models)
+    if not header_path.exists() or header_path.read_text() != text:
+        header_path.write_text(text)
+    out_path.write_text(emit_registry(models, header_path.name))
     return list(models)

@@ -2,6 +2,8 @@
 #include <cuda/atomic>
 
 #include "vgb_kernels.cuh"
+#include "vgb_math.cuh"
+#include "vgb_sources.cuh"
 
 namespace vgb {
 
@@ -397,43 +399,6 @@ void launch_vsrc_current(const double* fres, const int* vsrc_p, double* I, int n
     if (n_vsrc) vsrc_current_kernel<<<ceil_div(n_vsrc, 128), 128, 0, s>>>(fres, vsrc_p, I, n_vsrc);
 }
 
-// Source waveforms (vajax/analysis/sources.py:31-105)
-__device__ double eval_source(int kind, const double* p, int cnt, double t) {
-    if (kind == SRC_DC) return p[0];
-    if (kind == SRC_PULSE) {
-        // val0, val1, rise, fall, width, period, delay
-        const double v0 = p[0], v1 = p[1], r = p[2], f = p[3], w = p[4], per = p[5], d = p[6];
-        const double tp = vgb_fmod_floor(t - d, per);
-        if (t < d) return v0;
-        if (tp < r) return v0 + (v1 - v0) * tp / r;
-        if (tp < r + w) return v1;
-        if (tp < r + w + f) return v1 - (v1 - v0) * (tp - r - w) / f;
-        return v0;
-    }
-    if (kind == SRC_PWL) {
-        // [period, t0, v0, t1, v1, ...] (times already stretched, values scaled)
-        const double period = p[0];
-        const int np = (cnt - 1) / 2;
-        const double* tv = p + 1;
-        double tt = t;
-        if (period > 0) tt = vgb_fmod_floor(t, period);
-        if (tt <= tv[0]) return tv[1];
-        if (tt >= tv[2 * (np - 1)]) return tv[2 * (np - 1) + 1];
-        int lo = 0, hi = np - 1;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (tv[2 * mid] <= tt) lo = mid; else hi = mid;
-        }
-        const double t0 = tv[2 * lo], t1 = tv[2 * hi], v0 = tv[2 * lo + 1], v1 = tv[2 * hi + 1];
-        const double dt = t1 - t0;
-        return dt == 0.0 ? v1 : v0 + (tt - t0) * (v1 - v0) / dt;
-    }
-    if (kind == SRC_SINE) {
-        return p[0] + p[1] * sin(2.0 * 3.141592653589793 * p[2] * t + p[3]);
-    }
-    return 0.0;
-}
-
 // t_dev (device memory) replaces t when given: the transient graph computes the time on the device
 __global__ void eval_sources_kernel(const int* kind, const int* off, const int* cnt, const double* data,
                                     int n, double t, const double* t_dev, double* out) {
@@ -447,6 +412,29 @@ void launch_eval_sources(const Sources& src, int n, double t, double* out, cudaS
 void launch_eval_sources_dev(const Sources& src, int n, const double* t_dev, double* out, cudaStream_t s) {
     if (n) eval_sources_kernel<<<ceil_div(n, 128), 128, 0, s>>>(src.d_kind.p, src.d_off.p, src.d_cnt.p,
                                                                 src.d_data.p, n, 0.0, t_dev, out);
+}
+
+// The device elementary functions of the generated models, one per element
+// (accuracy tests of csrc/vgb_math.cuh).  fn: 0 a/b, 1 exp(a), 2 ln(a),
+// 3 pow(a, b), 4 the models' safe division (a/0 = 0).
+__global__ void math_eval_kernel(int fn, int n, const double* __restrict__ a, const double* __restrict__ b,
+                                 double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = a[i];
+    double r = 0.0;
+    switch (fn) {
+        case 0: r = vgb_div(x, b[i]); break;
+        case 1: r = vgb_exp(x); break;
+        case 2: r = vgb_log(x); break;
+        case 3: r = vgb_pow(x, b[i]); break;
+        default: r = vgb_msdiv(x, b[i]); break;
+    }
+    out[i] = r;
+}
+
+void launch_math_eval(int fn, int n, const double* a, const double* b, double* out, cudaStream_t s) {
+    if (n > 0) math_eval_kernel<<<ceil_div(n, 256), 256, 0, s>>>(fn, n, a, b, out);
 }
 
 } // namespace vgb
