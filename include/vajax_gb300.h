@@ -42,6 +42,15 @@ int vgb_num_models(void);
  * OpenVAFToJAX.get_dae_metadata() (openvaf_jax/__init__.py:253-280). */
 int vgb_model_info(int id, char* name, int name_cap, int* nn, int* nj, int* np, int* jrow, int* jcol);
 
+/* The FP64 elementary functions the generated device models use (table-driven
+ * exp and log, Newton-Raphson division, pow through exp and log), evaluated
+ * element-wise on the device, for accuracy tests against the host's libm.
+ * fn: 0 a/b, 1 exp(a), 2 ln(a), 3 pow(a, b), 4 safe division (a/0 = 0, the
+ * reference code generator's semantics, openvaf_jax/codegen/instruction.py).
+ * a, b, out are device arrays of n doubles (b unused for fn 1 and 2).  No
+ * counterpart in the reference (its models call XLA's math). */
+int vgb_math_eval(int fn, int n, const double* a, const double* b, double* out, vgb_stream_t stream);
+
 /* Circuit construction ------------------------------------------------------ */
 
 /* Create a circuit with n_nodes nodes (including ground) and the given
@@ -245,6 +254,55 @@ int vgb_tran_advance(void* session, int max_accepted, int* accepted, int* done);
 int vgb_tran_read(void* session, double* times, double* V_out, double* I_out, double* stats);
 int vgb_tran_state(void* session, double* X, double* Q);
 int vgb_tran_destroy(void* session);
+
+/* Batched transient of n_rep replicas of one small circuit (n_aug <= 48, no
+ * NOI nodes): Monte-Carlo / process / temperature corners, or served jobs of
+ * one pattern.  Replaces the reference's serial corner loop
+ * (vajax/analysis/engine.py:2274-2320, run_corners) and runs, per replica,
+ * the transient loop of vgb_transient (full_mna.py:1198-1441 fixed step,
+ * :1792-2196 adaptive) with that replica's own Newton iterations, time steps,
+ * rejections and outputs.  All replicas advance in one persistent cooperative
+ * kernel: device evaluation of every replica that needs one, a grid barrier,
+ * one warp per replica for assembly, dense LU with partial pivoting, Newton
+ * update and step control, a second barrier.  Values are batch-interleaved
+ * ([k][replica]) where the evaluation reads and writes them.
+ *   create:      h is the template circuit (one replica: groups, node maps,
+ *                sources; analysed here if it was not); every replica starts
+ *                with the template's parameters and source data.  Touches no
+ *                GPU.
+ *   set_group:   per-replica parameters of group `group`: n_varying columns
+ *                varying_idx (parameter indices) with values
+ *                [n_varying][n_dev][n_rep]; temperatures [n_dev][n_rep] kelvin
+ *                or NULL for the template's.
+ *   set_sources: per-replica source data [n_rep][len] of the template's
+ *                voltage (is_current 0) or current source table (the same
+ *                kinds, offsets and counts; len = the template's data length).
+ *   transient:   cfg as vgb_transient; X0 [n_rep][n_nodes+n_vsrc]; Q0, I0,
+ *                maxc0 ([n_rep][n_nodes-1], [n_rep][n_vsrc], [n_rep][n_nodes-1])
+ *                or Q0 = NULL for the uic start (charges and branch currents
+ *                from an evaluation at X0, as the engine's uic start).
+ *                Outputs, replica-major: times [n_rep][max_steps],
+ *                V_out [n_rep][max_steps][n_external],
+ *                I_out [n_rep][max_steps][max(n_vsrc,1)], stats [n_rep][8] =
+ *                {n_steps, rejected, total_nr_iters, min_dt_used, max_dt_used,
+ *                device_ms, nr_failures, pivot_failures}.
+ *   info:        out[12] = {device ms of the last run, ticks, evaluation items,
+ *                contribution slots per replica, then SM clock cycles summed
+ *                over the ticks of: evaluation, wait at the first grid
+ *                barrier, per-replica step, wait at the second barrier (as
+ *                the first CTA sees them), and, for replica 0: assembly of
+ *                the Newton system, LU and solve, Newton update and test,
+ *                step finish and plan}.
+ * Errors are reported through vgb_batch_last_error(b) (create: on h). */
+int vgb_batch_create(void* h, int n_rep, void** out_batch);
+int vgb_batch_set_group(void* b, int group, int n_varying, const int* varying_idx, const double* values,
+                        const double* temperatures);
+int vgb_batch_set_sources(void* b, int is_current, const double* data);
+int vgb_batch_transient(void* b, const double* cfg, const double* X0, const double* Q0, const double* I0,
+                        const double* maxc0, double* times, double* V_out, double* I_out, double* stats);
+int vgb_batch_info(void* b, double* out);
+const char* vgb_batch_last_error(void* b);
+int vgb_batch_destroy(void* b);
 
 /* Dense solve of J x = rhs for a small circuit that allocates nothing.
  * For callers that may not allocate device memory while they run: an XLA

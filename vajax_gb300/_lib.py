@@ -23,6 +23,14 @@ vp = C.c_void_p
 # name -> (restype, argtypes)
 SIGNATURES = {
     "vgb_version": (C.c_int, []),
+    "vgb_math_eval": (C.c_int, [C.c_int, C.c_int, vp, vp, vp, vp]),
+    "vgb_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+    "vgb_batch_set_group": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
+    "vgb_batch_set_sources": (C.c_int, [vp, C.c_int, vp]),
+    "vgb_batch_transient": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "vgb_batch_info": (C.c_int, [vp, vp]),
+    "vgb_batch_last_error": (C.c_char_p, [vp]),
+    "vgb_batch_destroy": (C.c_int, [vp]),
     "vgb_num_models": (C.c_int, []),
     "vgb_model_info": (C.c_int, [C.c_int, C.c_char_p, C.c_int, i32p, i32p, i32p, i32p, i32p]),
     "vgb_circuit_create": (C.c_int, [C.c_int, C.c_int, i32p, i32p, C.c_int, i32p, i32p, C.POINTER(vp)]),
