@@ -47,6 +47,8 @@ CORNERS = dict(ring=dict(workload="corners_1024x_ring7_fixed_bdf2_1ps", instance
                gates=dict(workload="corners_256x_gates2000T_fixed_bdf2_1ps", instances=256, gates=588),
                steps=2000, seed=7)
 L2_BYTES = 129 * 2 ** 20
+MODEL_NOTE = ("EKV 2.6 (the reference's bundled ekv.va, compiled by this repository's Verilog-A front end) "
+              "stands in for PSP103, whose source is absent: about 0.5 unknowns per transistor, not PSP103's ~2.5")
 STATUS_BYTES = 48  # NRStatus read back per Newton iteration
 
 
@@ -217,6 +219,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def fp64_peak_gflops():
+    """FP64 FMA rate of this GPU, measured now by the library's throughput
+    kernel (vgb_fp64_rate): the denominator of the FP64 fractions."""
+    import ctypes as C
+    from vajax_gb300 import _lib
+    lib = _lib.load()
+    v = C.c_double()
+    _lib.check(lib.vgb_fp64_rate(1 << 14, C.byref(v)))
+    return float(v.value)
+
+
 def ncu_traffic(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
     p = ROOT / "profiles" / "dram_traffic.txt"
@@ -351,11 +364,24 @@ def run_gb300(args):
     fac_ms = phase["factor_ms"]
     achieved = fac_bytes / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0
     work = args.workload if ring else f"gates{args.gates}"
+    fp64_peak = fp64_peak_gflops()
+    fac_gflops = info["front_flops"] / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0
     roofline = {"kernel": "mf_factor_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": ncu_traffic("mf_factor_kernel", work),
+                "traffic_source": "committed ncu capture (profiles/dram_traffic.txt)",
                 "algorithmic_bytes_per_launch": fac_bytes,
-                "fp64_gflops": info["front_flops"] / (fac_ms * 1e-3) / 1e9 if fac_ms > 0 else 0.0}
+                "fp64_gflops": fac_gflops, "fp64_peak_gflops": fp64_peak, "fp64_peak_kind": "measured in this run",
+                "fp64_frac": fac_gflops / fp64_peak if fp64_peak else None}
+    # device evaluation: MIR FP64 operations of the instances / eval time per Newton iteration
+    ev_ms = phase["eval_ms"]
+    mir_ops = sum(mir_flops(g.model) * g.n_dev for g in eng.rc.groups)
+    roofline["eval"] = {"kernel": "eval_kernel<Model_ekv>", "bound": "fp64", "mir_fp64_ops_per_launch": mir_ops,
+                        "achieved_gflops": mir_ops / (ev_ms * 1e-3) / 1e9 if ev_ms > 0 else 0.0,
+                        "peak_gflops": fp64_peak,
+                        "frac": mir_ops / (ev_ms * 1e-3) / 1e9 / fp64_peak if ev_ms > 0 and fp64_peak else None,
+                        "note": "MIR operations count every exp/ln/sqrt/division as one; the kernel issues more "
+                                "FP64 instructions than that"}
 
     # end to end through the public API: CircuitEngine.run_transient (host
     # buffers in and out, wall time / accepted steps of the transient call)
@@ -391,6 +417,8 @@ def run_gb300(args):
            "phase_ms_per_newton_iter": phase, "gpu_launches": launches, "roofline": roofline,
            "mixed_vs_fp64": mixed_vs_fp64,
            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+    if args.workload == "gates" and world == 1 and args.extras == "on":
+        out["configs"] = extra_configs(args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if pg:
@@ -411,7 +439,8 @@ def workload_config(args, ring, nstats, depth, info, world, dc_s, eng):
     if ring:
         return {"workload": RING["workload"], "stages": RING["stages"], "transistors": 2 * RING["stages"],
                 "dt": RING["dt"], "initial_condition": "n1 = VDD, others 0 (uic)", **common}
-    return {"workload": WORKLOAD["workload"], "gates": args.gates, "transistors": nstats.transistors, "depth": depth,
+    return {"workload": WORKLOAD["workload"], "model": WORKLOAD["model"], "model_note": MODEL_NOTE,
+            "gates": args.gates, "transistors": nstats.transistors, "depth": depth,
             "seed": WORKLOAD["seed"], "dc_seconds": dc_s, "dc_method": eng.dc_method, **common}
 
 
@@ -576,25 +605,41 @@ def serving_jobs(n_jobs: int, seed: int, max_transistors: int):
 def run_serving(args):
     """Served stream vs the plain FP64 path one job at a time, on the same seeded jobs."""
     import torch
-    from vajax_gb300.serving import run_group, serve
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
-    n = args.jobs
-    jobs, arrivals, sizes = serving_jobs(n, SERVING["seed"], args.max_transistors)
+    out = serving_measure(args, args.jobs, args.max_transistors, args.precision, gpu=gpu_index(local))
+    out["n_gpus"] = world
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def extra_serving(args):
+    """Config 5 inside the default run: a seeded Poisson stream of DC + 1,000
+    fixed-step jobs (rings of 3-31 stages, networks of 200-80k transistors),
+    served in mixed precision, against the plain FP64 path one job at a time."""
+    return serving_measure(args, args.extra_jobs, 80000, "mixed", gpu=None)
+
+
+def serving_measure(args, n, max_transistors, precision, gpu=None):
+    import torch
+    from vajax_gb300.serving import run_group, serve
+    world = 1
+    jobs, arrivals, sizes = serving_jobs(n, SERVING["seed"], max_transistors)
     # warm-up: one small job of each kind (library load, module load)
     warm, _, _ = serving_jobs(2, SERVING["seed"] + 1, 400)
     for j in warm:
         run_group([j])
-    sampler = ClockSampler(gpu_index(local))
-    sampler.start()
+    sampler = ClockSampler(gpu) if gpu is not None else None
+    if sampler:
+        sampler.start()
     torch.cuda.synchronize()
-    srv = serve(jobs, arrivals, slots=args.slots, precision=args.precision, max_batch=args.max_batch,
+    srv = serve(jobs, arrivals, slots=args.slots, precision=precision, max_batch=args.max_batch,
                 transient_graph=args.serving_graph == "on")
     torch.cuda.synchronize()
-    clocks = sampler.stop()
+    clocks = sampler.stop() if sampler else None
     st = srv.stats()
     # the same jobs, one at a time, each started when the previous finished
-    seq_jobs, _, _ = serving_jobs(n, SERVING["seed"], args.max_transistors)
+    seq_jobs, _, _ = serving_jobs(n, SERVING["seed"], max_transistors)
     t0 = time.perf_counter()
     iters = 0
     seq_lat = []
@@ -619,11 +664,11 @@ def run_serving(args):
                                for k in b.result.voltages))
     out = {"metric": "served_newton_solves_per_s", "value": st.get("solves_per_s", 0.0), "unit": "solves/s",
            "n_gpus": world, "steps": n, "warmup": len(warm), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32lu",
+           "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f64+f32lu",
            "data": "synthetic (seeded job stream)",
            "config": {"workload": SERVING["workload"], "jobs": n, "arrival_rate_per_s": SERVING["rate"],
-                      "ring_stages": SERVING["ring_stages"], "network_transistors": [200, args.max_transistors],
-                      "slots": args.slots, "max_batch": args.max_batch, "precision": args.precision,
+                      "ring_stages": SERVING["ring_stages"], "network_transistors": [200, max_transistors],
+                      "slots": args.slots, "max_batch": args.max_batch, "precision": precision,
                       "seed": SERVING["seed"], "l2": "inputs and fronts of concurrent jobs exceed L2",
                       "served_step_loop": "cuda_graph" if args.serving_graph == "on" else "host_driven",
                       "sequential_step_loop": "cuda_graph"},
@@ -637,8 +682,7 @@ def run_serving(args):
            "max_abs_dv_vs_alone_V": worst, "clocks": clocks,
            "e2e": {"value": st.get("solves_per_s", 0.0), "unit": "solves/s", "h2d_bytes_per_step": None,
                    "d2h_bytes_per_step": None}}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    return out
 
 
 def mir_flops(model: str) -> int:
@@ -710,6 +754,179 @@ def run_eval_stamp(args):
         print(json.dumps(out_line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# the other configurations, measured in the default run (one GPU)
+# ---------------------------------------------------------------------------
+
+def _ring_uic_start(eng):
+    from vajax_gb300.batch import uic_start
+    return uic_start(eng.rc, eng.options.ic)
+
+
+def extra_ring(args):
+    """7-stage ring, 20,000 fixed gear2 steps at 1 ps, on the batched engine
+    (one replica): ms/step from the kernel's CUDA events, e2e with host copies."""
+    from vajax_gb300.batch import BatchedTransient
+    eng = make_ring_engine(device=False)
+    rc = eng.rc
+    cfg = eng.transient_cfg()
+    X0 = _ring_uic_start(eng)[None, :]
+    bt = BatchedTransient([rc], gmin=eng.options.gmin)
+    bt.transient(dict(cfg, t_stop=200 * RING["dt"], max_steps=201), X0)  # warm-up
+    t0 = time.perf_counter()
+    out = bt.transient(cfg, X0)
+    wall = time.perf_counter() - t0
+    bt.close()
+    steps = int(out["n_steps"][0]) - 1
+    nr = int(out["total_nr_iters"][0])
+    ms = out["device_ms"]
+    ticks = max(out["ticks"], 1)
+    cpu = None
+    try:
+        cpu = ring_cpu_baseline(eng, 100)
+    except Exception as e:  # a failing CPU leg must not lose the GPU numbers
+        cpu = {"error": str(e)}
+    return {"workload": RING["workload"], "engine": "batched (one replica)", "steps": steps,
+            "ms_per_step": ms / steps, "newton_iters": nr, "newton_iters_per_s": nr / (ms * 1e-3),
+            "ticks": out["ticks"], "cycles_per_tick": {k: v / ticks for k, v in out["phase_cycles"].items()},
+            "e2e": {"value": wall * 1e3 / steps, "unit": "ms/step",
+                    "h2d_bytes_per_step": 8.0 * X0.size / steps,
+                    "d2h_bytes_per_step": 8.0 * (out["V"].size + out["I"].size + out["times"].size) / steps},
+            "reference_published_ms_per_step": {"jax_cpu": 0.511, "jax_gpu": 1.49},
+            "cpu_baseline": cpu}
+
+
+def ring_cpu_baseline(eng, steps):
+    """The oracle on the ring's first `steps` fixed steps (1 thread)."""
+    from oracle.transient import run_transient
+    S = _oracle_system(eng)
+    rc = eng.rc
+    X0 = _ring_uic_start(eng)
+    _, _, Q0, I0, _, _ = S.build_system(X0, rc.source_values(0.0))
+    c = dict(eng.transient_cfg(), t_stop=steps * RING["dt"], max_steps=steps + 1)
+    t0 = time.perf_counter()
+    o = run_transient(S, c, X0, Q0, I0)
+    wall = time.perf_counter() - t0
+    return {"value": wall * 1e3 / max(o["n_steps"] - 1, 1), "unit": "ms/step", "cores": 1, "kind": "port",
+            "sample": f"first {steps} fixed steps of the ring, oracle numpy + dense solve"}
+
+
+def extra_corners(args):
+    """Config 4: 1,024 Monte-Carlo ring corners on the batched engine (2,000
+    fixed steps), and 256 copies of a ~2,000-transistor network on the
+    block-diagonal path (a sample of the fixed steps, from the DC point)."""
+    from vajax_gb300.batch import BatchedTransient, uic_start
+    from vajax_gb300.corners import batch_circuit, create_monte_carlo_corners
+    from vajax_gb300.generators import ring_oscillator
+    out = {}
+    n = CORNERS["ring"]["instances"]
+    corners = create_monte_carlo_corners(n, seed=CORNERS["seed"])
+    rcs = [batch_circuit(ring_oscillator(stages=RING["stages"], vdd=RING["vdd"], c_load=RING["c_load"]),
+                         [c]).resolve() for c in corners]
+    eng = make_ring_engine(device=False)
+    steps = CORNERS["steps"]
+    cfg = dict(eng.transient_cfg(), t_stop=steps * RING["dt"], max_steps=steps + 1, n_external=rcs[0].n_external)
+    X0 = np.stack([uic_start(r, {"c0.n1": RING["vdd"], "c0.vdd": RING["vdd"]}) for r in rcs])
+    bt = BatchedTransient(rcs)
+    bt.transient(dict(cfg, t_stop=50 * RING["dt"], max_steps=51), X0)  # warm-up
+    t0 = time.perf_counter()
+    r = bt.transient(cfg, X0)
+    wall = time.perf_counter() - t0
+    bt.close()
+    nr = int(r["total_nr_iters"].sum())
+    ms = r["device_ms"]
+    out["ring"] = {"workload": CORNERS["ring"]["workload"], "engine": "batched, one replica per corner",
+                   "instances": n, "steps": steps, "ms_per_step": ms / steps,
+                   "solves_per_s": nr / (ms * 1e-3), "newton_iters_per_replica_mean": float(r["total_nr_iters"].mean()),
+                   "newton_iters_per_replica_max": int(r["total_nr_iters"].max()), "ticks": r["ticks"],
+                   "cycles_per_tick": {k: v / max(r["ticks"], 1) for k, v in r["phase_cycles"].items()},
+                   "wall_s": wall, "corner_seed": CORNERS["seed"]}
+    # gates corners: block-diagonal circuit, K timed steps of the fixed-step run
+    K = args.extra_steps
+    eng, n_inst, per_copy = make_corners_engine("gates", "fp64")
+    dev = eng.device
+    X0, Q0, I0, maxc0, ok = eng.initial_state()
+    if not ok:
+        out["gates"] = {"error": f"DC did not converge ({eng.dc_method})"}
+        return out
+    sess = dev.session(eng.transient_cfg(), X0, Q0, I0, maxc0)
+    dev_ms, iters = _time_session(sess, 3, K)
+    sess.close()
+    dev.close()
+    out["gates"] = {"workload": CORNERS["gates"]["workload"], "engine": "block-diagonal batch, one Newton loop",
+                    "instances": n_inst, "transistors_per_instance": per_copy, "steps_timed": K,
+                    "ms_per_step": dev_ms / K, "solves_per_s": n_inst * iters / (dev_ms * 1e-3)}
+    return out
+
+
+def _time_session(sess, warmup, steps):
+    """Device ms (CUDA events on the library's stream) and Newton iterations
+    of `steps` accepted steps after `warmup` untimed ones."""
+    import torch
+    for _ in range(warmup):
+        sess.advance(1)
+    torch.cuda.synchronize()
+    s0 = sess.stats()
+    for _ in range(steps):
+        if sess.advance(1) != 1:
+            break
+    s1 = sess.stats()
+    return float(s1[5] - s0[5]), int(s1[2] - s0[2])
+
+
+def extra_mixed(args):
+    """Config 3: the ~260k-transistor network (76,500 gates) with the FP32 LU
+    and FP64-residual refinement (3 sweeps), K adaptive steps after the DC
+    point; the same steps with the FP64 LU give the mixed run's error."""
+    K = args.extra_steps
+    gates = 76500
+    eng, nstats, depth = make_engine(gates, max_steps=K + 8, precision="mixed", refine=3)
+    dev = eng.device
+    info = dev.solver_info()
+    X0, Q0, I0, maxc0, ok = eng.initial_state()
+    if not ok:
+        return {"error": f"DC did not converge ({eng.dc_method})"}
+    cfg = eng.transient_cfg()
+    sess = dev.session(cfg, X0, Q0, I0, maxc0)
+    dev_ms, iters = _time_session(sess, 3, K)
+    out_m = sess.read()
+    sess.close()
+    dev.set_precision(0)
+    s64 = dev.session(cfg, X0, Q0, I0, maxc0)
+    ms64, it64 = _time_session(s64, 3, K)
+    out_d = s64.read()
+    s64.close()
+    dev.close()
+    n = min(out_m["n_steps"], out_d["n_steps"])
+    return {"workload": "random_gate_network_260k_transistors_adaptive_bdf2_mixed", "gates": gates,
+            "transistors": nstats.transistors, "n_unknowns": info["n_aug"], "nnz_lu": info["nnz_lu"],
+            "precision": "FP64 evaluation/residual/update/LTE, FP32 LU + 3 FP64 refinement sweeps",
+            "steps_timed": K, "ms_per_step": dev_ms / K, "newton_iters": iters,
+            "fp64_lu_ms_per_step": ms64 / K, "fp64_lu_newton_iters": it64,
+            "mixed_vs_fp64": {"max_abs_dv_V": float(np.max(np.abs(out_m["V"][:n] - out_d["V"][:n]))),
+                              "steps_compared": int(n),
+                              "times_identical": bool(np.array_equal(out_m["times"][:n], out_d["times"][:n]))},
+            "vs_oracle": "tests/test_config_parity.py::test_network_80k_mixed_precision_against_oracle "
+                         "(the 80k network, FP32 LU + 3 sweeps, within 1e-6 V of the FP64 oracle)"}
+
+
+def extra_configs(args):
+    """Every other configuration, each measured in this run."""
+    import torch
+    res = {}
+    for name, fn in (("config1_ring", extra_ring), ("config4_corners", extra_corners),
+                     ("config3_mixed_260k", extra_mixed), ("config5_serving", extra_serving)):
+        t0 = time.perf_counter()
+        try:
+            res[name] = fn(args)
+        except Exception as e:  # one failing configuration must not lose the others
+            res[name] = {"error": f"{type(e).__name__}: {e}"}
+        res[name]["seconds"] = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        log(name, json.dumps(res[name])[:400])
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -737,6 +954,11 @@ def main():
     ap.add_argument("--autotune", choices=["on", "off"], default="on",
                     help="tune launch shapes and the factorisation schedule before the run (outside the timing)")
     ap.add_argument("--reference-budget", type=float, default=150.0, help="seconds of timed CPU work, reference arm")
+    ap.add_argument("--extras", choices=["on", "off"], default="on",
+                    help="default workload on one GPU: also measure the ring, the corners, the 260k-T mixed-"
+                         "precision network and the serving stream, each under 'configs' in the JSON line")
+    ap.add_argument("--extra-steps", type=int, default=20, help="timed steps of the large extra configurations")
+    ap.add_argument("--extra-jobs", type=int, default=24, help="jobs of the serving stream inside the default run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         ap.error("--warmup must be >= 3")

@@ -51,6 +51,12 @@ int vgb_model_info(int id, char* name, int name_cap, int* nn, int* nj, int* np, 
  * counterpart in the reference (its models call XLA's math). */
 int vgb_math_eval(int fn, int n, const double* a, const double* b, double* out, vgb_stream_t stream);
 
+/* Measured FP64 FMA rate of the current device in GFLOP/s (2 flops per FMA):
+ * two CTAs per SM, each thread eight independent FMA chains of `iters`
+ * steps.  The denominator of the FP64 roofline fractions of the benchmark.
+ * No counterpart in the reference. */
+int vgb_fp64_rate(int iters, double* gflops);
+
 /* Circuit construction ------------------------------------------------------ */
 
 /* Create a circuit with n_nodes nodes (including ground) and the given

@@ -24,6 +24,7 @@ vp = C.c_void_p
 SIGNATURES = {
     "vgb_version": (C.c_int, []),
     "vgb_math_eval": (C.c_int, [C.c_int, C.c_int, vp, vp, vp, vp]),
+    "vgb_fp64_rate": (C.c_int, [C.c_int, f64p]),
     "vgb_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
     "vgb_batch_set_group": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
     "vgb_batch_set_sources": (C.c_int, [vp, C.c_int, vp]),

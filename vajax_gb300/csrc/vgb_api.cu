@@ -181,6 +181,13 @@ int vgb_math_eval(int fn, int n, const double* a, const double* b, double* out, 
     });
 }
 
+int vgb_fp64_rate(int iters, double* gflops) {
+    return guarded(nullptr, [&] {
+        VGB_REQUIRE(iters >= 8 && gflops, "vgb_fp64_rate: iters >= 8 and an output are required");
+        *gflops = measure_fp64_rate(iters, nullptr);
+    });
+}
+
 int vgb_num_models(void) {
     int n = 0;
     model_table(&n);

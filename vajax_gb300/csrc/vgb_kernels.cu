@@ -437,4 +437,46 @@ void launch_math_eval(int fn, int n, const double* a, const double* b, double* o
     if (n > 0) math_eval_kernel<<<ceil_div(n, 256), 256, 0, s>>>(fn, n, a, b, out);
 }
 
+// FP64 FMA throughput of the device: every SM runs warps of eight
+// independent dependent-FMA chains (the measured rate is the denominator of
+// the FP64 roofline fractions the benchmark reports).
+constexpr int FP64_RATE_THREADS = 512;
+__global__ void __launch_bounds__(FP64_RATE_THREADS) fp64_rate_kernel(int iters, double a, double b,
+                                                                      double* __restrict__ sink) {
+    double x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += x[c];
+    if (s == 12345.678) sink[blockIdx.x] = s;  // keeps the chains live; never true for these inputs
+}
+
+double measure_fp64_rate(int iters, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    VGB_CUDA(cudaGetDevice(&dev));
+    VGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* sink = nullptr;
+    VGB_CUDA(cudaMalloc(&sink, sizeof(double) * sms * 2));
+    cudaEvent_t e0, e1;
+    VGB_CUDA(cudaEventCreate(&e0));
+    VGB_CUDA(cudaEventCreate(&e1));
+    fp64_rate_kernel<<<sms * 2, FP64_RATE_THREADS, 0, s>>>(iters / 8, 0.9999999, 1e-9, sink);  // warm-up
+    VGB_CUDA(cudaEventRecord(e0, s));
+    fp64_rate_kernel<<<sms * 2, FP64_RATE_THREADS, 0, s>>>(iters, 0.9999999, 1e-9, sink);
+    VGB_CUDA(cudaEventRecord(e1, s));
+    VGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    VGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    const double flops = 2.0 * 8.0 * iters * (double)sms * 2 * FP64_RATE_THREADS;
+    return flops / (ms * 1e-3) / 1e9;
+}
+
 } // namespace vgb

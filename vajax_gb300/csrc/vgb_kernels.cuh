@@ -30,6 +30,7 @@ struct AssembleArgs {
 
 void launch_assemble(const AssembleArgs& a, cudaStream_t s);
 void launch_math_eval(int fn, int n, const double* a, const double* b, double* out, cudaStream_t s);
+double measure_fp64_rate(int iters, cudaStream_t s);
 
 struct NRUpdateArgs {
     int n_unk, n_aug;

@@ -368,9 +368,58 @@ class CircuitEngine:
         return TransientResult(times=out["times"], voltages=voltages, currents=currents, stats=stats)
 
 
+def _run_corners_replicas(self: CircuitEngine, corners, prepare_kwargs):
+    """Corners of a small circuit with a uic start on the batched engine: one
+    replica per corner, each with its own Newton iterations and time steps,
+    exactly as the corner would run alone.  None when the circuit does not
+    fit the engine."""
+    from vajax_gb300.batch import BatchedTransient, fits, same_pattern, uic_start
+    from vajax_gb300.corners import CornerResult, CornerSweepResult, batch_circuit
+    if self.options.icmode != "uic":
+        return None
+    rcs = [batch_circuit(self.circuit, [c]).resolve() for c in corners]
+    if not fits(rcs[0]) or not all(same_pattern(rcs[0], rc) for rc in rcs[1:]):
+        return None
+    t_stop, dt = prepare_kwargs.get("t_stop"), prepare_kwargs.get("dt")
+    if t_stop is None or dt is None:
+        return None
+    ref = CircuitEngine(batch_circuit(self.circuit, corners[:1]), self.options)
+    ref.rc = rcs[0]
+    ref.t_stop, ref.dt = float(t_stop), float(dt)
+    ref.config = ref._config(t_stop, dt, prepare_kwargs.get("adaptive_config"))
+    ms = prepare_kwargs.get("max_steps")
+    ref.max_steps = ms if ms is not None else int(t_stop / dt * 1.1) + 10
+    cfg = ref.transient_cfg()
+    ic = {f"c0.{n}": v for n, v in self.options.ic.items()}
+    X0 = np.stack([uic_start(rc, ic) for rc in rcs])
+    bt = BatchedTransient(rcs, gmin=self.options.gmin)
+    t0 = time.perf_counter()
+    try:
+        out = bt.transient(cfg, X0)
+    finally:
+        bt.close()
+    wall = time.perf_counter() - t0
+    results = []
+    for k, (corner, rc) in enumerate(zip(corners, rcs)):
+        n = int(out["n_steps"][k])
+        volts = {name[3:]: out["V"][k][:n, idx] for name, idx in rc.node_names.items()
+                 if 0 < idx < rc.n_external and name.startswith("c0.")}
+        curs = {name[3:]: out["I"][k][:n, j] for j, name in enumerate(rc.vsrc_names) if name.startswith("c0.")}
+        stats = dict(n_steps=n, total_timesteps=n, accepted_steps=n - 1 if cfg["fixed_step"] else n,
+                     rejected_steps=int(out["rejected"][k]), total_nr_iterations=int(out["total_nr_iters"][k]),
+                     nr_failures=int(out["nr_failures"][k]), wall_time=wall, batch=len(corners),
+                     engine="batched", device_ms=out["device_ms"])
+        ok = stats["nr_failures"] == 0 and all(np.all(np.isfinite(v)) for v in volts.values())
+        tr = TransientResult(times=out["times"][k][:n], voltages=volts, currents=curs, stats=stats)
+        results.append(CornerResult(corner=corner, result=tr, converged=ok, stats=stats))
+    return CornerSweepResult(corners=list(corners), results=results)
+
+
 def _run_corners(self: CircuitEngine, corners, analysis: str = "transient", **prepare_kwargs):
-    """All corners as one batched circuit in one transient run
-    (replaces the serial loop of engine.py:2235-2320).  ``prepare_kwargs``
+    """All corners in one run (replaces the serial loop of engine.py:2235-2320):
+    small circuits with a uic start on the batched engine (one replica per
+    corner, each with its own Newton iterations and steps), everything else
+    as one block-diagonal circuit in one transient run.  ``prepare_kwargs``
     are those of ``prepare()`` (t_stop, dt, adaptive_config, max_steps)."""
     import copy as _copy
 
@@ -379,6 +428,10 @@ def _run_corners(self: CircuitEngine, corners, analysis: str = "transient", **pr
         raise ValueError(f"Unsupported analysis type: {analysis}")
     if not corners:
         return CornerSweepResult(corners=[], results=[])
+    if not prepare_kwargs.pop("block_diagonal", False):
+        sweep = _run_corners_replicas(self, corners, prepare_kwargs)
+        if sweep is not None:
+            return sweep
     batched = batch_circuit(self.circuit, corners)
     opts = _copy.deepcopy(self.options)
     opts.ic = {f"c{k}.{n}": v for k in range(len(corners)) for n, v in self.options.ic.items()}

@@ -15,10 +15,14 @@ and memory.  Sessions use the host-driven step loop by default
 other groups' kernels interleave, and on the job stream of the benchmark it
 serves about twice the solves/s of one-graph-per-slice sessions.
 
-A job in a group of one gives bit-for-bit the result it gives alone (every
-kernel sums in a fixed order).  A job in a larger group shares the group's
-Newton iterations and time grid, which keeps its node voltages within the
-transient tolerance of its result alone.
+Groups of small circuits that start from initial conditions (rings) run on
+the batched engine (``vajax_gb300.batch``): every job is a replica with its
+own Newton iterations and time steps, so a job gives bit-for-bit the result
+it gives alone, whatever else is in its group.  Larger circuits run as one
+block-diagonal circuit: a job in a group of one gives bit-for-bit the result
+it gives alone (every kernel sums in a fixed order); a job in a larger group
+shares the group's Newton iterations and time grid, which keeps its node
+voltages within the transient tolerance of its result alone.
 
 Latency of a job = finish time - arrival time.  ``stats()`` reports p50/p99
 latency, jobs/s and Newton solves/s (per job: the Newton iterations it went
@@ -89,14 +93,63 @@ def estimate_footprint(info: Dict[str, int], precision: str = "fp64") -> int:
     return int(val * info["front_storage"] + 8 * (3 * info["contrib_slots"] + 2 * nnz) + 8 * 40 * n + (1 << 20))
 
 
+def _run_replicas(jobs: List[Job], circuits, reserve=None) -> Optional[int]:
+    """The group on the batched engine, one replica per job, when every job
+    is a small circuit with a uic start and fixed steps; else None."""
+    from vajax_gb300.batch import BatchedTransient, fits, same_pattern, uic_start
+    from vajax_gb300.engine import CircuitEngine, SimulationOptions, TransientResult
+    lead = jobs[0]
+    opts = SimulationOptions(**lead.options)
+    if opts.icmode != "uic" or not opts.fixed_step_transient:
+        return None
+    rcs = [j.resolved if j.resolved is not None else c.resolve() for j, c in zip(jobs, circuits)]
+    if not fits(rcs[0]) or not all(same_pattern(rcs[0], rc) for rc in rcs[1:]):
+        return None
+    eng = CircuitEngine(circuits[0], opts)
+    eng.rc = rcs[0]
+    eng.t_stop, eng.dt = lead.t_stop, lead.dt
+    eng.config = eng._config(lead.t_stop, lead.dt, None)
+    eng.max_steps = lead.max_steps
+    cfg = eng.transient_cfg()
+    R, n_ext = len(jobs), rcs[0].n_external
+    footprint = 8 * R * (lead.max_steps * (n_ext + len(rcs[0].vsources) + 1) + 4096) + (1 << 20)
+    if reserve is not None:
+        reserve(footprint)
+    t_adm = time.perf_counter()
+    X0 = np.stack([uic_start(rc, opts.ic) for rc in rcs])
+    bt = BatchedTransient(rcs, gmin=opts.gmin)
+    try:
+        out = bt.transient(cfg, X0)
+    finally:
+        bt.close()
+    for k, (j, rc) in enumerate(zip(jobs, rcs)):
+        n = int(out["n_steps"][k])
+        volts = {name: out["V"][k][:n, idx] for name, idx in rc.node_names.items() if 0 < idx < rc.n_external}
+        j.result = TransientResult(times=out["times"][k][:n], voltages=volts, currents={}, stats={
+            "n_steps": n, "rejected_steps": int(out["rejected"][k]),
+            "total_nr_iterations": int(out["total_nr_iters"][k]), "dc_method": "uic", "group_size": R,
+            "engine": "batched"})
+        j.newton_iters = int(out["total_nr_iters"][k])
+        j.group_size = R
+        j.admitted = t_adm
+        j.footprint = footprint // R
+        j.resolved = None
+    return footprint
+
+
 def run_group(jobs: List[Job], precision: str = "fp64", slice_steps: int = 50, reserve=None,
               transient_graph: bool = False):
-    """DC operating point + transient of a group of same-pattern jobs as one
-    batched circuit.  Fills each job's result; returns the reserved bytes."""
+    """DC operating point + transient of a group of same-pattern jobs: on the
+    batched engine (small circuits from initial conditions) or as one
+    block-diagonal circuit.  Fills each job's result; returns the reserved
+    bytes."""
     from vajax_gb300.corners import concat_circuits
     from vajax_gb300.engine import CircuitEngine, SimulationOptions, TransientResult
     lead = jobs[0]
     circuits = [j.circuit if j.circuit is not None else j.make_circuit() for j in jobs]
+    done = _run_replicas(jobs, circuits, reserve)
+    if done is not None:
+        return done
     single = len(jobs) == 1
     circuit = circuits[0] if single else concat_circuits(circuits)
     opts = dict(lead.options)
