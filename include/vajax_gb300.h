@@ -46,8 +46,9 @@ int vgb_model_info(int id, char* name, int name_cap, int* nn, int* nj, int* np, 
  * exp and log, Newton-Raphson division, pow through exp and log), evaluated
  * element-wise on the device, for accuracy tests against the host's libm.
  * fn: 0 a/b, 1 exp(a), 2 ln(a), 3 pow(a, b), 4 safe division (a/0 = 0, the
- * reference code generator's semantics, openvaf_jax/codegen/instruction.py).
- * a, b, out are device arrays of n doubles (b unused for fn 1 and 2).  No
+ * reference code generator's semantics, openvaf_jax/codegen/instruction.py),
+ * 5 1/a (the reciprocal on the factorisation's pivot chain).
+ * a, b, out are device arrays of n doubles (b unused for fn 1, 2 and 5).  No
  * counterpart in the reference (its models call XLA's math). */
 int vgb_math_eval(int fn, int n, const double* a, const double* b, double* out, vgb_stream_t stream);
 

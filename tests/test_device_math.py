@@ -62,6 +62,17 @@ def test_division_within_one_ulp(cuda):
 
 
 @pytest.mark.gpu
+def test_reciprocal_within_one_ulp(cuda):
+    rng = np.random.default_rng(6)
+    x = np.exp(rng.uniform(-700, 700, 1 << 18)) * rng.choice([-1, 1], 1 << 18)
+    with np.errstate(all="ignore"):
+        ref = 1.0 / x
+        assert _rel(_device_eval(5, x), ref) <= ULP
+        special = np.array([0.0, -0.0, np.inf, np.nan, 5e-324, 1e-310, 1e300])
+        assert _same_special(_device_eval(5, special), 1.0 / special)
+
+
+@pytest.mark.gpu
 def test_exp_within_two_ulp(cuda):
     rng = np.random.default_rng(2)
     x = np.concatenate([rng.uniform(-706, 706, 1 << 18), rng.uniform(-1, 1, 1 << 16),

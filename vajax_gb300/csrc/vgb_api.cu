@@ -174,8 +174,8 @@ int vgb_version(void) { return 100; }
 
 int vgb_math_eval(int fn, int n, const double* a, const double* b, double* out, vgb_stream_t stream) {
     return guarded(nullptr, [&] {
-        VGB_REQUIRE(fn >= 0 && fn <= 4 && n >= 0, "vgb_math_eval: fn must be 0..4 and n >= 0");
-        VGB_REQUIRE(n == 0 || (a && out && (b || fn == 1 || fn == 2)), "vgb_math_eval: missing array");
+        VGB_REQUIRE(fn >= 0 && fn <= 5 && n >= 0, "vgb_math_eval: fn must be 0..5 and n >= 0");
+        VGB_REQUIRE(n == 0 || (a && out && (b || fn == 1 || fn == 2 || fn == 5)), "vgb_math_eval: missing array");
         launch_math_eval(fn, n, a, b, out, (cudaStream_t)stream);
         VGB_CUDA(cudaGetLastError());
     });

@@ -27,6 +27,7 @@
 #include <cuda/atomic>
 #include <mutex>
 
+#include "vgb_fastdiv.cuh"
 #include "vgb_kernels.cuh"
 
 namespace vgb {
@@ -178,7 +179,8 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
             F[p + p * m] = piv;
             atomicOr(err, DEV_ERR_PIVOT);
         }
-        for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) F[i + p * m] /= piv;
+        const T rinv = vgb_rcp(piv);
+        for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) F[i + p * m] *= rinv;
         __syncthreads();
         for (int j = p + 1 + warp; j < m; j += nw) {
             const T u = F[p + j * m];
@@ -263,7 +265,7 @@ __device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T&
         if (lane == p) col = piv;
         if (lane == 0) atomicOr(err, DEV_ERR_PIVOT);
     }
-    r = (T)1 / piv;
+    r = vgb_rcp(piv);  // on the chain of dependent pivot steps: the short reciprocal
 }
 
 // The elimination steps below exchange the step's pivot column (or row) through a
@@ -324,7 +326,7 @@ template <typename T>
 __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     T* dinv = xch + 64;  // reciprocals of the diagonal, formed once in parallel
-    if (threadIdx.x < n) dinv[threadIdx.x] = (T)1 / d[threadIdx.x + threadIdx.x * LD];
+    if (threadIdx.x < n) dinv[threadIdx.x] = vgb_rcp(d[threadIdx.x + threadIdx.x * LD]);
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = x[lane + (g + NWARP * q) * LD];

@@ -416,7 +416,7 @@ void launch_eval_sources_dev(const Sources& src, int n, const double* t_dev, dou
 
 // The device elementary functions of the generated models, one per element
 // (accuracy tests of csrc/vgb_math.cuh).  fn: 0 a/b, 1 exp(a), 2 ln(a),
-// 3 pow(a, b), 4 the models' safe division (a/0 = 0).
+// 3 pow(a, b), 4 the models' safe division (a/0 = 0), 5 1/a.
 __global__ void math_eval_kernel(int fn, int n, const double* __restrict__ a, const double* __restrict__ b,
                                  double* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,7 +428,8 @@ __global__ void math_eval_kernel(int fn, int n, const double* __restrict__ a, co
         case 1: r = vgb_exp(x); break;
         case 2: r = vgb_log(x); break;
         case 3: r = vgb_pow(x, b[i]); break;
-        default: r = vgb_msdiv(x, b[i]); break;
+        case 4: r = vgb_msdiv(x, b[i]); break;
+        default: r = vgb_rcp(x); break;
     }
     out[i] = r;
 }

@@ -35,30 +35,10 @@
 
 #include <cuda_runtime.h>
 
+#include "vgb_fastdiv.cuh"
 #include "vgb_math_tables.cuh"
 
 namespace vgb {
-
-__device__ __forceinline__ double vgb_rcp_nr(double b) {
-    double y;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(b));
-    double e = fma(-b, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-b, y, 1.0);
-    return fma(y, e, y);
-}
-
-// a / b for finite a, b with |b| in [2^-500, 2^500) and |a| < 2^500 (the
-// quotient stays a normal number); everything else is the IEEE division.
-__device__ __forceinline__ double vgb_div(double a, double b) {
-    const int eb = (__double2hiint(b) >> 20) & 0x7ff;
-    const int ea = (__double2hiint(a) >> 20) & 0x7ff;
-    if (eb < 1023 - 500 || eb >= 1023 + 500 || ea >= 1023 + 500) return a / b;
-    const double y = vgb_rcp_nr(b);
-    const double q = a * y;
-    const double r = fma(-b, q, a);
-    return fma(r, y, q);
-}
 
 // The models' safe division (reference semantics: a / 0 = 0) on vgb_div.
 __device__ __forceinline__ double vgb_msdiv(double a, double b) {
