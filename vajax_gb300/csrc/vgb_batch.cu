@@ -263,8 +263,8 @@ __device__ __forceinline__ double cval(const BatchArgs& a, int idx, int r) {
 // in the same order as assemble_kernel): dense column-major M (if jac), f,
 // Q, maxc, fres in the warp's workspace; returns res_ok (residual test) and
 // sets *nonfinite.
-__device__ bool replica_assemble(const BatchArgs& a, const WarpWS& w, int r, const double* k, const double* floor_,
-                                 bool jac, bool* nonfinite, int lane) {
+__device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& w, int r, const double* k,
+                                              const double* floor_, bool jac, bool* nonfinite, int lane) {
     const int n = a.n_aug;
     const double* Xr = a.Xc;  // [n_x][n_rep]
     const double c0 = k[0], c1 = k[1], d1 = k[2], c2 = k[3], gshunt = k[4];
@@ -354,7 +354,7 @@ __device__ bool replica_assemble(const BatchArgs& a, const WarpWS& w, int r, con
 // diagonal keeps the reciprocal of each pivot, so that the dependent chain of
 // the back substitution has no division.  Returns 1 + the first column whose
 // pivot was zero or not finite (replaced by 1e-30), or 0.
-__device__ int replica_lu_solve(int n, double* M, double* b, int lane) {
+__device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int lane) {
     int bad = 0;
     for (int k = 0; k < n; ++k) {
         unsigned long long best = 0;
