@@ -13,8 +13,14 @@ use (``vajax/netlist/parser.py``; VACASK ``.sim`` grammar):
 * instances ``<name> (nodes) <master> k=v ...``; masters are subcircuits,
   ``model`` names, or modules (``vsource``, ``isource``, the compiled device
   models);
-* ``control ... endc``: ``analysis <name> tran step=.. stop=..`` is kept, the
-  rest skipped.
+* ``control ... endc``: ``analysis <name> tran step=.. stop=..`` and
+  ``elaborate circuit("name")`` (the subcircuit instantiated as the top level)
+  are kept, the rest skipped;
+* ``generate "name.py" <<<FILE ... >>>FILE``: the embedded Python script runs
+  at parse time with this interpreter (PEP 723 metadata stripped) and its
+  standard output replaces the block, as the reference's parser does
+  (``vajax/netlist/parser.py:651-700``).  A script that fails (for instance
+  one whose import is not installed) raises a NetlistError with its error.
 
 Parameter values are expressions over numbers with SI suffixes (``1u``,
 ``0.2n``), parameters in scope and ``+ - * / **`` and the usual functions,
@@ -29,6 +35,9 @@ import ast
 import math
 import operator
 import re
+import subprocess
+import sys
+import tempfile
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import Dict, List, Optional, Tuple
@@ -124,6 +133,7 @@ class Netlist:
     ground: str = "0"
     loads: List[str] = field(default_factory=list)
     analyses: List[Tuple[str, str, Dict[str, str]]] = field(default_factory=list)
+    elaborate: Optional[str] = None  # subcircuit elaborated as the top level
 
 
 def _strip_comments(text: str) -> str:
@@ -172,6 +182,31 @@ def _node_list(text: str) -> Tuple[List[str], str]:
     return text[1:close].replace(",", " ").split(), text[close + 1:].strip()
 
 
+_GENERATE = re.compile(r'generate\s+"([^"]+)"\s+<<<FILE\n(.*?)>>>FILE', re.DOTALL)
+_PEP723 = re.compile(r"^# /// script\n(?:#[^\n]*\n)*# ///\n", re.MULTILINE)
+
+
+def run_generate_blocks(text: str, base: Path, timeout: float = 120.0) -> str:
+    """Replace every generate block by the standard output of its script."""
+
+    def run(m: re.Match) -> str:
+        name, source = m.group(1), _PEP723.sub("", m.group(2), count=1)
+        with tempfile.TemporaryDirectory(prefix="vajax_gb300_generate_") as tmp:
+            script = Path(tmp) / Path(name).name
+            script.write_text(source)
+            r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, cwd=str(base),
+                               timeout=timeout)
+        if r.returncode != 0:
+            err = r.stderr.strip().splitlines()
+            last = err[-1] if err else f"exit status {r.returncode}"
+            mod = re.search(r"No module named '([^']+)'", r.stderr)
+            hint = f" (the script needs the Python package '{mod.group(1)}', which is not installed)" if mod else ""
+            raise NetlistError(f"generate block {name!r} failed{hint}: {last}")
+        return r.stdout
+
+    return _GENERATE.sub(run, text)
+
+
 def parse(text: str, base_path: Optional[Path] = None) -> Netlist:
     nl = Netlist()
     _parse_into(nl, text, base_path or Path("."))
@@ -179,6 +214,8 @@ def parse(text: str, base_path: Optional[Path] = None) -> Netlist:
 
 
 def _parse_into(nl: Netlist, text: str, base: Path):
+    if "<<<FILE" in text:
+        text = run_generate_blocks(text, base)
     lines = _join_paren_lines(_strip_comments(text).splitlines())
     stack: List[Subckt] = []
     in_control = False
@@ -195,6 +232,10 @@ def _parse_into(nl: Netlist, text: str, base: Path):
             elif word == "analysis":
                 parts = rest.split(None, 2)
                 nl.analyses.append((parts[0], parts[1], _kv(parts[2] if len(parts) > 2 else "")))
+            elif word == "elaborate":
+                m = re.search(r'circuit\(\s*"([^"]+)"\s*\)', rest)
+                if m:
+                    nl.elaborate = m.group(1)
             continue
         if word == "control":
             in_control = True
@@ -243,7 +284,8 @@ def _module(name: str) -> str:
     for k in model_keys():
         if k.lower() == key:
             return k
-    raise NetlistError(f"no compiled model for module '{name}'")
+    raise NetlistError(f"no compiled model for module '{name}': the library bundles {', '.join(model_keys())}; "
+                       f"a MIR/DAE fixture for '{name}' (vajax_gb300/devices/<name>.json) would add it")
 
 
 def to_circuit(nl: Netlist, temperature: float = 300.15) -> Circuit:
@@ -255,6 +297,17 @@ def to_circuit(nl: Netlist, temperature: float = 300.15) -> Circuit:
         scope[k] = evaluate(v, scope)
     glob = set(nl.globals) | {nl.ground, "0"}
     _expand(c, nl, nl.top, "", {}, scope, glob, depth=0)
+    if nl.elaborate:
+        # the elaborated subcircuit is the top level: its nets and instances keep their own names
+        sc = nl.subckts.get(nl.elaborate)
+        if sc is None:
+            raise NetlistError(f"elaborate: no subckt '{nl.elaborate}'")
+        if sc.ports:
+            raise NetlistError(f"elaborate: subckt '{nl.elaborate}' has ports")
+        inner = dict(scope)
+        for k, v in sc.params.items():
+            inner[k] = evaluate(v, inner)
+        _expand(c, nl, sc.body, "", {}, inner, glob, depth=1)
     return c
 
 
