@@ -293,13 +293,21 @@ int vgb_tran_destroy(void* session);
  *                I_out [n_rep][max_steps][max(n_vsrc,1)], stats [n_rep][8] =
  *                {n_steps, rejected, total_nr_iters, min_dt_used, max_dt_used,
  *                device_ms, nr_failures, pivot_failures}.
- *   info:        out[12] = {device ms of the last run, ticks, evaluation items,
+ *   set_coop:    enable (default) or disable the cooperative evaluation:
+ *                the models that carry a generated several-warp body (EKV)
+ *                are evaluated by groups of four warps, one per SM
+ *                sub-partition, that split each instance's dataflow graph
+ *                and exchange values through shared memory.  Disabled, one
+ *                warp evaluates 32 items.  Results agree to the last bits
+ *                (a multiply-add split between warps is not fused).
+ *   info:        out[13] = {device ms of the last run, ticks, evaluation items,
  *                contribution slots per replica, then SM clock cycles summed
  *                over the ticks of: evaluation, wait at the first grid
  *                barrier, per-replica step, wait at the second barrier (as
  *                the first CTA sees them), and, for replica 0: assembly of
  *                the Newton system, LU and solve, Newton update and test,
- *                step finish and plan}.
+ *                step finish and plan; then the number of item warps
+ *                evaluated cooperatively}.
  * Errors are reported through vgb_batch_last_error(b) (create: on h). */
 int vgb_batch_create(void* h, int n_rep, void** out_batch);
 int vgb_batch_set_group(void* b, int group, int n_varying, const int* varying_idx, const double* values,
@@ -307,6 +315,7 @@ int vgb_batch_set_group(void* b, int group, int n_varying, const int* varying_id
 int vgb_batch_set_sources(void* b, int is_current, const double* data);
 int vgb_batch_transient(void* b, const double* cfg, const double* X0, const double* Q0, const double* I0,
                         const double* maxc0, double* times, double* V_out, double* I_out, double* stats);
+int vgb_batch_set_coop(void* b, int enable);
 int vgb_batch_info(void* b, double* out);
 const char* vgb_batch_last_error(void* b);
 int vgb_batch_destroy(void* b);

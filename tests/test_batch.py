@@ -76,11 +76,39 @@ def test_batched_ring_all_20000_steps_match_oracle(cuda):
     cfg = G.tran_cfg(rc, True, M.RING_STEPS * 1e-12, 1e-12, M.RING_STEPS + 1)
     out = bt.transient(cfg, fx["X0"][None, :])
     bt.close()
+    assert out["coop_units"] >= 1  # the EKV devices went through the four-warp evaluation
     assert int(out["n_steps"][0]) == M.RING_STEPS + 1
     assert int(out["total_nr_iters"][0]) == int(fx["total_nr_iters"])
     np.testing.assert_allclose(out["times"][0][fx["rows"]], fx["times"], rtol=0, atol=1e-20)
     err = float(np.max(np.abs(out["V"][0][fx["rows"]] - fx["V"])))
     assert err < V_TOL, err
+
+
+@pytest.mark.gpu
+def test_cooperative_evaluation_matches_single_warp(cuda):
+    """96 ring corners (adaptive gear2, 0.4 ns) with the four-warp model
+    evaluation and with one warp per item: the same steps, rejections and
+    Newton iterations in every replica, step times within 1e-9 relative and
+    node voltages within 1e-9 V (a multiply-add split between warps is not
+    fused, so the last bits may differ)."""
+    from vajax_gb300.batch import BatchedTransient, uic_start
+    rcs = _ring_corners(96, 5)
+    rc = rcs[0]
+    cfg = G.tran_cfg(rc, False, 0.4e-9, 1e-12, 3000, max_dt=1e-10)
+    X0 = np.stack([uic_start(r, {"c0.n1": 1.2, "c0.vdd": 1.2}) for r in rcs])
+    outs = []
+    for coop in (True, False):
+        bt = BatchedTransient(rcs, coop=coop)
+        outs.append(bt.transient(cfg, X0))
+        bt.close()
+    a, b = outs
+    assert a["coop_units"] > 0 and b["coop_units"] == 0
+    for key in ("n_steps", "rejected", "total_nr_iters", "nr_failures"):
+        assert np.array_equal(a[key], b[key]), key
+    n = int(a["n_steps"].max())
+    # step control sees the last bits through the LTE estimate: times agree to the contract's 1e-9
+    np.testing.assert_allclose(a["times"][:, :n], b["times"][:, :n], rtol=1e-9)
+    assert float(np.max(np.abs(a["V"][:, :n] - b["V"][:, :n]))) < 1e-9
 
 
 @pytest.mark.gpu
@@ -97,6 +125,7 @@ def test_batched_ring_corners_match_oracle(cuda):
     X0 = np.stack([uic_start(r, {"c0.n1": 1.2, "c0.vdd": 1.2}) for r in rcs])
     out = bt.transient(cfg, X0)
     bt.close()
+    assert out["coop_units"] == (14 * M.CORNER_COUNT + 31) // 32
     assert np.all(out["n_steps"] == M.CORNER_STEPS + 1)
     worst = 0.0
     for k in fx["sample"]:

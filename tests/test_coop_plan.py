@@ -1,0 +1,242 @@
+"""The cooperative (four-warp) model evaluation plan, checked on the CPU.
+
+codegen/coop.py splits a model body over the warps of a group, which
+exchange values through shared-memory slots between named barriers.  These
+tests run the plan segment by segment in Python, with each warp's registers
+and the slot memory modelled explicitly:
+
+* every load must find the value it expects in its slot, whichever order the
+  warps take inside a segment (loads of all warps before any store; warps one
+  after another, forwards and backwards) -- a slot rewritten before its last
+  reader, or read before its writer, fails here;
+* every operand a warp uses must be in its registers (computed by it, or
+  loaded) when it is used;
+* the outputs must equal the oracle interpreter's, bit for bit (the same
+  numpy operations on the same values: the if-converted body computes every
+  value the branched one does);
+* every warp's generated code passes the same barriers, all at the top level
+  of its straight-line body.
+"""
+
+import json
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.mir_interp import MIRFunction
+from vajax_gb300.codegen.coop import CoopPlan, coop_plan
+
+DEVICES = Path(__file__).resolve().parents[1] / "vajax_gb300" / "devices"
+MODELS = ["ekv", "ekv_longchannel"]
+
+
+def _model(name):
+    return json.loads((DEVICES / f"{name}.json").read_text())
+
+
+def _inputs(model, n, seed):
+    """Parameter values in MIR order: defaults, TYPE of both signs, random
+    branch voltages over +-1.5 V and temperatures over -40..125 C."""
+    rng = np.random.default_rng(seed)
+    vals = []
+    for name, kind in zip(model["param_names"], model["param_kinds"]):
+        if kind == "voltage":
+            vals.append(rng.uniform(-1.5, 1.5, n))
+        elif kind == "temperature":
+            vals.append(rng.uniform(233.15, 398.15, n))
+        elif name == "TYPE":
+            vals.append(rng.choice([-1.0, 1.0], n))
+        else:
+            vals.append(np.full(n, float(model["param_defaults"][name])))
+    return vals
+
+
+def _simulate(plan, fn, vals, n, order):
+    """Run the plan; returns {output value: array}."""
+    env0 = {}
+    for k, v in fn.consts.items():
+        env0[k] = np.full(n, v, dtype=bool if isinstance(v, bool) else np.float64)
+    for pid, v in zip(fn.mir["params"], vals):
+        env0[pid] = np.asarray(v, np.float64)
+    W = plan.W
+    regs = [dict() for _ in range(W)]
+    slots = {}
+    act = np.ones(n, bool)
+
+    def get(w, v):
+        if plan.prog.is_value(v) or v.startswith(("a_", "e_")):
+            assert v in regs[w], f"warp {w} uses {v} before it has it"
+            return regs[w][v]
+        return env0[v]
+
+    def compute(w, node):
+        kind = plan.kind[node.val]
+        if kind == "inst":
+            op = node.inst["opcode"].lower()
+            return MIRFunction._apply(op, [get(w, o) for o in node.inst.get("operands", [])])
+        if kind == "phi":
+            out = None
+            for po in node.inst["phi_operands"]:
+                e = get(w, f"e_{po['block']}_{node.block}")
+                v = get(w, po["value"])
+                out = np.where(e, v, np.zeros_like(v) if out is None else out)
+            return out.astype(bool) if plan.types[node.val] == "bool" else out
+        if kind == "act":
+            if node.block == plan.entry:
+                return act.copy()
+            r = np.zeros(n, bool)
+            for p in plan.pred[node.block]:
+                r |= get(w, f"e_{p}_{node.block}")
+            return r
+        a = get(w, f"a_{node.block}")
+        c = plan.cond.get(node.block)
+        if c is None:
+            return a.copy()
+        cv = get(w, c).astype(bool)
+        first = node.val == f"e_{node.block}_{plan.succ[node.block][0]}"
+        return a & cv if first else a & ~cv
+
+    def do_loads(w, g):
+        for v, sg in plan.loads[w].items():
+            if sg == g:
+                name, val = slots.get(plan.slot[v], (None, None))
+                assert name == v, f"warp {w} segment {g}: slot {plan.slot[v]} holds {name}, expected {v}"
+                regs[w][v] = val
+
+    def do_nodes(w, g):
+        for node in sorted((x for x in plan.seq if x.owner == w and x.seg == g), key=lambda x: x.start):
+            with np.errstate(all="ignore"):
+                regs[w][node.val] = compute(w, node)
+            if node.val in plan.slot:
+                slots[plan.slot[node.val]] = (node.val, regs[w][node.val])
+
+    for g in range(plan.n_segments):
+        if order == "loads_first":
+            for w in range(W):
+                do_loads(w, g)
+            for w in range(W):
+                do_nodes(w, g)
+        else:
+            ws = range(W) if order == "forward" else reversed(range(W))
+            for w in ws:
+                do_loads(w, g)
+                do_nodes(w, g)
+    out = {}
+    for _, _, v in plan.prog.outputs:
+        if plan.prog.is_value(v):
+            out[v] = regs[plan.nodes[v].owner][v]
+    return out
+
+
+@pytest.mark.parametrize("name", MODELS)
+@pytest.mark.parametrize("order", ["loads_first", "forward", "backward"])
+def test_plan_matches_oracle_interpreter(name, order):
+    model = _model(name)
+    plan = CoopPlan(model)
+    fn = MIRFunction(model["mir"])
+    n = 96
+    vals = _inputs(model, n, seed=11)
+    ref = fn.run(vals, n)
+    got = _simulate(plan, fn, vals, n, order)
+    assert got
+    for v, arr in got.items():
+        r = ref[v]
+        assert np.array_equal(np.asarray(arr, np.float64), np.asarray(r, np.float64), equal_nan=True), v
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_generated_barriers_are_uniform(name):
+    plan = CoopPlan(_model(name))
+    src = plan.emit()
+    bodies = re.split(r"static void coop_w\d+\(", src)[1:]
+    assert len(bodies) == plan.W
+    call = f"vgb_coop_bar(bar, {32 * plan.W});"
+    for body in bodies:
+        body = body.split("static void coop(")[0]
+        lines = body.splitlines()
+        bars = [ln for ln in lines if call in ln]
+        assert len(bars) == plan.n_barriers
+        # straight-line: every barrier at the body's top level, and no branch
+        # before the output stores
+        assert all(ln == "        " + call for ln in bars)
+        head = body.split("if (act) {")[0]
+        assert not re.search(r"\b(if|for|while|goto|switch)\b", head.split("{", 1)[1])
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_plan_covers_every_output_once(name):
+    plan = CoopPlan(_model(name))
+    src = plan.emit()
+    idx = [int(m) for m in re.findall(r"out\((\d+),", src)]
+    assert sorted(idx) == sorted(i for i, _, _ in plan.prog.outputs)
+
+
+def test_plan_balance_and_size():
+    """EKV: the four parts within 10 % of each other, the modelled span under
+    30 % of the single-warp work, the exchange area within a CTA's shared
+    memory for two groups."""
+    plan = CoopPlan(_model("ekv"))
+    info = plan.info()
+    assert max(info["per_warp"]) < 1.1 * min(info["per_warp"])
+    assert info["makespan"] < 0.3 * info["work"]
+    assert 2 * plan.n_slots * 32 * 8 <= 227 * 1024
+
+
+def test_small_models_stay_single_warp():
+    assert coop_plan(_model("capacitor")) is None
+    assert coop_plan(_model("resistor")) is None
+
+
+def _coop_emulator():
+    """Generate the model header into tests/_build and compile
+    tests/emu/coop_emu.cpp against it with the host stand-ins."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    from vajax_gb300.codegen.cuda import write_generated
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    root = Path(__file__).resolve().parents[1]
+    out = root / "tests" / "_build" / "coop_emu"
+    out.mkdir(parents=True, exist_ok=True)
+    write_generated(DEVICES, out / "vgb_models_table.cu", out / "vgb_models_gen.cuh")
+    lib = out / f"libcoop_emu.{os.getpid()}.so"
+    subprocess.run([gxx, "-std=c++20", "-O1", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+                    "-I", str(root / "tests" / "emu" / "shim"), "-I", str(out),
+                    str(root / "tests" / "emu" / "coop_emu.cpp"), "-o", str(lib)], check=True, capture_output=True)
+    handle = C.CDLL(str(lib))
+    lib.unlink()
+    return handle
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_generated_cooperative_code_matches_single_thread_body(name):
+    """The emitted C of the four warp parts, compiled for the host and run as
+    four threads meeting at a barrier where the device code has its named
+    barrier: every output bit-identical to the single-thread body (both built
+    without contraction), over both transistor types, -40..125 C and +-1.5 V."""
+    import ctypes as C
+    from vajax_gb300.codegen.cuda import ModelSpec, _cname
+    lib = _coop_emulator()
+    model = _model(name)
+    spec = ModelSpec(model)
+    models = sorted(p.stem for p in DEVICES.glob("*.json"))
+    mid = models.index(name)
+    n = 48
+    rng = np.random.default_rng(7)
+    P = np.array([[float(model["param_defaults"][p]) for p in spec.user_params] for _ in range(n)])
+    if "TYPE" in spec.user_params:
+        P[:, spec.user_params.index("TYPE")] = rng.choice([-1.0, 1.0], n)
+    T = rng.uniform(233.15, 398.15, n)
+    V = rng.uniform(-1.5, 1.5, (n, len(spec.nodes)))
+    no = 2 * len(spec.jac) + 2 * len(spec.nodes)
+    plain, coop = np.zeros((n, no)), np.zeros((n, no))
+    dp = lambda x: np.ascontiguousarray(x).ctypes.data_as(C.POINTER(C.c_double))
+    Pc, Vc = np.ascontiguousarray(P), np.ascontiguousarray(V)
+    bad = lib.coop_emu_compare(mid, n, dp(Pc), dp(T), dp(Vc), dp(plain), dp(coop))
+    assert bad == 0, f"{bad} outputs differ ({_cname(name)})"
+    assert np.all(np.isfinite(plain))

@@ -30,6 +30,7 @@ SIGNATURES = {
     "vgb_batch_set_sources": (C.c_int, [vp, C.c_int, vp]),
     "vgb_batch_transient": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "vgb_batch_info": (C.c_int, [vp, vp]),
+    "vgb_batch_set_coop": (C.c_int, [vp, C.c_int]),
     "vgb_batch_last_error": (C.c_char_p, [vp]),
     "vgb_batch_destroy": (C.c_int, [vp]),
     "vgb_num_models": (C.c_int, []),

@@ -57,7 +57,7 @@ class BatchedTransient:
     """All replicas in one run.  ``replicas`` are resolved circuits of one
     pattern (``same_pattern``); the first is the template."""
 
-    def __init__(self, replicas: Sequence[ResolvedCircuit], gmin: float = 1e-12):
+    def __init__(self, replicas: Sequence[ResolvedCircuit], gmin: float = 1e-12, coop: bool = True):
         if not replicas:
             raise ValueError("no replicas")
         tpl = replicas[0]
@@ -77,6 +77,9 @@ class BatchedTransient:
         self.h = h
         self._keep = []
         try:
+            # cooperative evaluation: four warps share each instance of a model that has a generated
+            # several-warp body (results agree with coop=False to the last bits)
+            self._check(self.lib.vgb_batch_set_coop(self.h, int(bool(coop))))
             self._set_params()
             self._set_sources()
         except Exception:
@@ -133,12 +136,12 @@ class BatchedTransient:
         self._check(self.lib.vgb_batch_transient(self.h, _dp(c), _dp(X0),
                                                  *[None if a is None else _dp(a) for a in opt],
                                                  _dp(times), _dp(V), _dp(I), _dp(stats)))
-        info = np.zeros(12)
+        info = np.zeros(13)
         self._check(self.lib.vgb_batch_info(self.h, _dp(info)))
         return {"times": times, "V": V, "I": I, "n_steps": stats[:, 0].astype(np.int64),
                 "rejected": stats[:, 1].astype(np.int64), "total_nr_iters": stats[:, 2].astype(np.int64),
                 "nr_failures": stats[:, 6].astype(np.int64), "pivot_failures": stats[:, 7].astype(np.int64),
-                "device_ms": float(info[0]), "ticks": int(info[1]),
+                "device_ms": float(info[0]), "ticks": int(info[1]), "coop_units": int(info[12]),
                 "phase_cycles": dict(zip(("eval", "barrier1", "replica", "barrier2", "r0_assemble", "r0_lu",
                                           "r0_update", "r0_finish_plan"), info[4:12].tolist()))}
 

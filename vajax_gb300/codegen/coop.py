@@ -1,0 +1,417 @@
+"""Cooperative evaluation of a model body by several warps of one SM.
+
+GB300 issues one FP64 warp-instruction per 64 cycles on each of an SM's four
+sub-partitions, whatever the number of active lanes.  A model evaluated by
+one warp therefore takes (FP64 instructions x 64) cycles even when only one
+lane has an instance to evaluate, which is what bounds small batches (one
+ring oscillator, a few hundred corners).  The EKV body holds ~5,000 FP64
+instructions but its longest dependent chain is ~370, so four warps -- one
+per sub-partition -- can share one evaluation.
+
+The emitter partitions the MIR dataflow graph over ``W`` warps:
+
+* control flow is if-converted: every instruction runs for every lane, a
+  lane carries one flag per CFG edge (``reached the source block and took
+  this edge``) computed from the branch conditions, and a phi becomes a
+  select on the flags of its incoming edges.  The body is then one straight
+  line per warp, with no branch around any barrier.  The instructions of the
+  branches a lane does not take (about a tenth of the EKV body) are the
+  price;
+* the instructions are list-scheduled over the warps (earliest finish time,
+  priority = longest path to an output), with a cost per opcode in
+  FP64-instruction units and a fixed cost for a value that crosses to
+  another warp;
+* a value read by another warp goes through shared memory (one slot of 32
+  lane-interleaved doubles); a slot is reused by a value written after every
+  read of the previous one, by interval colouring over the segments between
+  barriers;
+* named barriers (``bar.sync id, 32 W``) separate the segments: the fewest
+  that put every cross-warp producer before its consumers (interval
+  stabbing).  Every warp executes every barrier, in the same order.
+
+Uses whose definitions do not dominate them (which a branched body would
+read as the initial 0) are refused, so that if-conversion cannot change a
+result.
+
+The generated struct members (inside the model's struct):
+
+* ``COOP_W`` warps and ``COOP_SLOTS`` exchange slots (32 doubles each);
+* ``coop_w0 .. coop_w{W-1}(P, T, V, xs, act, out, bar)``: warp w's part;
+  ``xs`` is the group's exchange area offset by the lane (a shared-memory
+  address: every access is a volatile ld/st.shared, vgb_xs_* in
+  csrc/vgb_eval.cuh, so that no load is served from this warp's own earlier
+  store or moved across a barrier), ``act`` whether the
+  lane has an instance, ``out(i, v)`` stores output ``i`` of the
+  [jr | jq | rr | rq] layout, ``bar`` the named barrier of the group;
+* ``coop(w, ...)``: dispatch on the warp index.
+"""
+
+from __future__ import annotations
+
+from typing import Dict, List, Tuple
+
+from vajax_gb300.codegen.cuda import MirProgram
+
+W_DEFAULT = 4
+DELTA = 1.0  # cost of handing a value to another warp (store, barrier, load), FP64-instruction units
+MIN_COST = 0.05
+# FP64-instruction equivalents per opcode, measured on GB300 for the
+# table-driven functions of csrc/vgb_math.cuh (division 8.7, exp 13.5,
+# log 17.8, pow 32); integer, predicate and select work is near free.
+COST = {"fmul": 1.0, "fadd": 1.0, "fsub": 1.0, "fneg": MIN_COST, "fdiv": 8.7, "sqrt": 10.0, "exp": 13.5,
+        "ln": 17.8, "log": 18.8, "pow": 32.0, "fmin": 1.0, "fmax": 1.0, "frem": 12.0,
+        "feq": 1.0, "fne": 1.0, "flt": 1.0, "fle": 1.0, "fgt": 1.0, "fge": 1.0,
+        "select": 0.1, "phi": 0.1, "bnot": MIN_COST, "fbcast": 1.0, "ibcast": 1.0, "bfcast": 0.1,
+        "bicast": 0.1, "ifcast": MIN_COST, "ficast": 1.0, "copy": MIN_COST, "optbarrier": MIN_COST,
+        "sin": 25.0, "cos": 25.0, "tan": 40.0, "sinh": 30.0, "cosh": 30.0, "tanh": 30.0, "asin": 30.0,
+        "acos": 30.0, "atan": 30.0, "atan2": 40.0, "hypot": 15.0, "asinh": 40.0, "acosh": 40.0,
+        "atanh": 40.0, "fabs": MIN_COST, "abs": MIN_COST, "floor": 1.0, "ceil": 1.0}
+
+
+class CoopUnsupported(Exception):
+    """The MIR has a shape the cooperative emitter does not handle (a back
+    edge, or a use its definition does not dominate)."""
+
+
+def _cost(op: str) -> float:
+    if op in ("iadd", "isub", "imul", "ineg", "ieq", "ine", "ilt", "ile", "igt", "ige", "beq", "bne"):
+        return 0.1
+    return max(COST.get(op, 1.0), MIN_COST)
+
+
+class _Node:
+    __slots__ = ("val", "inst", "phi", "deps", "cost", "block", "pos", "blevel", "owner", "start", "finish", "seg")
+
+    def __init__(self, val, inst, phi, deps, cost, block, pos):
+        self.val, self.inst, self.phi, self.deps, self.cost, self.block, self.pos = \
+            val, inst, phi, deps, cost, block, pos
+        self.blevel = 0.0
+        self.owner = -1
+        self.start = self.finish = 0.0
+        self.seg = 0
+
+
+class CoopPlan:
+    """The partition of one model body over ``W`` warps."""
+
+    def __init__(self, model: dict, W: int = W_DEFAULT, delta: float = DELTA, latency: float = 1.0):
+        self.W = W
+        self.delta = delta
+        self.latency = latency  # result latency of an op, in units of its issue cost
+        self.prog = MirProgram(model)
+        self._cfg()
+        self._nodes()
+        self._check_dominance()
+        self._liveness()
+        self._schedule()
+        self._exchange()
+
+    # ---- control flow ---------------------------------------------------------
+    def _cfg(self):
+        prog = self.prog
+        self.order = prog.order
+        pos = {b: i for i, b in enumerate(self.order)}
+        self.succ: Dict[str, List[str]] = {b: [] for b in self.order}
+        for b in self.order:
+            for inst in prog.insts_by_block[b]:
+                op = inst["opcode"].lower()
+                if op == "br":
+                    self.succ[b] = [inst["true_block"], inst["false_block"]]
+                elif op == "jmp":
+                    self.succ[b] = [inst["destination"]]
+        self.pred: Dict[str, List[str]] = {b: [] for b in self.order}
+        for b in self.order:
+            for s in self.succ[b]:
+                if s not in pos or pos[s] <= pos[b]:
+                    raise CoopUnsupported(f"edge {b} -> {s} is not forward in the block order")
+                if b not in self.pred[s]:
+                    self.pred[s].append(b)
+        self.entry = self.order[0]
+        if self.pred[self.entry]:
+            raise CoopUnsupported("the entry block has predecessors")
+        self.exits = [b for b in self.order if not self.succ[b]]
+        dom: Dict[str, set] = {}
+        for b in self.order:  # forward order is a topological order
+            ps = self.pred[b]
+            d = set.intersection(*(dom[p] for p in ps)) if ps else set()
+            dom[b] = d | {b}
+        self.dom = dom
+
+    def _nodes(self):
+        """One node per instruction, phi, block flag (a_B: the lane reached
+        B) and edge flag (e_B_S: the lane went from B to S), in an order
+        where every node follows its operands."""
+        prog = self.prog
+        self.nodes: Dict[str, _Node] = {}
+        self.seq: List[_Node] = []
+        self.cond: Dict[str, str] = {}
+        self.kind: Dict[str, str] = {}  # val -> "inst" | "phi" | "act" | "edge"
+        self.expr: Dict[str, str] = {}
+        self.types = dict(prog.types)
+        k = 0
+
+        def add(val, inst, phi, deps, cost, block, kind, expr=None):
+            nonlocal k
+            n = _Node(val, inst, phi, deps, cost, block, k)
+            k += 1
+            self.nodes[val] = n
+            self.seq.append(n)
+            self.kind[val] = kind
+            if expr is not None:
+                self.expr[val] = expr
+            return n
+
+        for b in self.order:
+            if b == self.entry:
+                add(f"a_{b}", None, False, [], MIN_COST, b, "act", "act")
+            else:
+                es = [f"e_{p}_{b}" for p in self.pred[b]]
+                add(f"a_{b}", None, False, es, MIN_COST, b, "act", " || ".join(es))
+            self.types[f"a_{b}"] = "bool"
+            for inst in prog.insts_by_block[b]:
+                op = inst["opcode"].lower()
+                if op == "phi":
+                    deps = [p["value"] for p in inst["phi_operands"] if prog.is_value(p["value"])]
+                    deps += [f"e_{p['block']}_{b}" for p in inst["phi_operands"]]
+                    add(inst["result"], inst, True, deps, _cost("phi") * len(inst["phi_operands"]), b, "phi")
+                elif op == "br":
+                    self.cond[b] = inst["condition"]
+                elif op in ("jmp", "exit"):
+                    pass
+                else:
+                    deps = [o for o in inst.get("operands", []) if prog.is_value(o)]
+                    add(inst["result"], inst, False, deps, _cost(op), b, "inst")
+            c = self.cond.get(b)
+            for j, s in enumerate(self.succ[b]):
+                deps = [f"a_{b}"]
+                if c is None:
+                    e = f"a_{b}"
+                else:
+                    if prog.is_value(c):
+                        deps.append(c)
+                    e = f"a_{b} && ({prog.opnd(c)})" if j == 0 else f"a_{b} && !({prog.opnd(c)})"
+                add(f"e_{b}_{s}", None, False, deps, MIN_COST, b, "edge", e)
+                self.types[f"e_{b}_{s}"] = "bool"
+
+    def _check_dominance(self):
+        prog = self.prog
+        for n in self.seq:
+            if self.kind[n.val] == "phi":
+                for po in n.inst["phi_operands"]:
+                    v, p = po["value"], po["block"]
+                    if prog.is_value(v) and self.nodes[v].block not in self.dom[p]:
+                        raise CoopUnsupported(f"phi {n.val}: {v} does not dominate the edge from {p}")
+            elif self.kind[n.val] == "inst":
+                for v in n.deps:
+                    d = self.nodes[v]
+                    if d.block not in self.dom[n.block] or (d.block == n.block and d.pos > n.pos):
+                        raise CoopUnsupported(f"{n.val}: operand {v} does not dominate its use")
+        for b, c in self.cond.items():
+            if prog.is_value(c) and self.nodes[c].block not in self.dom[b]:
+                raise CoopUnsupported(f"branch condition of {b} does not dominate the branch")
+        for _, _, v in prog.outputs:
+            if prog.is_value(v):
+                for e in self.exits:
+                    if self.nodes[v].block not in self.dom[e]:
+                        raise CoopUnsupported(f"output {v} does not dominate exit {e}")
+
+    def _liveness(self):
+        prog = self.prog
+        roots = [v for _, _, v in prog.outputs if prog.is_value(v)]
+        live, stack = set(), list(roots)
+        while stack:
+            v = stack.pop()
+            if v in live:
+                continue
+            live.add(v)
+            stack += self.nodes[v].deps
+        self.seq = [n for n in self.seq if n.val in live]
+        self.users: Dict[str, List[_Node]] = {}
+        for n in self.seq:
+            for d in n.deps:
+                self.users.setdefault(d, []).append(n)
+        for n in reversed(self.seq):
+            n.blevel = n.cost + max((u.blevel for u in self.users.get(n.val, [])), default=0.0)
+
+    # ---- scheduling -------------------------------------------------------------
+    def _schedule(self):
+        W = self.W
+        indeg = {n.val: len(set(n.deps)) for n in self.seq}
+        ready = [n for n in self.seq if indeg[n.val] == 0]
+        free = [0.0] * W
+        self.work = [0.0] * W
+        done = 0
+        import heapq
+        heap = [(-n.blevel, n.pos, n.val) for n in ready]
+        heapq.heapify(heap)
+        while heap:
+            _, _, v = heapq.heappop(heap)
+            n = self.nodes[v]
+            best = None
+            for w in range(W):
+                est = free[w]
+                for d in n.deps:
+                    p = self.nodes[d]
+                    est = max(est, p.finish + (0.0 if p.owner == w else self.delta))
+                key = (est, free[w], w)
+                if best is None or key < best[0]:
+                    best = (key, w, est)
+            _, w, est = best
+            n.owner, n.start, n.finish = w, est, est + n.cost * self.latency
+            free[w] = est + n.cost
+            self.work[w] += n.cost
+            done += 1
+            for u in self.users.get(v, []):
+                indeg[u.val] -= 1
+                if indeg[u.val] == 0:
+                    heapq.heappush(heap, (-u.blevel, u.pos, u.val))
+        if done != len(self.seq):
+            raise CoopUnsupported("the dataflow graph has a cycle")
+        self.makespan = max(max(free), max((n.finish for n in self.seq), default=0.0))
+        # barriers: stab every cross-warp interval [finish(producer), start(consumer)]
+        iv = sorted(((self.nodes[d].finish, n.start) for n in self.seq for d in n.deps
+                     if self.nodes[d].owner != n.owner), key=lambda t: t[1])
+        taus: List[float] = []
+        for lo, hi in iv:
+            if not (taus and lo <= taus[-1] <= hi):
+                taus.append(hi)
+        import bisect
+        for n in self.seq:
+            n.seg = bisect.bisect_right(taus, n.start)  # barriers at or before the node's start
+        self.n_barriers = len(taus)
+        self.n_segments = len(taus) + 1
+
+    # ---- exchange slots ----------------------------------------------------------
+    def _exchange(self):
+        # first read of each cross value by each other warp (a loaded copy stays in a register)
+        self.loads: Dict[int, Dict[str, int]] = {w: {} for w in range(self.W)}
+        last_read: Dict[str, int] = {}
+        for n in self.seq:
+            for d in n.deps:
+                p = self.nodes[d]
+                if p.owner == n.owner:
+                    continue
+                if p.seg >= n.seg:
+                    raise CoopUnsupported(f"{d} is read in its own segment")
+                m = self.loads[n.owner]
+                if d not in m or n.seg < m[d]:
+                    m[d] = n.seg
+                last_read[d] = max(last_read.get(d, -1), n.seg)
+        for w in range(self.W):  # a warp's first read is its only read
+            for d, g in self.loads[w].items():
+                assert g <= last_read[d]
+        last_read = {d: max(g for w in range(self.W) for v, g in self.loads[w].items() if v == d)
+                     for d in last_read}
+        cross = sorted(last_read, key=lambda v: self.nodes[v].seg)
+        slot_free_after: List[int] = []
+        self.slot: Dict[str, int] = {}
+        for v in cross:
+            wseg = self.nodes[v].seg
+            for s, fa in enumerate(slot_free_after):
+                if fa < wseg:
+                    self.slot[v] = s
+                    slot_free_after[s] = last_read[v]
+                    break
+            else:
+                self.slot[v] = len(slot_free_after)
+                slot_free_after.append(last_read[v])
+        self.n_slots = max(len(slot_free_after), 1)
+        self.last_read = last_read
+
+    # ---- emission ------------------------------------------------------------------
+    def info(self) -> dict:
+        return {"warps": self.W, "work": sum(self.work), "per_warp": list(self.work), "makespan": self.makespan,
+                "barriers": self.n_barriers, "slots": self.n_slots, "cross_values": len(self.slot)}
+
+    def emit(self) -> str:
+        parts = [f"    static constexpr int COOP_W = {self.W};",
+                 f"    static constexpr int COOP_SLOTS = {self.n_slots};",
+                 f"    static constexpr int COOP_BARRIERS = {self.n_barriers};"]
+        for w in range(self.W):
+            parts.append(self._emit_warp(w))
+        cases = " ".join(f"case {w}: coop_w{w}(P, T, V, xs, act, out, bar); break;" for w in range(self.W))
+        parts.append(f"""    template <class PF, class OF>
+    __device__ __forceinline__ static void coop(int w, const PF& P, double T, const double* __restrict__ V,
+                                                vgb_xs_t xs, bool act, const OF& out, int bar)
+    {{
+        switch (w) {{ {cases} default: break; }}
+    }}
+""")
+        return "\n".join(parts)
+
+    def _line(self, n: _Node) -> str:
+        prog = self.prog
+        kind = self.kind[n.val]
+        if kind == "inst":
+            return f"{n.val} = {prog.expr(n.inst)};"
+        if kind == "phi":
+            sel = "false" if self.types[n.val] == "bool" else "0.0"
+            for po in reversed(n.inst["phi_operands"]):
+                sel = f"(e_{po['block']}_{n.block} ? {prog.opnd(po['value'])} : {sel})"
+            return f"{n.val} = {sel};"
+        return f"{n.val} = {self.expr[n.val]};"
+
+    def _emit_warp(self, w: int) -> str:
+        types = self.types
+        ind = "        "
+        mine = [n for n in self.seq if n.owner == w]
+        used = {n.val for n in mine} | set(self.loads[w])
+        key = lambda v: (v[0], int(v[1:]) if v[1:].isdigit() else 0, v)
+        dbl = sorted((v for v in used if types[v] == "double"), key=key)
+        bol = sorted((v for v in used if types[v] == "bool"), key=key)
+        lines: List[str] = []
+        for i in range(0, len(dbl), 16):
+            lines.append(ind + "double " + ", ".join(dbl[i:i + 16]) + ";")
+        for i in range(0, len(bol), 16):
+            lines.append(ind + "bool " + ", ".join(bol[i:i + 16]) + ";")
+        by_seg: Dict[int, List[_Node]] = {}
+        for n in sorted(mine, key=lambda n: n.start):
+            by_seg.setdefault(n.seg, []).append(n)
+        loads_by_seg: Dict[int, List[str]] = {}
+        for v, g in self.loads[w].items():
+            loads_by_seg.setdefault(g, []).append(v)
+        for g in range(self.n_segments):
+            for v in sorted(loads_by_seg.get(g, []), key=key):
+                s = self.slot[v]
+                if types[v] == "bool":
+                    lines.append(ind + f"{v} = vgb_xs_ldb(xs, {32 * s});")
+                else:
+                    lines.append(ind + f"{v} = vgb_xs_ld(xs, {32 * s});")
+            for n in by_seg.get(g, []):
+                lines.append(ind + self._line(n))
+                if n.val in self.slot:
+                    s = self.slot[n.val]
+                    if types[n.val] == "bool":
+                        lines.append(ind + f"vgb_xs_stb(xs, {32 * s}, {n.val});")
+                    else:
+                        lines.append(ind + f"vgb_xs_st(xs, {32 * s}, {n.val});")
+            if g + 1 < self.n_segments:
+                lines.append(ind + f"vgb_coop_bar(bar, {32 * self.W});")
+        prog = self.prog
+        outs = [(i, v) for i, _, v in prog.outputs
+                if (prog.is_value(v) and self.nodes[v].owner == w) or (not prog.is_value(v) and w == 0)]
+        if outs:
+            lines.append(ind + "if (act) {")
+            for i, v in outs:
+                lines.append(ind + f"    out({i}, {prog.opnd(v)});")
+            lines.append(ind + "}")
+        body = "\n".join(lines)
+        return f"""    template <class PF, class OF>
+    __device__ __noinline__ static void coop_w{w}(const PF& P, double T, const double* __restrict__ V,
+                                                  vgb_xs_t xs, bool act, const OF& out, int bar)
+    {{
+{body}
+    }}
+"""
+
+
+def coop_plan(model: dict, W: int = W_DEFAULT, min_work: float = 400.0):
+    """The cooperative plan of a model, or None when the body is too small to
+    gain from more than one warp (or has a shape the emitter does not take)."""
+    try:
+        plan = CoopPlan(model, W)
+    except CoopUnsupported:
+        return None
+    if sum(plan.work) < min_work:
+        return None
+    return plan

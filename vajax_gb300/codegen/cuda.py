@@ -76,7 +76,124 @@ class ModelSpec:
         self.user_params = [n for n, k in zip(self.param_names, self.param_kinds) if k == "param"]
 
 
-def emit_model(model: dict, fn_name: str | None = None) -> str:
+class MirProgram:
+    """One model's MIR prepared for emission: blocks in topological order,
+    the instructions of each block, the C type of every value, the phi moves
+    of every CFG edge, operand rendering and the outputs (residuals and
+    Jacobian entries) with the values that hold them."""
+
+    def __init__(self, model: dict):
+        self.spec = spec = ModelSpec(model)
+        self.mir = mir = model["mir"]
+        self.blocks = list(mir["blocks"].keys())
+        self.order = _topo(mir)  # deterministic topological block order, entry first
+        self.insts_by_block: Dict[str, list] = {b: [] for b in self.blocks}
+        for inst in mir["instructions"]:
+            self.insts_by_block[inst["block"]].append(inst)
+        self.consts = {k: float(v) for k, v in mir.get("constants", {}).items()}
+        self.bconsts = {k: bool(v) for k, v in mir.get("bool_constants", {}).items()}
+        self.iconsts = {k: float(v) for k, v in mir.get("int_constants", {}).items()}
+        self.types = self._types()
+        params = mir["params"]
+        self.pkind = dict(zip(params, spec.param_kinds))
+        self.pname = dict(zip(params, spec.param_names))
+        self.user_index = {n: i for i, n in enumerate(spec.user_params)}
+        self.volt_index = {}
+        vi = 0
+        for pid, k in zip(params, spec.param_kinds):
+            if k == "voltage":
+                self.volt_index[pid] = vi
+                vi += 1
+        # phi assignments grouped per (pred, succ)
+        self.phi_moves: Dict[tuple, list] = {}
+        for b in self.blocks:
+            for inst in self.insts_by_block[b]:
+                if inst["opcode"].lower() == "phi":
+                    for po in inst["phi_operands"]:
+                        self.phi_moves.setdefault((po["block"], b), []).append((inst["result"], po["value"]))
+        dae = model["dae"]
+        nn, nj = len(spec.nodes), len(spec.jac)
+        # (index in the [jr | jq | rr | rq] output layout, C name, MIR value)
+        self.outputs = []
+        for k, j in enumerate(dae["jacobian"]):
+            self.outputs.append((k, f"jr[{k}]", _mir_key(j["resist_var"])))
+            self.outputs.append((nj + k, f"jq[{k}]", _mir_key(j["react_var"])))
+        for k, res in enumerate(dae["residuals"]):
+            self.outputs.append((2 * nj + k, f"rr[{k}]", _mir_key(res["resist_var"])))
+            self.outputs.append((2 * nj + nn + k, f"rq[{k}]", _mir_key(res["react_var"])))
+
+    def _types(self) -> Dict[str, str]:
+        types: Dict[str, str] = {}
+        insts = self.mir["instructions"]
+        for inst in insts:
+            if "result" not in inst:
+                continue
+            op = inst["opcode"].lower()
+            if op in _CMP or op in ("bnot", "fbcast", "ibcast"):
+                types[inst["result"]] = "bool"
+            elif op in ("select", "phi"):
+                types[inst["result"]] = None  # resolved below
+            else:
+                types[inst["result"]] = "double"
+        # resolve select/phi types from operands (iterate to a fixed point)
+        changed = True
+        while changed:
+            changed = False
+            for inst in insts:
+                r = inst.get("result")
+                if r is None or types.get(r) is not None:
+                    continue
+                op = inst["opcode"].lower()
+                srcs = ([inst["operands"][1], inst["operands"][2]] if op == "select"
+                        else [p["value"] for p in inst["phi_operands"]])
+                ts = {types.get(s) if s in types else ("bool" if s in self.bconsts else "double") for s in srcs}
+                ts.discard(None)
+                if ts:
+                    types[r] = "bool" if ts == {"bool"} else "double"
+                    changed = True
+        return {k: (v or "double") for k, v in types.items()}
+
+    def is_value(self, v: str) -> bool:
+        """True for the result of an instruction (as opposed to a constant,
+        a parameter, a voltage or the temperature)."""
+        return v in self.types
+
+    def opnd(self, v: str) -> str:
+        if v in self.consts:
+            return _lit(self.consts[v])
+        if v in self.bconsts:
+            return "true" if self.bconsts[v] else "false"
+        if v in self.iconsts:
+            return _lit(self.iconsts[v])
+        if v in self.pkind:
+            k = self.pkind[v]
+            if k == "voltage":
+                a, b = self.spec.voltage_pairs[self.volt_index[v]]
+                return f"(V[{a}] - V[{b}])" if b >= 0 else f"V[{a}]"
+            if k == "temperature":
+                return "T"
+            if k == "param":
+                return f"P({self.user_index[self.pname[v]]})"
+            return "0.0"
+        return v
+
+    def expr(self, inst: dict, opnd=None) -> str:
+        opnd = opnd or self.opnd
+        return _expr(inst["opcode"].lower(), [opnd(o) for o in inst.get("operands", [])])
+
+    def struct_header(self, name: str) -> str:
+        spec = self.spec
+        jrow = ", ".join(str(r) for r, _ in spec.jac) or "0"
+        jcol = ", ".join(str(c) for _, c in spec.jac) or "0"
+        return f"""    static constexpr int NN = {len(spec.nodes)};
+    static constexpr int NJ = {len(spec.jac)};
+    static constexpr int NP = {len(spec.user_params)};
+    static constexpr int JROW[] = {{{jrow}}};
+    static constexpr int JCOL[] = {{{jcol}}};
+"""
+
+
+def emit_model(model: dict, fn_name: str | None = None, extra: str = "") -> str:
     """Return CUDA source for one model.
 
     The generated ``struct`` exposes:
@@ -87,104 +204,26 @@ def emit_model(model: dict, fn_name: str | None = None) -> str:
     * ``eval(P, T, V, rr, rq, jr, jq)``: ``P(k)`` returns user parameter ``k``,
       ``T`` is the temperature in kelvin, ``V[n]`` the node voltages of the
       instance; outputs are written to the four arrays.
+
+    ``extra`` is appended inside the struct (the cooperative evaluation of
+    codegen/coop.py).
     """
-    spec = ModelSpec(model)
-    mir = model["mir"]
+    prog = MirProgram(model)
+    spec = prog.spec
     name = fn_name or f"Model_{_cname(spec.name)}"
-    blocks = list(mir["blocks"].keys())
-    # keep a deterministic topological block order (entry first)
-    order = _topo(mir)
-    insts_by_block: Dict[str, list] = {b: [] for b in blocks}
-    for inst in mir["instructions"]:
-        insts_by_block[inst["block"]].append(inst)
-
-    consts = {k: float(v) for k, v in mir.get("constants", {}).items()}
-    bconsts = {k: bool(v) for k, v in mir.get("bool_constants", {}).items()}
-    iconsts = {k: float(v) for k, v in mir.get("int_constants", {}).items()}
-
-    types: Dict[str, str] = {}
-    for inst in mir["instructions"]:
-        if "result" not in inst:
-            continue
-        op = inst["opcode"].lower()
-        if op in _CMP or op in ("bnot", "fbcast", "ibcast"):
-            types[inst["result"]] = "bool"
-        elif op == "select":
-            types[inst["result"]] = None  # resolved below
-        elif op == "phi":
-            types[inst["result"]] = None
-        else:
-            types[inst["result"]] = "double"
-    # resolve select/phi types from operands (iterate to a fixed point)
-    changed = True
-    while changed:
-        changed = False
-        for inst in mir["instructions"]:
-            r = inst.get("result")
-            if r is None or types.get(r) is not None:
-                continue
-            op = inst["opcode"].lower()
-            srcs = ([inst["operands"][1], inst["operands"][2]] if op == "select"
-                    else [p["value"] for p in inst["phi_operands"]])
-            ts = {types.get(s) if s in types else ("bool" if s in bconsts else "double") for s in srcs}
-            ts.discard(None)
-            if ts:
-                types[r] = "bool" if ts == {"bool"} else "double"
-                changed = True
-    for k, v in types.items():
-        if v is None:
-            types[k] = "double"
-
-    params = mir["params"]
-    pkind = dict(zip(params, spec.param_kinds))
-    pname = dict(zip(params, spec.param_names))
-    user_index = {n: i for i, n in enumerate(spec.user_params)}
-    volt_index = {}
-    vi = 0
-    for pid, k in zip(params, spec.param_kinds):
-        if k == "voltage":
-            volt_index[pid] = vi
-            vi += 1
-
-    def opnd(v: str) -> str:
-        if v in consts:
-            return _lit(consts[v])
-        if v in bconsts:
-            return "true" if bconsts[v] else "false"
-        if v in iconsts:
-            return _lit(iconsts[v])
-        if v in pkind:
-            k = pkind[v]
-            if k == "voltage":
-                a, b = spec.voltage_pairs[volt_index[v]]
-                return f"(V[{a}] - V[{b}])" if b >= 0 else f"V[{a}]"
-            if k == "temperature":
-                return "T"
-            if k == "param":
-                return f"P({user_index[pname[v]]})"
-            return "0.0"
-        return v
+    types, opnd = prog.types, prog.opnd
 
     lines: List[str] = []
     ind = "        "
-    declared = [r for r in types]
-    dbl = [r for r in declared if types[r] == "double"]
-    bol = [r for r in declared if types[r] == "bool"]
+    dbl = [r for r in types if types[r] == "double"]
+    bol = [r for r in types if types[r] == "bool"]
     for i in range(0, len(dbl), 16):
         lines.append(ind + "double " + ", ".join(f"{v} = 0.0" for v in dbl[i:i + 16]) + ";")
     for i in range(0, len(bol), 16):
         lines.append(ind + "bool " + ", ".join(f"{v} = false" for v in bol[i:i + 16]) + ";")
 
-    # phi assignments grouped per (pred, succ)
-    phi_moves: Dict[tuple, list] = {}
-    for b in blocks:
-        for inst in insts_by_block[b]:
-            if inst["opcode"].lower() == "phi":
-                for po in inst["phi_operands"]:
-                    phi_moves.setdefault((po["block"], b), []).append((inst["result"], po["value"]))
-
     def moves(pred, succ) -> List[str]:
-        mv = phi_moves.get((pred, succ), [])
+        mv = prog.phi_moves.get((pred, succ), [])
         if not mv:
             return []
         # parallel copy semantics: read all sources first
@@ -197,9 +236,9 @@ def emit_model(model: dict, fn_name: str | None = None) -> str:
         out += [f"{dst} = {t};" for dst, t in tmps]
         return ["{ " + " ".join(out) + " }"]
 
-    for b in order:
+    for b in prog.order:
         lines.append(f"    {b}:;")
-        for inst in insts_by_block[b]:
+        for inst in prog.insts_by_block[b]:
             op = inst["opcode"].lower()
             if op == "phi":
                 continue
@@ -217,33 +256,14 @@ def emit_model(model: dict, fn_name: str | None = None) -> str:
             if op == "exit":
                 lines.append(ind + "goto done;")
                 continue
-            r = inst["result"]
-            a = [opnd(o) for o in inst.get("operands", [])]
-            lines.append(ind + f"{r} = {_expr(op, a)};")
+            lines.append(ind + f"{inst['result']} = {prog.expr(inst)};")
     lines.append("    done:;")
+    outs = [f"        {cname} = {opnd(v)};" for _, cname, v in prog.outputs]
 
-    dae = model["dae"]
-    outs = []
-    for k, res in enumerate(dae["residuals"]):
-        outs.append(f"        rr[{k}] = {opnd(_mir_key(res['resist_var']))};")
-        outs.append(f"        rq[{k}] = {opnd(_mir_key(res['react_var']))};")
-    for k, j in enumerate(dae["jacobian"]):
-        outs.append(f"        jr[{k}] = {opnd(_mir_key(j['resist_var']))};")
-        outs.append(f"        jq[{k}] = {opnd(_mir_key(j['react_var']))};")
-
-    nn = len(spec.nodes)
-    nj = len(spec.jac)
-    jrow = ", ".join(str(r) for r, _ in spec.jac) or "0"
-    jcol = ", ".join(str(c) for _, c in spec.jac) or "0"
     src = f"""
 // Generated from the MIR of Verilog-A module '{spec.name}'.
 struct {name} {{
-    static constexpr int NN = {nn};
-    static constexpr int NJ = {nj};
-    static constexpr int NP = {len(spec.user_params)};
-    static constexpr int JROW[] = {{{jrow}}};
-    static constexpr int JCOL[] = {{{jcol}}};
-
+{prog.struct_header(name)}
     template <class PF>
     __device__ __forceinline__ static void eval(const PF& P, double T, const double* __restrict__ V,
                                                 double* rr, double* rq, double* jr, double* jq)
@@ -251,7 +271,7 @@ struct {name} {{
 {chr(10).join(lines)}
 {chr(10).join(outs)}
     }}
-}};
+{extra}}};
 """
     return src
 
@@ -320,15 +340,25 @@ def load_model(path) -> dict:
 def emit_header(models: Dict[str, dict]) -> str:
     """The model structs, plus an X-macro VGB_MODEL_LIST(X) that expands
     X(id, struct) for every model in model-table order, so that other
-    translation units (the batched engine) can dispatch on a model id."""
+    translation units (the batched engine) can dispatch on a model id, and
+    VGB_COOP_LIST(X) for the models that also carry a cooperative evaluation
+    (codegen/coop.py)."""
+    from vajax_gb300.codegen.coop import coop_plan
     parts = ["#pragma once", '#include "vgb_eval.cuh"', '#include "vgb_math.cuh"', "namespace vgb {"]
-    names = []
-    for key, m in models.items():
+    names, coop, slots = [], [], 1
+    for i, (key, m) in enumerate(models.items()):
         sname = f"Model_{_cname(key)}"
-        parts.append(emit_model(m, sname))
+        plan = coop_plan(m)
+        parts.append(emit_model(m, sname, plan.emit() if plan else ""))
         names.append(sname)
+        if plan:
+            coop.append(f"X({i}, {sname})")
+            slots = max(slots, plan.n_slots)
     parts.append("} // namespace vgb")
     parts.append("#define VGB_MODEL_LIST(X) " + " ".join(f"X({i}, {n})" for i, n in enumerate(names)))
+    parts.append("// models with a cooperative (several-warp) evaluation, and the most exchange slots any needs")
+    parts.append("#define VGB_COOP_LIST(X) " + " ".join(coop))
+    parts.append(f"#define VGB_COOP_SLOTS_MAX {slots}")
     return "\n".join(parts) + "\n"
 
 

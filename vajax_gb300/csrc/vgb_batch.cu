@@ -46,6 +46,7 @@ constexpr int BATCH_MAX_N = 48;       // n_aug limit: each warp's dense system l
 constexpr int BATCH_THREADS = 256;
 constexpr int BATCH_MAX_GROUPS = 16;
 constexpr unsigned BARRIER_POLLS = 1u << 26;
+constexpr int COOP_WARPS = 4;  // warps that share one cooperative evaluation: one per SM sub-partition
 
 // Replica states between ticks: INIT (uic start: charges from the evaluation
 // at X0), START (given initial state: step 1 from X0), NR (a Newton
@@ -62,6 +63,7 @@ struct BGroup {
     double temp_shared;
     long long cbase;         // first contribution slot of the group
     long long item0;         // first evaluation item of the group
+    long long cu0, cu1;      // its cooperative units [cu0, cu1) (empty: one warp per item warp)
 };
 
 // Per-replica controller state (field names as ctl_plan / ctl_finish expect).
@@ -83,6 +85,8 @@ struct BatchArgs {
     int n_rep, n_nodes, n_unk, n_vsrc, n_isrc, n_aug, n_x, n_ext, nvo, nnz;
     int n_groups;
     long long n_items, n_contrib;
+    long long n_coop_units;  // item warps evaluated by a group of COOP_WARPS warps
+    long long coop_stride;   // doubles of shared memory per group (exchange slots x 32 lanes)
     double gmin, reltol, abstol, vntol, damping;
     const BGroup* groups;
     // pattern and gather lists (one replica)
@@ -187,11 +191,66 @@ __device__ __noinline__ void eval_item(const BatchArgs& a, const BGroup& g, int 
     }
 }
 
+// Output sink of a cooperative evaluation: output i of the [jr | jq | rr | rq]
+// layout of instance (d, r).
+struct CoopOut {
+    double* base;
+    size_t sd, o;
+    __device__ __forceinline__ void operator()(int i, double v) const { __stcg(base + (size_t)i * sd + o, v); }
+};
+
+// One item warp evaluated by the COOP_WARPS warps of a group (this warp is
+// part w).  Lanes without an instance (padding, or a replica that needs no
+// evaluation) run the straight-line body on instance (0, 0) and store
+// nothing, so that every warp of the group passes every barrier.
+template <class M>
+__device__ __noinline__ void eval_coop_item(const BatchArgs& a, const BGroup& g, int d, int r, bool act, int w,
+                                            vgb_xs_t xs, int bar) {
+    double V[M::NN];
+#pragma unroll
+    for (int t = 0; t < M::NN; ++t)
+        V[t] = __ldcg(a.Xc + (size_t)__ldg(g.node_map + (size_t)t * g.n_dev + d) * a.n_rep + r);
+    const double T = g.temps ? __ldg(g.temps + (size_t)d * a.n_rep + r) : g.temp_shared;
+    BParam P{g, d, r, a.n_rep};
+    const CoopOut out{a.contrib + (size_t)g.cbase * a.n_rep, (size_t)g.n_dev * a.n_rep, (size_t)d * a.n_rep + r};
+    M::coop(w, P, T, V, xs, act, out, bar);
+}
+
 // Item warps (32 consecutive items: one device of 32 consecutive replicas)
 // are dealt round-robin over the CTAs, so every SM holds as few evaluation
-// warps as the batch allows.
+// warps as the batch allows.  Item warps of a model with a cooperative body
+// go to groups of COOP_WARPS warps (two per CTA, one warp per sub-partition
+// each), dealt round-robin over the CTAs first; the rest to single warps.
 __device__ void eval_phase(const BatchArgs& a) {
     const int lane = threadIdx.x & 31;
+    if (a.n_coop_units) {
+        extern __shared__ double batch_smem[];
+        const int warp = threadIdx.x >> 5;
+        const int grp = warp / COOP_WARPS, w = warp % COOP_WARPS;
+        const int ngrp = (blockDim.x >> 5) / COOP_WARPS;
+        const vgb_xs_t xs = vgb_xs_base(batch_smem + (size_t)grp * a.coop_stride + lane);
+        for (long long u = blockIdx.x + (long long)gridDim.x * grp; u < a.n_coop_units;
+             u += (long long)gridDim.x * ngrp) {
+            int gi = 0;
+            while (gi + 1 < a.n_groups && !(u >= a.groups[gi].cu0 && u < a.groups[gi].cu1)) ++gi;
+            const BGroup g = a.groups[gi];
+            const long long loc = (u - g.cu0) * 32 + lane;
+            int d = (int)(loc / a.n_rep);
+            int r = (int)(loc - (long long)d * a.n_rep);
+            bool act = d < g.n_dev;
+            if (act) act = *(volatile int*)&a.rep[r].need_eval != 0;
+            if (!act) d = r = 0;
+            // the same decision in every warp of the group (each lane's flag is)
+            if (!__any_sync(0xffffffffu, act)) continue;
+            switch (g.model) {
+#define VGB_COOP_CASE(ID, STRUCT) \
+    case ID: eval_coop_item<STRUCT>(a, g, d, r, act, w, xs, 1 + grp); break;
+                VGB_COOP_LIST(VGB_COOP_CASE)
+#undef VGB_COOP_CASE
+                default: break;
+            }
+        }
+    }
     const long long n_iw = (a.n_items + 31) / 32;
     const long long step = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long iw = (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; iw < n_iw; iw += step) {
@@ -200,6 +259,7 @@ __device__ void eval_phase(const BatchArgs& a) {
         int gi = 0;
         while (gi + 1 < a.n_groups && it >= a.groups[gi + 1].item0) ++gi;
         const BGroup g = a.groups[gi];
+        if (g.cu1 > g.cu0) continue;  // evaluated cooperatively
         const long long loc = it - g.item0;
         const int d = (int)(loc / a.n_rep);
         const int r = (int)(loc - (long long)d * a.n_rep);
@@ -690,6 +750,16 @@ __global__ void __launch_bounds__(BATCH_THREADS, 1) batch_kernel(BatchArgs a) {
 // host side
 // ---------------------------------------------------------------------------
 
+static bool model_has_coop(int model) {
+    switch (model) {
+#define VGB_COOP_ID(ID, STRUCT) \
+    case ID: return true;
+        VGB_COOP_LIST(VGB_COOP_ID)
+#undef VGB_COOP_ID
+        default: return false;
+    }
+}
+
 struct Batch {
     Circuit* c = nullptr;
     int n_rep = 0;
@@ -708,7 +778,8 @@ struct Batch {
     DevBuf<unsigned char> d_csr_diag, d_conv_mask;
     std::vector<DevBuf<int>> d_node_map, d_vidx;
     std::vector<DevBuf<double>> d_shared, d_varying, d_temps;
-    long long n_contrib = 0, n_items = 0;
+    long long n_contrib = 0, n_items = 0, n_coop_units = 0;
+    bool coop = true;  // cooperative evaluation of the models that have one
     double run_ms = 0.0;
     long long ticks = 0;
     long long phase_cycles[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -753,6 +824,7 @@ static void batch_build(Batch& b) {
         B.cbase = bbase[g];
         B.item0 = items;
         items += ((long long)G.n_dev * R + 31) / 32 * 32;
+        B.cu0 = B.cu1 = 0;
     }
     b.n_contrib = nb;
     b.n_items = items;
@@ -888,6 +960,26 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
         B.varying = b.d_varying[g].p;
         B.temps = b.temps[g].empty() ? nullptr : b.d_temps[g].p;
     }
+    // cooperative units: the item warps of the models that have a cooperative
+    // body, when their exchange slots fit in shared memory beside nothing else
+    int dev = 0;
+    VGB_CUDA(cudaGetDevice(&dev));
+    int sms = 0, per_sm = 0, smem_optin = 0;
+    VGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    VGB_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t ws_bytes = sizeof(double) * ws_doubles(n, nu) * (BATCH_THREADS / 32);
+    const long long coop_stride = 32LL * VGB_COOP_SLOTS_MAX;
+    const size_t coop_bytes = sizeof(double) * coop_stride * (BATCH_THREADS / 32 / COOP_WARPS);
+    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin;
+    b.n_coop_units = 0;
+    for (size_t g = 0; g < c.groups.size(); ++g) {
+        BGroup& B = b.groups[g];
+        B.cu0 = B.cu1 = b.n_coop_units;
+        if (coop && model_has_coop(B.model)) {
+            B.cu1 = B.cu0 + ((long long)B.n_dev * R + 31) / 32;
+            b.n_coop_units = B.cu1;
+        }
+    }
     b.d_groups.upload(b.groups);
     b.d_vs_data.upload(b.vs_data);
     b.d_is_data.upload(b.is_data);
@@ -992,11 +1084,11 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     a.max_ticks = (long long)(16LL * max_steps + 1000) * (itl + 2);
     a.ticks_out = ticks.p;
     a.phase_cycles = pcyc.p;
-    int dev = 0;
-    VGB_CUDA(cudaGetDevice(&dev));
-    int sms = 0, per_sm = 0;
-    VGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t smem = sizeof(double) * ws_doubles(n, nu) * (BATCH_THREADS / 32);
+    a.n_coop_units = b.n_coop_units;
+    a.coop_stride = coop_stride;
+    // the exchange slots of the evaluation phase and the per-warp workspaces of
+    // the replica phase share the dynamic shared memory (grid barriers between)
+    const size_t smem = std::max(ws_bytes, b.n_coop_units ? coop_bytes : (size_t)0);
     VGB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BATCH_THREADS, smem));
     batch_require(per_sm >= 1, "batched transient: the kernel does not fit on an SM");
@@ -1149,6 +1241,13 @@ int vgb_batch_transient(void* bh, const double* cfg, const double* X0, const dou
     });
 }
 
+int vgb_batch_set_coop(void* bh, int enable) {
+    Batch* b = static_cast<Batch*>(bh);
+    if (!b) return VGB_ERR_INVALID;
+    b->coop = enable != 0;
+    return VGB_OK;
+}
+
 int vgb_batch_info(void* bh, double* out) {
     Batch* b = static_cast<Batch*>(bh);
     if (!b || !out) return VGB_ERR_INVALID;
@@ -1157,6 +1256,7 @@ int vgb_batch_info(void* bh, double* out) {
     out[2] = (double)b->n_items;
     out[3] = (double)b->n_contrib;
     for (int q = 0; q < 8; ++q) out[4 + q] = (double)b->phase_cycles[q];
+    out[12] = (double)b->n_coop_units;
     return VGB_OK;
 }
 

@@ -34,6 +34,42 @@ struct GroupArgs {
     int inst_per_replica;                 // instances per replica (batched mode), else n_dev
 };
 
+// Named barrier of the warps that share one cooperative model evaluation
+// (generated coop_w* members): `threads` = 32 x warps of the group, ids from 1
+// (0 is __syncthreads).  Every warp of the group executes the same barriers
+// in the same order: the cooperative body is straight-line code.  The
+// non-aligned form counts threads one by one, so a warp still diverged after
+// a library fallback inside a math function arrives correctly.
+__device__ __forceinline__ void vgb_coop_bar(int id, int threads) {
+    asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// The group's exchange slots: a shared-memory address (this lane's column of
+// 32-double slots) and volatile accesses at constant offsets (doubles), so
+// that the compiler neither forwards a warp's own store to a later load of
+// the same slot (another warp may have rewritten it after a barrier) nor
+// moves an access across a barrier.
+typedef unsigned vgb_xs_t;
+__device__ __forceinline__ vgb_xs_t vgb_xs_base(const double* p) {
+    return (vgb_xs_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ double vgb_xs_ld(vgb_xs_t xs, int off) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(xs + 8u * (unsigned)off) : "memory");
+    return v;
+}
+__device__ __forceinline__ void vgb_xs_st(vgb_xs_t xs, int off, double v) {
+    asm volatile("st.shared.f64 [%0], %1;" ::"r"(xs + 8u * (unsigned)off), "d"(v) : "memory");
+}
+__device__ __forceinline__ bool vgb_xs_ldb(vgb_xs_t xs, int off) {
+    unsigned v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(xs + 8u * (unsigned)off) : "memory");
+    return v != 0u;
+}
+__device__ __forceinline__ void vgb_xs_stb(vgb_xs_t xs, int off, bool b) {
+    asm volatile("st.shared.u32 [%0], %1;" ::"r"(xs + 8u * (unsigned)off), "r"(b ? 1u : 0u) : "memory");
+}
+
 template <class M>
 struct ParamReader {
     const GroupArgs& g;
