@@ -293,21 +293,26 @@ int vgb_tran_destroy(void* session);
  *                I_out [n_rep][max_steps][max(n_vsrc,1)], stats [n_rep][8] =
  *                {n_steps, rejected, total_nr_iters, min_dt_used, max_dt_used,
  *                device_ms, nr_failures, pivot_failures}.
- *   set_coop:    enable (default) or disable the cooperative evaluation:
+ *   set_coop:    allow (default) or forbid the cooperative evaluation:
  *                the models that carry a generated several-warp body (EKV)
- *                are evaluated by groups of four warps, one per SM
- *                sub-partition, that split each instance's dataflow graph
- *                and exchange values through shared memory.  Disabled, one
- *                warp evaluates 32 items.  Results agree to the last bits
- *                (a multiply-add split between warps is not fused).
- *   info:        out[13] = {device ms of the last run, ticks, evaluation items,
+ *                are evaluated by groups of four warps that split each
+ *                instance's dataflow graph and exchange values through
+ *                shared memory, with the body's parameter-only part computed
+ *                once per run into a per-instance cache.  Used when the
+ *                batch has no more such item warps than the GPU has SMs
+ *                (beyond that, one warp per 32 items keeps the SMs' FP64
+ *                issue fuller).  Results agree with the one-warp evaluation
+ *                to the last bits (multiply-adds are fused differently).
+ *   info:        out[17] = {device ms of the last run, ticks, evaluation items,
  *                contribution slots per replica, then SM clock cycles summed
  *                over the ticks of: evaluation, wait at the first grid
  *                barrier, per-replica step, wait at the second barrier (as
  *                the first CTA sees them), and, for replica 0: assembly of
  *                the Newton system, LU and solve, Newton update and test,
  *                step finish and plan; then the number of item warps
- *                evaluated cooperatively}.
+ *                evaluated cooperatively; then, for replica 0, the cycles of
+ *                the assembly's Jacobian and of its residual rows, of the
+ *                LU factorisation and of its substitutions}.
  * Errors are reported through vgb_batch_last_error(b) (create: on h). */
 int vgb_batch_create(void* h, int n_rep, void** out_batch);
 int vgb_batch_set_group(void* b, int group, int n_varying, const int* varying_idx, const double* values,

@@ -125,7 +125,7 @@ def test_batched_ring_corners_match_oracle(cuda):
     X0 = np.stack([uic_start(r, {"c0.n1": 1.2, "c0.vdd": 1.2}) for r in rcs])
     out = bt.transient(cfg, X0)
     bt.close()
-    assert out["coop_units"] == (14 * M.CORNER_COUNT + 31) // 32
+    assert out["coop_units"] == 0  # 448 item warps, more than the SMs: one warp each
     assert np.all(out["n_steps"] == M.CORNER_STEPS + 1)
     worst = 0.0
     for k in fx["sample"]:

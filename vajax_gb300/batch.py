@@ -136,14 +136,16 @@ class BatchedTransient:
         self._check(self.lib.vgb_batch_transient(self.h, _dp(c), _dp(X0),
                                                  *[None if a is None else _dp(a) for a in opt],
                                                  _dp(times), _dp(V), _dp(I), _dp(stats)))
-        info = np.zeros(13)
+        info = np.zeros(17)
         self._check(self.lib.vgb_batch_info(self.h, _dp(info)))
         return {"times": times, "V": V, "I": I, "n_steps": stats[:, 0].astype(np.int64),
                 "rejected": stats[:, 1].astype(np.int64), "total_nr_iters": stats[:, 2].astype(np.int64),
                 "nr_failures": stats[:, 6].astype(np.int64), "pivot_failures": stats[:, 7].astype(np.int64),
                 "device_ms": float(info[0]), "ticks": int(info[1]), "coop_units": int(info[12]),
                 "phase_cycles": dict(zip(("eval", "barrier1", "replica", "barrier2", "r0_assemble", "r0_lu",
-                                          "r0_update", "r0_finish_plan"), info[4:12].tolist()))}
+                                          "r0_update", "r0_finish_plan", "r0_assemble_jacobian",
+                                          "r0_assemble_rows", "r0_lu_factor", "r0_lu_substitute"),
+                                         info[4:12].tolist() + info[13:17].tolist()))}
 
     def close(self):
         if getattr(self, "h", None):

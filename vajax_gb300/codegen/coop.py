@@ -43,7 +43,12 @@ The generated struct members (inside the model's struct):
   store or moved across a barrier), ``act`` whether the
   lane has an instance, ``out(i, v)`` stores output ``i`` of the
   [jr | jq | rr | rq] layout, ``bar`` the named barrier of the group;
-* ``coop(w, ...)``: dispatch on the warp index.
+* ``coop(w, ...)``: dispatch on the warp index;
+* ``NCACHE`` and ``cache(P, T, cw)``: the hoisted parameter-only part, run
+  once per instance, storing cw(k, value) for the values the rest reads;
+* ``eval_cached(P, C, T, V, rr, rq, jr, jq)``: the branched single-thread
+  body reading the same cache (for batches large enough to keep every SM's
+  FP64 issue busy with one warp per 32 items).
 """
 
 from __future__ import annotations
@@ -103,6 +108,8 @@ class CoopPlan:
         self._nodes()
         self._check_dominance()
         self._liveness()
+        self._fuse_fma()
+        self._hoist()
         self._schedule()
         self._exchange()
 
@@ -146,27 +153,24 @@ class CoopPlan:
         self.seq: List[_Node] = []
         self.cond: Dict[str, str] = {}
         self.kind: Dict[str, str] = {}  # val -> "inst" | "phi" | "act" | "edge"
-        self.expr: Dict[str, str] = {}
+        self.act_in: Dict[str, List[str]] = {}  # act node -> incoming edge flags (entry: none)
+        self.edge_of: Dict[str, tuple] = {}  # edge node -> (source block, index of the successor)
         self.types = dict(prog.types)
         k = 0
 
-        def add(val, inst, phi, deps, cost, block, kind, expr=None):
+        def add(val, inst, phi, deps, cost, block, kind):
             nonlocal k
             n = _Node(val, inst, phi, deps, cost, block, k)
             k += 1
             self.nodes[val] = n
             self.seq.append(n)
             self.kind[val] = kind
-            if expr is not None:
-                self.expr[val] = expr
             return n
 
         for b in self.order:
-            if b == self.entry:
-                add(f"a_{b}", None, False, [], MIN_COST, b, "act", "act")
-            else:
-                es = [f"e_{p}_{b}" for p in self.pred[b]]
-                add(f"a_{b}", None, False, es, MIN_COST, b, "act", " || ".join(es))
+            es = [f"e_{p}_{b}" for p in self.pred[b]]
+            self.act_in[f"a_{b}"] = es
+            add(f"a_{b}", None, False, es, MIN_COST, b, "act")
             self.types[f"a_{b}"] = "bool"
             for inst in prog.insts_by_block[b]:
                 op = inst["opcode"].lower()
@@ -184,13 +188,10 @@ class CoopPlan:
             c = self.cond.get(b)
             for j, s in enumerate(self.succ[b]):
                 deps = [f"a_{b}"]
-                if c is None:
-                    e = f"a_{b}"
-                else:
-                    if prog.is_value(c):
-                        deps.append(c)
-                    e = f"a_{b} && ({prog.opnd(c)})" if j == 0 else f"a_{b} && !({prog.opnd(c)})"
-                add(f"e_{b}_{s}", None, False, deps, MIN_COST, b, "edge", e)
+                if c is not None and prog.is_value(c):
+                    deps.append(c)
+                self.edge_of[f"e_{b}_{s}"] = (b, j)
+                add(f"e_{b}_{s}", None, False, deps, MIN_COST, b, "edge")
                 self.types[f"e_{b}_{s}"] = "bool"
 
     def _check_dominance(self):
@@ -225,6 +226,7 @@ class CoopPlan:
                 continue
             live.add(v)
             stack += self.nodes[v].deps
+        self.live = live
         self.seq = [n for n in self.seq if n.val in live]
         self.users: Dict[str, List[_Node]] = {}
         for n in self.seq:
@@ -232,6 +234,101 @@ class CoopPlan:
                 self.users.setdefault(d, []).append(n)
         for n in reversed(self.seq):
             n.blevel = n.cost + max((u.blevel for u in self.users.get(n.val, [])), default=0.0)
+
+    def _fuse_fma(self):
+        """A product used once, by an add or subtract, becomes one fused
+        multiply-add node (what the compiler does to the single-thread body):
+        one FP64 instruction instead of two, and the pair can no longer be
+        split between warps."""
+        prog = self.prog
+        self.fma: Dict[str, tuple] = {}  # add node -> (m0, m1, other, product first, subtract)
+        self.fma_prod: Dict[str, str] = {}  # add node -> the product value folded into it
+        dead = set()
+        outputs = {v for _, _, v in prog.outputs}
+        for n in self.seq:
+            if self.kind[n.val] != "inst" or n.inst["opcode"].lower() not in ("fadd", "fsub"):
+                continue
+            a, b = n.inst["operands"]
+            for k, x in enumerate((a, b)):
+                if not prog.is_value(x) or x in dead or x in outputs:
+                    continue
+                m = self.nodes.get(x)
+                if m is None or self.kind[m.val] != "inst" or m.inst["opcode"].lower() != "fmul":
+                    continue
+                if len(self.users.get(x, [])) != 1:
+                    continue
+                other = b if k == 0 else a
+                m0, m1 = m.inst["operands"]
+                self.fma[n.val] = (m0, m1, other, k == 0, n.inst["opcode"].lower() == "fsub")
+                self.fma_prod[n.val] = x
+                dead.add(x)
+                n.deps = [d for d in n.deps if d != x] + list(m.deps)
+                n.cost = 1.0
+                break
+        if not dead:
+            return
+        self.seq = [n for n in self.seq if n.val not in dead]
+        for v in dead:
+            del self.nodes[v]
+        self.users = {}
+        for n in self.seq:
+            for d in n.deps:
+                self.users.setdefault(d, []).append(n)
+        for n in reversed(self.seq):
+            n.blevel = n.cost + max((u.blevel for u in self.users.get(n.val, [])), default=0.0)
+
+    def _leaves(self, n: _Node) -> List[str]:
+        """The operands of a node that are not values (constants, parameters,
+        voltages, the temperature)."""
+        prog = self.prog
+        kind = self.kind[n.val]
+        if kind == "inst" and n.val in self.fma:
+            ops = list(self.fma[n.val][:3])
+        elif kind == "inst":
+            ops = list(n.inst.get("operands", []))
+        elif kind == "phi":
+            ops = [po["value"] for po in n.inst["phi_operands"]]
+        elif kind == "edge":
+            c = self.cond.get(self.edge_of[n.val][0])
+            ops = [c] if c is not None else []
+        else:
+            ops = []
+        return [o for o in ops if not prog.is_value(o)]
+
+    def _hoist(self):
+        """Nodes that depend on parameters, the temperature and constants
+        only (not on a voltage) move to the cache program, run once per
+        instance; the values the rest reads from them become cached leaves
+        ``C(k)``.  The entry flag counts as such a node (true: outputs of
+        lanes without an instance are never stored)."""
+        prog = self.prog
+        volt = {v for v, k in prog.pkind.items() if k == "voltage"}
+        po = set()
+        for n in self.seq:
+            if self.kind[n.val] == "act" and n.block == self.entry:
+                po.add(n.val)
+                continue
+            if any(d not in po for d in n.deps) or any(o in volt for o in self._leaves(n)):
+                continue
+            po.add(n.val)
+        outputs = {v for _, _, v in prog.outputs}
+        # branch conditions too: the branched body (eval_cached) still branches on them
+        conds = {c for c in self.cond.values() if prog.is_value(c)}
+        cached = [n.val for n in self.seq if n.val in po and
+                  (n.val in outputs or n.val in conds or
+                   any(u.val not in po for u in self.users.get(n.val, [])))]
+        self.cache_index = {v: k for k, v in enumerate(cached)}
+        self.setup_seq = [n for n in self.seq if n.val in po]
+        self.seq = [n for n in self.seq if n.val not in po]
+        for n in self.seq:
+            n.deps = [d for d in n.deps if d not in po]
+        self.users = {}
+        for n in self.seq:
+            for d in n.deps:
+                self.users.setdefault(d, []).append(n)
+        for n in reversed(self.seq):
+            n.blevel = n.cost + max((u.blevel for u in self.users.get(n.val, [])), default=0.0)
+        self.hoisted_cost = sum(n.cost for n in self.setup_seq)
 
     # ---- scheduling -------------------------------------------------------------
     def _schedule(self):
@@ -321,35 +418,112 @@ class CoopPlan:
     # ---- emission ------------------------------------------------------------------
     def info(self) -> dict:
         return {"warps": self.W, "work": sum(self.work), "per_warp": list(self.work), "makespan": self.makespan,
-                "barriers": self.n_barriers, "slots": self.n_slots, "cross_values": len(self.slot)}
+                "barriers": self.n_barriers, "slots": self.n_slots, "cross_values": len(self.slot),
+                "cached": len(self.cache_index), "hoisted_work": self.hoisted_cost}
 
     def emit(self) -> str:
         parts = [f"    static constexpr int COOP_W = {self.W};",
                  f"    static constexpr int COOP_SLOTS = {self.n_slots};",
-                 f"    static constexpr int COOP_BARRIERS = {self.n_barriers};"]
+                 f"    static constexpr int COOP_BARRIERS = {self.n_barriers};",
+                 f"    static constexpr int NCACHE = {max(len(self.cache_index), 1)};",
+                 self._emit_cache(), self._emit_eval_cached()]
         for w in range(self.W):
             parts.append(self._emit_warp(w))
-        cases = " ".join(f"case {w}: coop_w{w}(P, T, V, xs, act, out, bar); break;" for w in range(self.W))
-        parts.append(f"""    template <class PF, class OF>
-    __device__ __forceinline__ static void coop(int w, const PF& P, double T, const double* __restrict__ V,
-                                                vgb_xs_t xs, bool act, const OF& out, int bar)
+        cases = " ".join(f"case {w}: coop_w{w}(P, C, T, V, xs, act, out, bar); break;" for w in range(self.W))
+        parts.append(f"""    template <class PF, class CF, class OF>
+    __device__ __forceinline__ static void coop(int w, const PF& P, const CF& C, double T,
+                                                const double* __restrict__ V, vgb_xs_t xs, bool act,
+                                                const OF& out, int bar)
     {{
         switch (w) {{ {cases} default: break; }}
     }}
 """)
         return "\n".join(parts)
 
-    def _line(self, n: _Node) -> str:
+    def ref(self, v: str, cached: bool = True) -> str:
+        """C expression of an operand: a cached leaf, a value, a parameter,
+        a voltage, the temperature or a constant."""
+        if cached and v in self.cache_index:
+            k = self.cache_index[v]
+            return f"C.b({k})" if self.types.get(v) == "bool" else f"C({k})"
+        return self.prog.opnd(v)
+
+    def _line(self, n: _Node, cached: bool = True) -> str:
         prog = self.prog
         kind = self.kind[n.val]
+        ref = lambda v: self.ref(v, cached)
+        if kind == "inst" and n.val in self.fma:
+            m0, m1, other, prod_first, sub = self.fma[n.val]
+            a, b, c = ref(m0), ref(m1), ref(other)
+            if not sub:
+                return f"{n.val} = fma({a}, {b}, {c});"
+            if prod_first:
+                return f"{n.val} = fma({a}, {b}, -({c}));"
+            return f"{n.val} = fma(-({a}), {b}, {c});"
         if kind == "inst":
-            return f"{n.val} = {prog.expr(n.inst)};"
+            return f"{n.val} = {prog.expr(n.inst, ref)};"
         if kind == "phi":
             sel = "false" if self.types[n.val] == "bool" else "0.0"
             for po in reversed(n.inst["phi_operands"]):
-                sel = f"(e_{po['block']}_{n.block} ? {prog.opnd(po['value'])} : {sel})"
+                sel = f"({ref('e_' + po['block'] + '_' + n.block)} ? {ref(po['value'])} : {sel})"
             return f"{n.val} = {sel};"
-        return f"{n.val} = {self.expr[n.val]};"
+        if kind == "act":
+            es = self.act_in[n.val]
+            return f"{n.val} = {' || '.join(ref(e) for e in es) if es else 'true'};"
+        b, j = self.edge_of[n.val]
+        c = self.cond.get(b)
+        a = ref(f"a_{b}")
+        if c is None:
+            return f"{n.val} = {a};"
+        return f"{n.val} = {a} && ({ref(c)});" if j == 0 else f"{n.val} = {a} && !({ref(c)});"
+
+    def _emit_eval_cached(self) -> str:
+        """eval_cached(P, C, T, V, rr, rq, jr, jq): the single-thread branched
+        body with the hoisted part read from the cache (what one warp runs
+        for 32 items when the batch is too large for cooperative groups)."""
+        from vajax_gb300.codegen.cuda import branched_body
+        prog = self.prog
+        hoisted = {n.val for n in self.setup_seq if prog.is_value(n.val)}
+        hoisted |= {self.fma_prod[v] for v in hoisted if v in self.fma_prod}  # products folded into them
+        cached = {v: self.ref(v) for v in self.cache_index if prog.is_value(v)}
+        dead = {v for v in prog.types if v not in self.live}  # outside the outputs' cone
+        lines = branched_body(prog, cached, (hoisted - set(cached)) | dead)
+        outs = [f"        {cname} = {self.ref(v) if v in self.cache_index else prog.opnd(v)};"
+                for _, cname, v in prog.outputs]
+        body = "\n".join(lines + outs)
+        return f"""    template <class PF, class CF>
+    __device__ __forceinline__ static void eval_cached(const PF& P, const CF& C, double T,
+                                                       const double* __restrict__ V, double* rr, double* rq,
+                                                       double* jr, double* jq)
+    {{
+{body}
+    }}
+"""
+
+    def _emit_cache(self) -> str:
+        """cache(P, T, cw): the hoisted nodes, straight-line, and cw(k, v)
+        for every cached value (booleans as 1.0 / 0.0)."""
+        ind = "        "
+        key = lambda v: (v[0], int(v[1:]) if v[1:].isdigit() else 0, v)
+        vals = [n.val for n in self.setup_seq]
+        dbl = sorted((v for v in vals if self.types[v] == "double"), key=key)
+        bol = sorted((v for v in vals if self.types[v] == "bool"), key=key)
+        lines: List[str] = []
+        for i in range(0, len(dbl), 16):
+            lines.append(ind + "double " + ", ".join(dbl[i:i + 16]) + ";")
+        for i in range(0, len(bol), 16):
+            lines.append(ind + "bool " + ", ".join(bol[i:i + 16]) + ";")
+        for n in self.setup_seq:
+            lines.append(ind + self._line(n, cached=False))
+        for v, k in self.cache_index.items():
+            lines.append(ind + (f"cw({k}, {v} ? 1.0 : 0.0);" if self.types[v] == "bool" else f"cw({k}, {v});"))
+        body = "\n".join(lines)
+        return f"""    template <class PF, class CW>
+    __device__ static void cache(const PF& P, double T, const CW& cw)
+    {{
+{body}
+    }}
+"""
 
     def _emit_warp(self, w: int) -> str:
         types = self.types
@@ -388,24 +562,28 @@ class CoopPlan:
             if g + 1 < self.n_segments:
                 lines.append(ind + f"vgb_coop_bar(bar, {32 * self.W});")
         prog = self.prog
-        outs = [(i, v) for i, _, v in prog.outputs
-                if (prog.is_value(v) and self.nodes[v].owner == w) or (not prog.is_value(v) and w == 0)]
+        def owner(v):
+            if v in self.cache_index or not prog.is_value(v):
+                return 0
+            return self.nodes[v].owner
+        outs = [(i, v) for i, _, v in prog.outputs if owner(v) == w]
         if outs:
             lines.append(ind + "if (act) {")
             for i, v in outs:
-                lines.append(ind + f"    out({i}, {prog.opnd(v)});")
+                lines.append(ind + f"    out({i}, {self.ref(v)});")
             lines.append(ind + "}")
         body = "\n".join(lines)
-        return f"""    template <class PF, class OF>
-    __device__ __noinline__ static void coop_w{w}(const PF& P, double T, const double* __restrict__ V,
-                                                  vgb_xs_t xs, bool act, const OF& out, int bar)
+        return f"""    template <class PF, class CF, class OF>
+    __device__ __noinline__ static void coop_w{w}(const PF& P, const CF& C, double T,
+                                                  const double* __restrict__ V, vgb_xs_t xs, bool act,
+                                                  const OF& out, int bar)
     {{
 {body}
     }}
 """
 
 
-def coop_plan(model: dict, W: int = W_DEFAULT, min_work: float = 400.0):
+def coop_plan(model: dict, W: int = W_DEFAULT, min_work: float = 200.0):
     """The cooperative plan of a model, or None when the body is too small to
     gain from more than one warp (or has a shape the emitter does not take)."""
     try:

@@ -211,19 +211,46 @@ def emit_model(model: dict, fn_name: str | None = None, extra: str = "") -> str:
     prog = MirProgram(model)
     spec = prog.spec
     name = fn_name or f"Model_{_cname(spec.name)}"
-    types, opnd = prog.types, prog.opnd
+    lines = branched_body(prog)
+    outs = [f"        {cname} = {prog.opnd(v)};" for _, cname, v in prog.outputs]
 
+    src = f"""
+// Generated from the MIR of Verilog-A module '{spec.name}'.
+struct {name} {{
+{prog.struct_header(name)}
+    template <class PF>
+    __device__ __forceinline__ static void eval(const PF& P, double T, const double* __restrict__ V,
+                                                double* rr, double* rq, double* jr, double* jq)
+    {{
+{chr(10).join(lines)}
+{chr(10).join(outs)}
+    }}
+{extra}}};
+"""
+    return src
+
+
+def branched_body(prog: MirProgram, cached: Dict[str, str] | None = None, dropped=frozenset()) -> List[str]:
+    """The model body with its control flow as labelled blocks and gotos.
+
+    ``cached`` maps values to the expression that replaces their computation
+    (a read of a per-instance cache, emitted where the value is defined: in
+    place of the instruction, or at the head of the block of a phi);
+    ``dropped`` values are not computed at all (nothing that remains reads
+    them)."""
+    cached = cached or {}
+    types, opnd = prog.types, prog.opnd
     lines: List[str] = []
     ind = "        "
-    dbl = [r for r in types if types[r] == "double"]
-    bol = [r for r in types if types[r] == "bool"]
+    dbl = [r for r in types if types[r] == "double" and r not in dropped]
+    bol = [r for r in types if types[r] == "bool" and r not in dropped]
     for i in range(0, len(dbl), 16):
         lines.append(ind + "double " + ", ".join(f"{v} = 0.0" for v in dbl[i:i + 16]) + ";")
     for i in range(0, len(bol), 16):
         lines.append(ind + "bool " + ", ".join(f"{v} = false" for v in bol[i:i + 16]) + ";")
 
     def moves(pred, succ) -> List[str]:
-        mv = prog.phi_moves.get((pred, succ), [])
+        mv = [(d, v) for d, v in prog.phi_moves.get((pred, succ), []) if d not in cached and d not in dropped]
         if not mv:
             return []
         # parallel copy semantics: read all sources first
@@ -238,6 +265,9 @@ def emit_model(model: dict, fn_name: str | None = None, extra: str = "") -> str:
 
     for b in prog.order:
         lines.append(f"    {b}:;")
+        for inst in prog.insts_by_block[b]:
+            if inst["opcode"].lower() == "phi" and inst["result"] in cached:
+                lines.append(ind + f"{inst['result']} = {cached[inst['result']]};")
         for inst in prog.insts_by_block[b]:
             op = inst["opcode"].lower()
             if op == "phi":
@@ -256,24 +286,12 @@ def emit_model(model: dict, fn_name: str | None = None, extra: str = "") -> str:
             if op == "exit":
                 lines.append(ind + "goto done;")
                 continue
-            lines.append(ind + f"{inst['result']} = {prog.expr(inst)};")
+            r = inst["result"]
+            if r in dropped:
+                continue
+            lines.append(ind + f"{r} = {cached[r] if r in cached else prog.expr(inst)};")
     lines.append("    done:;")
-    outs = [f"        {cname} = {opnd(v)};" for _, cname, v in prog.outputs]
-
-    src = f"""
-// Generated from the MIR of Verilog-A module '{spec.name}'.
-struct {name} {{
-{prog.struct_header(name)}
-    template <class PF>
-    __device__ __forceinline__ static void eval(const PF& P, double T, const double* __restrict__ V,
-                                                double* rr, double* rq, double* jr, double* jq)
-    {{
-{chr(10).join(lines)}
-{chr(10).join(outs)}
-    }}
-{extra}}};
-"""
-    return src
+    return lines
 
 
 def _expr(op: str, a: List[str]) -> str:

@@ -32,6 +32,7 @@
 // barriers by a poll limit that sets an error flag and stops the kernel.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "vgb_core.h"
@@ -64,6 +65,7 @@ struct BGroup {
     long long cbase;         // first contribution slot of the group
     long long item0;         // first evaluation item of the group
     long long cu0, cu1;      // its cooperative units [cu0, cu1) (empty: one warp per item warp)
+    double* cache;           // cooperative groups: [NCACHE][n_dev][n_rep] parameter-only values
 };
 
 // Per-replica controller state (field names as ctl_plan / ctl_finish expect).
@@ -118,7 +120,9 @@ struct BatchArgs {
     // SM clock cycles summed over ticks: [0..3] each phase of a tick as CTA 0's
     // thread 0 sees it (evaluation, wait at the first barrier, per-replica
     // step, wait at the second barrier); [4..7] replica 0's assembly, LU and
-    // solve, Newton update and test, step finish and plan
+    // solve, Newton update and test, step finish and plan; [8..11] inside
+    // those: the assembly's Jacobian and its residual rows, the LU's
+    // factorisation and its substitutions
     long long* phase_cycles;
 };
 
@@ -165,6 +169,30 @@ struct BParam {
     }
 };
 
+// The per-instance cache of a cooperative model: the values of its body that
+// depend on parameters and temperature only, computed once per run
+// (batch_cache_kernel) and read by every evaluation.
+struct CacheW {
+    double* c;
+    size_t sd, o;
+    __device__ __forceinline__ void operator()(int k, double v) const { c[(size_t)k * sd + o] = v; }
+};
+struct CacheR {
+    const double* c;
+    size_t sd, o;
+    __device__ __forceinline__ double operator()(int k) const { return __ldg(c + (size_t)k * sd + o); }
+    __device__ __forceinline__ bool b(int k) const {
+        return __double_as_longlong(__ldg(c + (size_t)k * sd + o)) != 0;
+    }
+};
+
+// Models with a generated cache program (the cooperative ones) read their
+// parameter-only values from the per-instance cache in the one-warp path too.
+template <class M, class = void>
+struct HasCache : std::false_type {};
+template <class M>
+struct HasCache<M, std::void_t<decltype(M::NCACHE)>> : std::true_type {};
+
 template <class M>
 __device__ __noinline__ void eval_item(const BatchArgs& a, const BGroup& g, int d, int r) {
     double V[M::NN];
@@ -174,7 +202,12 @@ __device__ __noinline__ void eval_item(const BatchArgs& a, const BGroup& g, int 
     const double T = g.temps ? __ldg(g.temps + (size_t)d * a.n_rep + r) : g.temp_shared;
     double rr[M::NN], rq[M::NN], jr[M::NJ > 0 ? M::NJ : 1], jq[M::NJ > 0 ? M::NJ : 1];
     BParam P{g, d, r, a.n_rep};
-    M::eval(P, T, V, rr, rq, jr, jq);
+    if constexpr (HasCache<M>::value) {
+        const CacheR C{g.cache, (size_t)g.n_dev * a.n_rep, (size_t)d * a.n_rep + r};
+        M::eval_cached(P, C, T, V, rr, rq, jr, jq);
+    } else {
+        M::eval(P, T, V, rr, rq, jr, jq);
+    }
     // layout of a group: [2 NJ + 2 NN][n_dev]: jr, jq, rr, rq
     double* base = a.contrib + (size_t)g.cbase * a.n_rep;
     const size_t sd = (size_t)g.n_dev * a.n_rep;
@@ -199,6 +232,17 @@ struct CoopOut {
     __device__ __forceinline__ void operator()(int i, double v) const { __stcg(base + (size_t)i * sd + o, v); }
 };
 
+// One thread per instance (d, r) of a cooperative group: the cache program.
+template <class M>
+__global__ void __launch_bounds__(128) batch_cache_kernel(BGroup g, int n_rep) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)g.n_dev * n_rep) return;
+    const int d = (int)(i / n_rep), r = (int)(i - (long long)d * n_rep);
+    const double T = g.temps ? __ldg(g.temps + (size_t)d * n_rep + r) : g.temp_shared;
+    BParam P{g, d, r, n_rep};
+    M::cache(P, T, CacheW{g.cache, (size_t)g.n_dev * n_rep, (size_t)d * n_rep + r});
+}
+
 // One item warp evaluated by the COOP_WARPS warps of a group (this warp is
 // part w).  Lanes without an instance (padding, or a replica that needs no
 // evaluation) run the straight-line body on instance (0, 0) and store
@@ -212,8 +256,9 @@ __device__ __noinline__ void eval_coop_item(const BatchArgs& a, const BGroup& g,
         V[t] = __ldcg(a.Xc + (size_t)__ldg(g.node_map + (size_t)t * g.n_dev + d) * a.n_rep + r);
     const double T = g.temps ? __ldg(g.temps + (size_t)d * a.n_rep + r) : g.temp_shared;
     BParam P{g, d, r, a.n_rep};
+    const CacheR C{g.cache, (size_t)g.n_dev * a.n_rep, (size_t)d * a.n_rep + r};
     const CoopOut out{a.contrib + (size_t)g.cbase * a.n_rep, (size_t)g.n_dev * a.n_rep, (size_t)d * a.n_rep + r};
-    M::coop(w, P, T, V, xs, act, out, bar);
+    M::coop(w, P, C, T, V, xs, act, out, bar);
 }
 
 // Item warps (32 consecutive items: one device of 32 consecutive replicas)
@@ -328,6 +373,8 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
     const int n = a.n_aug;
     const double* Xr = a.Xc;  // [n_x][n_rep]
     const double c0 = k[0], c1 = k[1], d1 = k[2], c2 = k[3], gshunt = k[4];
+    const bool prof = r == 0 && lane == 0;
+    const long long t0 = prof ? clock64() : 0;
     if (jac) {
         for (int t = lane; t < n * n; t += 32) w.M[t] = 0.0;
         __syncwarp();
@@ -352,6 +399,7 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
         }
         __syncwarp();
     }
+    const long long t1 = prof ? clock64() : 0;
     bool ok = true, nf = false;
     for (int row = lane; row < n; row += 32) {
         double fn, tol;
@@ -406,22 +454,34 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
     }
     __syncwarp();
     *nonfinite = __any_sync(0xffffffffu, nf);
-    return __all_sync(0xffffffffu, ok);
+    const bool all_ok = __all_sync(0xffffffffu, ok);
+    if (prof && jac) {
+        a.phase_cycles[8] += t1 - t0;
+        a.phase_cycles[9] += clock64() - t1;
+    }
+    return all_ok;
 }
 
 // Dense LU with partial pivoting (largest |M(i,k)|, ties to the smaller row)
 // and the solve of M x = b in place of b, all in shared memory.  The
 // diagonal keeps the reciprocal of each pivot, so that the dependent chain of
-// the back substitution has no division.  Returns 1 + the first column whose
-// pivot was zero or not finite (replaced by 1e-30), or 0.
-__device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int lane) {
+// the back substitution has no division.  The rank-1 update of each step is
+// spread over the lanes element by element (an n = 9 system takes one or two
+// FP64 instructions per lane a step instead of one per trailing column), and
+// the pivot search and pivot checks are integer work on the bit patterns.
+// Returns 1 + the first column whose pivot was zero or not finite (replaced
+// by 1e-30), or 0.  `prof` (replica 0, lane 0) accumulates the cycles of the
+// factorisation and of the substitutions.
+__device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int lane, long long* prof) {
     int bad = 0;
+    const long long t0 = prof ? clock64() : 0;
     for (int k = 0; k < n; ++k) {
         unsigned long long best = 0;
         int bi = n;
         for (int i = k + lane; i < n; i += 32) {
-            const double v = fabs(M[i + (size_t)k * n]);
-            const unsigned long long key = v == v ? (unsigned long long)__double_as_longlong(v) : 0ull;
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(M[i + (size_t)k * n]) &
+                                            0x7fffffffffffffffull;  // |M(i,k)|
+            const unsigned long long key = bits > 0x7ff0000000000000ull ? 0ull : bits;  // NaN counts as 0
             if (bi == n || key > best) { best = key; bi = i; }
         }
         for (int o = 16; o; o >>= 1) {
@@ -444,7 +504,8 @@ __device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int la
         }
         __syncwarp();
         double piv = M[k + (size_t)k * n];
-        if (piv == 0.0 || !isfinite(piv)) {
+        const unsigned long long pb = (unsigned long long)__double_as_longlong(piv) & 0x7fffffffffffffffull;
+        if (pb == 0ull || pb >= 0x7ff0000000000000ull) {  // zero, infinite or NaN
             piv = 1e-30;
             if (!bad) bad = k + 1;
         }
@@ -453,12 +514,15 @@ __device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int la
         if (lane == 0) M[k + (size_t)k * n] = rinv;  // the diagonal keeps 1 / pivot
         for (int i = k + 1 + lane; i < n; i += 32) M[i + (size_t)k * n] *= rinv;
         __syncwarp();
-        for (int j = k + 1; j < n; ++j) {
-            const double u = M[k + (size_t)j * n];
-            for (int i = k + 1 + lane; i < n; i += 32) M[i + (size_t)j * n] -= M[i + (size_t)k * n] * u;
+        const int m = n - k - 1;
+        for (int t = lane; t < m * m; t += 32) {
+            const int jj = t / m, ii = t - jj * m;
+            const int i = k + 1 + ii, j = k + 1 + jj;
+            M[i + (size_t)j * n] -= M[i + (size_t)k * n] * M[k + (size_t)j * n];
         }
         __syncwarp();
     }
+    const long long t1 = prof ? clock64() : 0;
     for (int k = 0; k < n; ++k) {
         const double yk = b[k];
         for (int i = k + 1 + lane; i < n; i += 32) b[i] -= M[i + (size_t)k * n] * yk;
@@ -470,6 +534,10 @@ __device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int la
         const double xk = b[k];
         for (int i = lane; i < k; i += 32) b[i] -= M[i + (size_t)k * n] * xk;
         __syncwarp();
+    }
+    if (prof) {
+        prof[0] += t1 - t0;
+        prof[1] += clock64() - t1;
     }
     return bad;
 }
@@ -487,7 +555,7 @@ __device__ void replica_nr(const BatchArgs& a, const WarpWS& w, int r, BRep& s, 
     for (int i = lane; i < n; i += 32) b[i] = -b[i];
     __syncwarp();
     const long long c1 = clock64();
-    const int bad = replica_lu_solve(n, w.M, b, lane);
+    const int bad = replica_lu_solve(n, w.M, b, lane, r == 0 && lane == 0 ? a.phase_cycles + 10 : nullptr);
     const long long c2 = clock64();
     // delta test (before the update) and the damped update
     bool dok = true;
@@ -760,6 +828,28 @@ static bool model_has_coop(int model) {
     }
 }
 
+static int model_ncache(int model) {
+    switch (model) {
+#define VGB_COOP_NC(ID, STRUCT) \
+    case ID: return STRUCT::NCACHE;
+        VGB_COOP_LIST(VGB_COOP_NC)
+#undef VGB_COOP_NC
+        default: return 0;
+    }
+}
+
+static void launch_cache(const BGroup& g, int n_rep, cudaStream_t s) {
+    const long long n = (long long)g.n_dev * n_rep;
+    const int blocks = (int)((n + 127) / 128);
+    switch (g.model) {
+#define VGB_COOP_LAUNCH(ID, STRUCT) \
+    case ID: batch_cache_kernel<STRUCT><<<blocks, 128, 0, s>>>(g, n_rep); break;
+        VGB_COOP_LIST(VGB_COOP_LAUNCH)
+#undef VGB_COOP_LAUNCH
+        default: break;
+    }
+}
+
 struct Batch {
     Circuit* c = nullptr;
     int n_rep = 0;
@@ -777,12 +867,12 @@ struct Batch {
     DevBuf<double> d_csr_const, d_vs_data, d_is_data;
     DevBuf<unsigned char> d_csr_diag, d_conv_mask;
     std::vector<DevBuf<int>> d_node_map, d_vidx;
-    std::vector<DevBuf<double>> d_shared, d_varying, d_temps;
+    std::vector<DevBuf<double>> d_shared, d_varying, d_temps, d_cache;
     long long n_contrib = 0, n_items = 0, n_coop_units = 0;
     bool coop = true;  // cooperative evaluation of the models that have one
     double run_ms = 0.0;
     long long ticks = 0;
-    long long phase_cycles[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long phase_cycles[12] = {0};
 };
 
 static void batch_require(bool ok, const std::string& m) {
@@ -970,16 +1060,33 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     const size_t ws_bytes = sizeof(double) * ws_doubles(n, nu) * (BATCH_THREADS / 32);
     const long long coop_stride = 32LL * VGB_COOP_SLOTS_MAX;
     const size_t coop_bytes = sizeof(double) * coop_stride * (BATCH_THREADS / 32 / COOP_WARPS);
-    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin;
+    // FP64 issue on GB300 is an SM-wide budget (about one warp-instruction per
+    // 19 cycles) that one warp can use only a third of (one per 64 cycles):
+    // four warps sharing an instance finish it 1.7x sooner than one warp, but
+    // the if-converted body holds more instructions, so the cooperative
+    // evaluation pays only while no SM holds more than one group's work.
+    long long units = 0;
+    for (const BGroup& B : b.groups)
+        if (model_has_coop(B.model)) units += ((long long)B.n_dev * R + 31) / 32;
+    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin && units <= sms;
     b.n_coop_units = 0;
+    b.d_cache.resize(c.groups.size());
     for (size_t g = 0; g < c.groups.size(); ++g) {
         BGroup& B = b.groups[g];
         B.cu0 = B.cu1 = b.n_coop_units;
-        if (coop && model_has_coop(B.model)) {
-            B.cu1 = B.cu0 + ((long long)B.n_dev * R + 31) / 32;
-            b.n_coop_units = B.cu1;
+        B.cache = nullptr;
+        if (model_has_coop(B.model) && B.n_dev > 0) {
+            if (coop) {
+                B.cu1 = B.cu0 + ((long long)B.n_dev * R + 31) / 32;
+                b.n_coop_units = B.cu1;
+            }
+            // the cache serves the one-warp evaluation as well
+            b.d_cache[g].alloc((size_t)model_ncache(B.model) * B.n_dev * R);
+            B.cache = b.d_cache[g].p;
+            launch_cache(B, R, c.stream);  // ordered before the persistent kernel on the same stream
         }
     }
+    VGB_CUDA(cudaGetLastError());
     b.d_groups.upload(b.groups);
     b.d_vs_data.upload(b.vs_data);
     b.d_is_data.upload(b.is_data);
@@ -1055,7 +1162,7 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     ctl.zero(s);
     ticks.alloc(1);
     ticks.zero(s);
-    pcyc.alloc(8);
+    pcyc.alloc(12);
     pcyc.zero(s);
     VGB_CUDA(cudaStreamSynchronize(s));
 
@@ -1257,6 +1364,7 @@ int vgb_batch_info(void* bh, double* out) {
     out[3] = (double)b->n_contrib;
     for (int q = 0; q < 8; ++q) out[4 + q] = (double)b->phase_cycles[q];
     out[12] = (double)b->n_coop_units;
+    for (int q = 8; q < 12; ++q) out[5 + q] = (double)b->phase_cycles[q];
     return VGB_OK;
 }
 
