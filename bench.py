@@ -76,7 +76,7 @@ def make_engine_host(gates: int):
     return eng, stats, depth
 
 
-def make_engine(gates: int, max_steps: int, precision: str = "fp64", refine: int = 3):
+def make_engine(gates: int, max_steps: int, precision: str = "fp64", refine: int = 1):
     eng, stats, depth = make_engine_host(gates)
     eng.precision = precision
     eng.refine_sweeps = refine
@@ -876,11 +876,12 @@ def _time_session(sess, warmup, steps):
 
 def extra_mixed(args):
     """Config 3: the ~260k-transistor network (76,500 gates) with the FP32 LU
-    and FP64-residual refinement (3 sweeps), K adaptive steps after the DC
-    point; the same steps with the FP64 LU give the mixed run's error."""
+    and FP64-residual refinement (--refine sweeps, default one), K adaptive
+    steps after the DC point; the same steps with the FP64 LU give the mixed
+    run's error."""
     K = args.extra_steps
     gates = 76500
-    eng, nstats, depth = make_engine(gates, max_steps=K + 8, precision="mixed", refine=3)
+    eng, nstats, depth = make_engine(gates, max_steps=K + 8, precision="mixed", refine=args.refine)
     dev = eng.device
     info = dev.solver_info()
     X0, Q0, I0, maxc0, ok = eng.initial_state()
@@ -900,14 +901,14 @@ def extra_mixed(args):
     n = min(out_m["n_steps"], out_d["n_steps"])
     return {"workload": "random_gate_network_260k_transistors_adaptive_bdf2_mixed", "gates": gates,
             "transistors": nstats.transistors, "n_unknowns": info["n_aug"], "nnz_lu": info["nnz_lu"],
-            "precision": "FP64 evaluation/residual/update/LTE, FP32 LU + 3 FP64 refinement sweeps",
+            "precision": f"FP64 evaluation/residual/update/LTE, FP32 LU + {args.refine} FP64 refinement sweep(s)",
             "steps_timed": K, "ms_per_step": dev_ms / K, "newton_iters": iters,
             "fp64_lu_ms_per_step": ms64 / K, "fp64_lu_newton_iters": it64,
             "mixed_vs_fp64": {"max_abs_dv_V": float(np.max(np.abs(out_m["V"][:n] - out_d["V"][:n]))),
                               "steps_compared": int(n),
                               "times_identical": bool(np.array_equal(out_m["times"][:n], out_d["times"][:n]))},
             "vs_oracle": "tests/test_config_parity.py::test_network_80k_mixed_precision_against_oracle "
-                         "(the 80k network, FP32 LU + 3 sweeps, within 1e-6 V of the FP64 oracle)"}
+                         "(the 80k network, FP32 LU + one sweep, within 1e-6 V of the FP64 oracle)"}
 
 
 def extra_configs(args):
@@ -941,7 +942,7 @@ def main():
     ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="fp64: FP64 LU; mixed: FP32 LU + FP64-residual refinement (--refine sweeps)")
-    ap.add_argument("--refine", type=int, default=3, help="mixed: refinement sweeps (0-3)")
+    ap.add_argument("--refine", type=int, default=1, help="mixed: refinement sweeps (0-3)")
     ap.add_argument("--jobs", type=int, default=SERVING["jobs"], help="serving: jobs in the stream")
     ap.add_argument("--slots", type=int, default=8, help="serving: concurrent groups")
     ap.add_argument("--max-batch", type=int, default=64, help="serving: jobs per same-pattern group")

@@ -346,7 +346,7 @@ int vgb_set_tuning(void* h, int knob, int value) {
                 SparseLU& L = c->lu;
                 if (!c->analyzed || L.task_type.empty()) return;
                 // the host list schedule simulates one worker per CTA
-                schedule_tasks(L, (c->finalized ? sm_count() : 150) * value);
+                schedule_tasks(L, (c->finalized ? sm_count() : 152) * std::min(value, MF_FACTOR_CTAS_MAX));
                 if (c->finalized) {
                     VGB_CUDA(cudaStreamSynchronize(c->stream));
                     L.d_task_type.upload(L.task_type);

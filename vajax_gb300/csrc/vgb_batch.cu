@@ -334,17 +334,29 @@ __device__ __forceinline__ double warp_max(double v) {
 // contributions and resistive residuals of the node rows.
 struct WarpWS {
     double* M; double* f; double* Q; double* maxc; double* fres;
+    BRep* rep;  // the replica's controller state for the tick (read once, written back at its end)
 };
 
+constexpr size_t BREP_DOUBLES = (sizeof(BRep) + 7) / 8;
+
 __host__ __device__ inline size_t ws_doubles(int n_aug, int n_unk) {
-    return (size_t)n_aug * n_aug + n_aug + 3 * (size_t)(n_unk > 0 ? n_unk : 1);
+    return (size_t)n_aug * n_aug + n_aug + 3 * (size_t)(n_unk > 0 ? n_unk : 1) + BREP_DOUBLES;
 }
 
 __device__ __forceinline__ WarpWS warp_ws(const BatchArgs& a) {
     extern __shared__ double batch_smem[];
     const size_t n = a.n_aug, nu = a.n_unk > 0 ? a.n_unk : 1;
     double* base = batch_smem + (threadIdx.x >> 5) * ws_doubles(a.n_aug, a.n_unk);
-    return WarpWS{base, base + n * n, base + n * n + n, base + n * n + n + nu, base + n * n + n + 2 * nu};
+    return WarpWS{base, base + n * n, base + n * n + n, base + n * n + n + nu, base + n * n + n + 2 * nu,
+                  reinterpret_cast<BRep*>(base + n * n + n + 3 * nu)};
+}
+
+// Warp-cooperative copy of a controller state (32-bit words).
+__device__ __forceinline__ void copy_brep(BRep* dst, const BRep* src, int lane) {
+    static_assert(sizeof(BRep) % 4 == 0, "BRep is copied as 32-bit words");
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int i = lane; i < (int)(sizeof(BRep) / 4); i += 32) d[i] = s[i];
 }
 
 // Source waveforms of replica r at time t (lanes over sources).
@@ -476,20 +488,36 @@ __device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int la
     int bad = 0;
     const long long t0 = prof ? clock64() : 0;
     for (int k = 0; k < n; ++k) {
-        unsigned long long best = 0;
-        int bi = n;
-        for (int i = k + lane; i < n; i += 32) {
-            const unsigned long long bits = (unsigned long long)__double_as_longlong(M[i + (size_t)k * n]) &
-                                            0x7fffffffffffffffull;  // |M(i,k)|
-            const unsigned long long key = bits > 0x7ff0000000000000ull ? 0ull : bits;  // NaN counts as 0
-            if (bi == n || key > best) { best = key; bi = i; }
+        int p;
+        if (n - k <= 32) {
+            // the column fits the warp: three reductions (high word, low word, first index)
+            const int i = k + lane;
+            const bool valid = i < n;
+            unsigned long long key = 0;
+            if (valid) {
+                key = (unsigned long long)__double_as_longlong(M[i + (size_t)k * n]) & 0x7fffffffffffffffull;
+                if (key > 0x7ff0000000000000ull) key = 0;  // NaN counts as 0
+            }
+            const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+            const unsigned mh = __reduce_max_sync(0xffffffffu, valid ? hi : 0u);
+            const unsigned ml = __reduce_max_sync(0xffffffffu, valid && hi == mh ? lo : 0u);
+            p = (int)__reduce_min_sync(0xffffffffu, valid && hi == mh && lo == ml ? (unsigned)i : 0xffffffffu);
+        } else {
+            unsigned long long best = 0;
+            int bi = n;
+            for (int i = k + lane; i < n; i += 32) {
+                const unsigned long long bits = (unsigned long long)__double_as_longlong(M[i + (size_t)k * n]) &
+                                                0x7fffffffffffffffull;  // |M(i,k)|
+                const unsigned long long key = bits > 0x7ff0000000000000ull ? 0ull : bits;  // NaN counts as 0
+                if (bi == n || key > best) { best = key; bi = i; }
+            }
+            for (int o = 16; o; o >>= 1) {
+                const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (oi < n && (bi == n || ob > best || (ob == best && oi < bi))) { best = ob; bi = oi; }
+            }
+            p = bi;
         }
-        for (int o = 16; o; o >>= 1) {
-            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (oi < n && (bi == n || ob > best || (ob == best && oi < bi))) { best = ob; bi = oi; }
-        }
-        const int p = bi;
         if (p != k) {
             for (int j = lane; j < n; j += 32) {
                 const double t = M[k + (size_t)j * n];
@@ -744,9 +772,7 @@ __device__ bool replica_init(const BatchArgs& a, const WarpWS& w, int r, BRep& s
     return replica_plan(a, r, s, true, lane);
 }
 
-__device__ __noinline__ void replica_tick(const BatchArgs& a, int r, int lane) {
-    BRep& s = a.rep[r];
-    const WarpWS w = warp_ws(a);
+__device__ void replica_tick_body(const BatchArgs& a, const WarpWS& w, int r, BRep& s, int lane) {
     const int state = s.state;
     if (state == RS_DONE) return;
     __syncwarp();
@@ -771,6 +797,22 @@ __device__ __noinline__ void replica_tick(const BatchArgs& a, int r, int lane) {
     }
     // RS_NR: the contributions in hand are those of Xc
     replica_nr(a, w, r, s, lane);
+}
+
+// One tick of replica r.  Its controller state lives in the warp's shared
+// workspace for the tick: every field the step reads (Newton coefficients,
+// counters, the plan) would otherwise be a dependent global load, each an L2
+// round trip since lane 0 rewrote the line in the previous tick.
+__device__ __noinline__ void replica_tick(const BatchArgs& a, int r, int lane) {
+    BRep* gs = a.rep + r;
+    if (gs->state == RS_DONE) return;
+    const WarpWS w = warp_ws(a);
+    copy_brep(w.rep, gs, lane);
+    __syncwarp();
+    replica_tick_body(a, w, r, *w.rep, lane);
+    __syncwarp();
+    copy_brep(gs, w.rep, lane);
+    __syncwarp();
 }
 
 __global__ void __launch_bounds__(BATCH_THREADS, 1) batch_kernel(BatchArgs a) {

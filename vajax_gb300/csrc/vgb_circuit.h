@@ -139,7 +139,7 @@ struct SparseLU {
     std::vector<int> fr_tile0;                        // first tile of the front in the tile arrays
     long long n_tiles = 0;
     double sched_makespan_ns = 0;                     // simulated factorisation time of the task schedule
-    int sched_slots = 600;                            // workers of the list-schedule simulation
+    int sched_slots = 304;                            // workers of the list-schedule simulation
     std::vector<long long> tasm_ptr;                  // per tile: A entries (slot, tile-local position)
     std::vector<int> tasm_e, tasm_pos;
     std::vector<long long> tch_ptr;                   // per tile: child blocks {child, r0, r1, c0, c1}
@@ -258,5 +258,10 @@ int sm_count();
 void mf_prepare_capture(Circuit& c);
 // Re-order the factorisation task list for `slots` concurrent workers.
 void schedule_tasks(SparseLU& L, int slots);
+
+// Factorisation CTAs: eight warps each (two per SM sub-partition), at most two
+// per SM; a tuning value above that runs as that.
+constexpr int MF_FACTOR_THREADS = 256;
+constexpr int MF_FACTOR_CTAS_MAX = 2;
 
 } // namespace vgb

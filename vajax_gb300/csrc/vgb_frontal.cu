@@ -99,7 +99,6 @@ struct MFArgs {
 };
 
 constexpr int MF_THREADS = 128;
-constexpr int MF_CTAS_PER_SM = 4;
 constexpr int LD = FRONT_TILE_LD;
 constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
 // shared memory of a factorisation CTA: one small front, or three tiles
@@ -193,14 +192,17 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
 // ---- tiles of large fronts -----------------------------------------------------
 
 // The tile kernels below spread each elimination step over the CTA's four
-// warps (one per SM sub-partition: FP64 issue is the bottleneck on this part)
-// and exchange the step's pivot row or column through shared memory.
-constexpr int NWARP = MF_THREADS / 32;
+// eight warps (two per SM sub-partition: each warp issues FP64 at a third of
+// the SM's rate, so the chain of dependent elimination steps shortens with
+// fewer columns per warp) and exchange the step's pivot row or column through
+// shared memory.
+constexpr int NWARP = MF_FACTOR_THREADS / 32;
 constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
+static_assert((NWARP & (NWARP - 1)) == 0 && FRONT_TILE % NWARP == 0, "warps per tile: a power of two dividing 32");
 
 // Tile rows [r0, r0+nr) x columns [c0, c0+nc) of front F (leading dimension m),
 // zero-padded to 32 x 32, held in registers (lane = row, warp w has columns w,
-// w + 4, ...).  fetch_tile only issues the loads, so a task fetches all of its
+// w + NWARP, ...).  fetch_tile only issues the loads, so a task fetches all of its
 // tiles before the first shared-memory store and their L2 latencies overlap.
 template <typename T>
 struct TileRegs {
@@ -274,7 +276,7 @@ __device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T&
 // the barrier that every reader of that slot has passed.
 
 // LU without pivoting of the leading n x n block of a tile.  lane = row; warp
-// g owns columns g, g + 4, ... in registers.  The owner of column p + 1
+// g owns columns g, g + NWARP, ... in registers.  The owner of column p + 1
 // updates that column first and forms the next pivot's reciprocal (kept in its
 // registers) while the other warps finish step p, which keeps the FP64
 // division off the chain of dependent steps.
@@ -321,7 +323,7 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
 }
 
 // x := x U^-1 with U the upper triangle (with diagonal) of the n x n tile d.
-// lane = row of x; warp g owns columns g, g + 4, ...
+// lane = row of x; warp g owns columns g, g + NWARP, ...
 template <typename T>
 __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
@@ -354,7 +356,7 @@ __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
 }
 
 // x := L^-1 x with L the unit lower triangle of the n x n tile d.  lane =
-// column of x; warp g owns rows g, g + 4, ...
+// column of x; warp g owns rows g, g + NWARP, ...
 template <typename T>
 __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
@@ -381,27 +383,26 @@ __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch) {
 }
 
 // c -= l u over the first nk columns of l / rows of u (all tiles zero-padded):
-// lane = row, warp w takes columns w, w + 4, ...
+// lane = row, warp w takes columns w, w + NWARP, ...
 template <typename T>
 __device__ void gemm_tile(T* c, const T* l, const T* u, int nk, int nj) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int Q = FRONT_TILE / (MF_THREADS / 32);
-    T acc[Q];
+    T acc[QPW];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) acc[q] = (T)0;
+    for (int q = 0; q < QPW; ++q) acc[q] = (T)0;
     for (int k = 0; k < nk; ++k) {
         const T lv = l[lane + k * LD];
 #pragma unroll
-        for (int q = 0; q < Q; ++q)
-            if (warp + 4 * q < nj) acc[q] += lv * u[k + (warp + 4 * q) * LD];
+        for (int q = 0; q < QPW; ++q)
+            if (warp + NWARP * q < nj) acc[q] += lv * u[k + (warp + NWARP * q) * LD];
     }
 #pragma unroll
-    for (int q = 0; q < Q; ++q) c[lane + (warp + 4 * q) * LD] -= acc[q];
+    for (int q = 0; q < QPW; ++q) c[lane + (warp + NWARP * q) * LD] -= acc[q];
     __syncthreads();
 }
 
 template <typename T>
-__global__ void __launch_bounds__(MF_THREADS, MF_CTAS_PER_SM) mf_factor_kernel(MFArgs a, T* pool) {
+__global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_factor_kernel(MFArgs a, T* pool) {
     extern __shared__ double smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_task;
@@ -856,9 +857,9 @@ static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, L.n_tiles * sizeof(int), s));
     MFArgs a = mf_args(c, A);
     a.epoch = 1;
-    const int blocks = std::min(sm_count() * std::min(std::max(c.tune_factor_ctas, 1), MF_CTAS_PER_SM),
+    const int blocks = std::min(sm_count() * std::min(std::max(c.tune_factor_ctas, 1), MF_FACTOR_CTAS_MAX),
                                 std::max(a.n_tasks, 1));
-    mf_factor_kernel<T><<<blocks, MF_THREADS, smem, s>>>(a, pool);
+    mf_factor_kernel<T><<<blocks, MF_FACTOR_THREADS, smem, s>>>(a, pool);
     VGB_CUDA(cudaGetLastError());
 }
 

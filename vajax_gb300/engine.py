@@ -181,7 +181,7 @@ class CircuitEngine:
             prec = {"fp64": 0, "fp32": 1, "mixed": 1}[self.precision]
             if self.rc.n_nodes - 1 + len(self.rc.vsources) <= DENSE_MAX:
                 prec = 2  # small circuits: dense LU with partial pivoting, as the reference's dense path
-            dev = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 3),
+            dev = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 1),
                                 gmin=self.options.gmin, device=False)
             try:
                 if on_analyzed is not None:
@@ -256,7 +256,7 @@ class CircuitEngine:
         prec = getattr(dev, "precision", 0)
         if prec != 1:
             return self._initial_state()
-        sweeps = getattr(self, "refine_sweeps", 3)
+        sweeps = getattr(self, "refine_sweeps", 1)
         dev.set_precision(0)
         try:
             return self._initial_state()
