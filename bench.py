@@ -754,6 +754,41 @@ def run_eval_stamp(args):
         print(json.dumps(out_line), flush=True)
 
 
+def run_ring_batch(args):
+    """The 7-stage ring on the batched engine (one replica, the cooperative
+    evaluation): --warmup steps in a first run, then --steps fixed 1 ps gear2
+    steps timed by the kernel's own CUDA events.  The JSON line carries the
+    batch kernel's per-tick phase cycles."""
+    import torch
+    from vajax_gb300.batch import BatchedTransient
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    eng = make_ring_engine(device=False)
+    rc = eng.rc
+    cfg = eng.transient_cfg()
+    X0 = _ring_uic_start(eng)[None, :]
+    bt = BatchedTransient([rc], gmin=eng.options.gmin)
+    bt.transient(dict(cfg, t_stop=args.warmup * RING["dt"], max_steps=args.warmup + 1), X0)
+    sampler = ClockSampler(gpu_index(local))
+    sampler.start()
+    out = bt.transient(dict(cfg, t_stop=args.steps * RING["dt"], max_steps=args.steps + 1), X0)
+    clocks = sampler.stop()
+    bt.close()
+    steps = int(out["n_steps"][0]) - 1
+    ms = out["device_ms"]
+    ticks = max(out["ticks"], 1)
+    line = {"metric": "transient_ms_per_step", "value": ms / steps, "unit": "ms/step", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (7-stage ring)",
+            "config": {"workload": RING["workload"] + "_batched", "model": "ekv", "engine": "batched (one replica)",
+                       "coop_units": out["coop_units"], "l2": "working set far below L2 (one small circuit)"},
+            "newton_iters": int(out["total_nr_iters"][0]), "ticks": out["ticks"],
+            "cycles_per_tick": {k: v / ticks for k, v in out["phase_cycles"].items()},
+            "gpu_launches": 2, "clocks": clocks, "e2e": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------
 # the other configurations, measured in the default run (one GPU)
 # ---------------------------------------------------------------------------
@@ -934,10 +969,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["gates", "ring", "corners_ring", "corners_gates", "serving", "eval_stamp"],
+    ap.add_argument("--workload", choices=["gates", "ring", "ring_batch", "corners_ring", "corners_gates", "serving",
+                                           "eval_stamp"],
                     default="gates",
                     help="gates: seeded random gate network, adaptive BDF2 (default, 80k transistors); "
-                         "ring: 7-stage ring, fixed-step BDF2 at 1 ps; corners_ring / corners_gates: 1,024 "
+                         "ring: 7-stage ring, fixed-step BDF2 at 1 ps (single-circuit path); ring_batch: the same "
+                         "on the batched engine (--steps 1 ps steps); corners_ring / corners_gates: 1,024 "
                          "ring or 256 ~2,000-transistor network Monte-Carlo corners batched in one circuit")
     ap.add_argument("--gates", type=int, default=WORKLOAD["gates"], help="network size (default: the 80k-T network)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
@@ -969,6 +1006,8 @@ def main():
         run_serving(args)
     elif args.workload == "eval_stamp":
         run_eval_stamp(args)
+    elif args.workload == "ring_batch":
+        run_ring_batch(args)
     else:
         run_gb300(args)
 

@@ -124,58 +124,52 @@ def test_block_diagonal_ring_corners_match_oracle(cuda):
 
 # ---- config 2: the 80k-transistor network ---------------------------------------
 
-def _switch_run(mode, precision="fp64"):
+def _switch_run(precision="fp64"):
     fx = load("gates23530_switch")
     X, Q, I, maxc = M.dc_state()
     eng = M.switch_engine()
     eng.precision = precision
-    eng.refine_sweeps = 3
+    eng.refine_sweeps = 1
     eng.prepare(t_stop=eng.t_stop, dt=eng.dt, max_steps=M.NET_STEPS + 1)
-    g = eng.device.transient(M.switch_cfg(eng, mode), X, Q, I, maxc)
+    g = eng.device.transient(M.switch_cfg(eng), X, Q, I, maxc)
     eng.device.close()
     return fx, g
 
 
-def _switch_check(fx, g, mode):
-    """Largest node-voltage difference to the oracle: every node at the last
-    step, the fixture's node sample at every step."""
+def _switch_check(fx, g):
+    """The oracle's step sequence, and the largest node-voltage difference to
+    the oracle: every node at the last step, the fixture's node sample at
+    every step."""
     n = g["n_steps"]
-    assert n == len(fx[f"{mode}_times"])
-    assert g["rejected"] == int(fx[f"{mode}_rejected"])
-    np.testing.assert_allclose(g["times"][:n], fx[f"{mode}_times"], rtol=1e-9)
+    assert n == len(fx["times"])
+    assert g["rejected"] == int(fx["rejected"])
+    np.testing.assert_allclose(g["times"][:n], fx["times"], rtol=1e-9)
     V = g["V"][:n]
-    err_last = float(np.max(np.abs(V[-1] - fx[f"{mode}_V_last"])))
-    err_rows = float(np.max(np.abs(V[:, fx[f"{mode}_sample"]] - fx[f"{mode}_V_sample"])))
+    err_last = float(np.max(np.abs(V[-1] - fx["V_last"])))
+    err_rows = float(np.max(np.abs(V[:, fx["sample"]] - fx["V_sample"])))
     return max(err_last, err_rows)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["fixed", "adaptive"])
-def test_network_80k_matches_oracle(cuda, mode):
-    """The benchmarked 23,530-gate network (inputs switching from 2 ps on),
-    from the oracle's DC point: every node within 1e-6 V of the oracle, the
-    same step times, rejections and step count, no Newton failure; adaptive
-    runs also take the oracle's Newton iterations."""
-    fx, g = _switch_run(mode)
-    assert g["nr_failures"] == 0
-    if mode == "adaptive":
-        assert g["total_nr_iters"] == int(fx[f"{mode}_total_nr_iters"])
-    else:
-        # fixed steps from the DC point: the first residual test of a step
-        # compares a residual of rounding size with its tolerance, so whether
-        # it passes at iteration 0 or 1 can go either way (the solution moves
-        # by rounding only)
-        assert abs(g["total_nr_iters"] - int(fx[f"{mode}_total_nr_iters"])) <= M.NET_STEPS
-    err = _switch_check(fx, g, mode)
+def test_network_80k_matches_oracle(cuda):
+    """The benchmarked 23,530-gate network, its inputs switching from 10 ps
+    on, adaptive gear2 with the benchmark's settings from the oracle's DC
+    point through the first input edges: the oracle's step times, rejections,
+    Newton iterations and Newton failures, every node within 1e-6 V."""
+    fx, g = _switch_run()
+    assert g["total_nr_iters"] == int(fx["total_nr_iters"])
+    assert g["nr_failures"] == int(fx["nr_failures"])
+    err = _switch_check(fx, g)
     assert err < V_TOL, err
 
 
 @pytest.mark.gpu
 def test_network_80k_mixed_precision_against_oracle(cuda):
-    """FP32 LU with three FP64-residual refinement sweeps on the same fixed
-    (trapezoidal) steps: node voltages within 1e-6 V of the FP64 oracle."""
-    fx, g = _switch_run("fixed", precision="mixed")
-    err = _switch_check(fx, g, "fixed")
+    """FP32 LU with one FP64-residual refinement sweep (the default) on the
+    same adaptive run: the oracle's steps, node voltages within 1e-6 V of the
+    FP64 oracle."""
+    fx, g = _switch_run(precision="mixed")
+    err = _switch_check(fx, g)
     assert err < V_TOL, err
 
 
@@ -236,7 +230,7 @@ def test_network_fixture_matches_the_benchmark_network():
     X, _, _, _ = M.dc_state()
     rc = M.switch_network().resolve()
     assert rc.n_nodes + len(rc.vsources) == len(X)
-    for mode in ("fixed", "adaptive"):
-        assert len(fx[f"{mode}_V_last"]) == rc.n_external
-        assert fx[f"{mode}_V_sample"].shape == (len(fx[f"{mode}_times"]), M.NET_SAMPLE)
-        assert np.all(fx[f"{mode}_sample"] < rc.n_external)
+    assert len(fx["V_last"]) == rc.n_external
+    assert fx["V_sample"].shape == (len(fx["times"]), M.NET_SAMPLE)
+    assert np.all(fx["sample"] < rc.n_external)
+    assert len(fx["times"]) == M.NET_STEPS + 1

@@ -58,7 +58,10 @@ from typing import Dict, List, Tuple
 from vajax_gb300.codegen.cuda import MirProgram
 
 W_DEFAULT = 4
-DELTA = 1.0  # cost of handing a value to another warp (store, barrier, load), FP64-instruction units
+# cost of handing a value to another warp, FP64-instruction units (64 cycles):
+# a store, a named barrier and a load take about 190 cycles on GB300, and
+# measured over 1.0-4.5 the larger cost (fewer, longer segments) ran fastest
+DELTA = 4.5
 MIN_COST = 0.05
 # FP64-instruction equivalents per opcode, measured on GB300 for the
 # table-driven functions of csrc/vgb_math.cuh (division 8.7, exp 13.5,

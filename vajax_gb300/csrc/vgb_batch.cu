@@ -369,6 +369,19 @@ __device__ void replica_sources(const BatchArgs& a, int r, double t, int lane) {
                                                      a.is_cnt[k], t);
 }
 
+// NaN -> 0 and the running max of |v| on the bit patterns: integer work, not
+// the FP64 pipe, which one warp reaches only once per 64 cycles.  Same values
+// as nan0(x) and fmax(m, fabs(v)) for m >= 0 and v not NaN.
+__device__ __forceinline__ double nan0_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0.0 : x;
+}
+__device__ __forceinline__ double max_abs_bits(double m, double v) {
+    const unsigned long long bm = (unsigned long long)__double_as_longlong(m);
+    const unsigned long long bv = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return __longlong_as_double((long long)(bv > bm ? bv : bm));
+}
+
 // Contribution of gather entry idx of replica r.  Another SM may have
 // written it in this tick: read it from L2, unless the grid is one CTA.
 __device__ __forceinline__ double cval(const BatchArgs& a, int idx, int r) {
@@ -403,7 +416,7 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
                     }
 #pragma unroll
                 for (int t = 0; t < 8; ++t)
-                    if (q + t < q1) s += nan0(jr[t] + c0 * jq[t]);
+                    if (q + t < q1) s += nan0_bits(jr[t] + c0 * jq[t]);
             }
             if (a.csr_diag[e]) s += a.gmin + gshunt;
             s += a.csr_const[e];
@@ -429,18 +442,18 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
 #pragma unroll
                 for (int t = 0; t < 8; ++t)
                     if (e + t < e1) {
-                        const double v = nan0(rv[t]);
+                        const double v = nan0_bits(rv[t]);
                         fr += v;
-                        mc = fmax(mc, fabs(v));
-                        q += nan0(qv[t]);
+                        mc = max_abs_bits(mc, v);
+                        q += nan0_bits(qv[t]);
                     }
             }
             for (int e = a.ni_ptr[row]; e < a.ni_ptr[row + 1]; ++e) {
                 const int kk = a.ni_idx[e];
                 double v = kk > 0 ? a.is[(size_t)r * a.n_isrc + kk - 1] : -a.is[(size_t)r * a.n_isrc - kk - 1];
-                v = nan0(v);
+                v = nan0_bits(v);
                 fr += v;
-                mc = fmax(mc, fabs(v));
+                mc = max_abs_bits(mc, v);
             }
             w.fres[row] = fr;
             for (int e = a.nb_ptr[row]; e < a.nb_ptr[row + 1]; ++e) {
