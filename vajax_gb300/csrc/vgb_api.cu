@@ -518,6 +518,12 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
             g.d_shared.upload(g.shared.empty() ? std::vector<double>{0.0} : g.shared);
             if (!g.varying.empty()) g.d_varying.upload(g.varying);
             if (!g.temps.empty()) g.d_temps.upload(g.temps);
+            // parameters are fixed from here on: the model's cache program runs once
+            if (g.me && g.me->ncache > 0 && g.n_dev > 0) {
+                g.d_cache.alloc((size_t)g.me->ncache * g.n_dev);
+                g.me->launch_cache(g.args(nullptr), g.d_cache.p, c->stream);
+                VGB_CUDA(cudaGetLastError());
+            }
         }
         c->d_csr_src_ptr.upload(c->csr_src_ptr);
         c->d_csr_src.upload(c->csr_src);

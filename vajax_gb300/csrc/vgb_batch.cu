@@ -186,12 +186,8 @@ struct CacheR {
     }
 };
 
-// Models with a generated cache program (the cooperative ones) read their
-// parameter-only values from the per-instance cache in the one-warp path too.
-template <class M, class = void>
-struct HasCache : std::false_type {};
-template <class M>
-struct HasCache<M, std::void_t<decltype(M::NCACHE)>> : std::true_type {};
+// Models with a generated cache program (HasCache) read their parameter-only
+// values from the per-instance cache in the one-warp path too.
 
 template <class M>
 __device__ __noinline__ void eval_item(const BatchArgs& a, const BGroup& g, int d, int r) {

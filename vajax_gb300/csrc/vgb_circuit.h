@@ -54,6 +54,7 @@ struct Group {
     std::vector<int> csr_pos;        // [n_dev][nj] CSR data position or -1 (reference layout)
     DevBuf<int> d_node_map, d_vidx;
     DevBuf<double> d_shared, d_varying, d_temps;
+    DevBuf<double> d_cache;          // [ncache][n_dev] parameter-only values of the model body, if it has them
     GroupArgs args(double* contrib) const {
         GroupArgs g{};
         g.n_dev = n_dev;
@@ -66,6 +67,7 @@ struct Group {
         g.contrib = contrib + contrib_base;
         g.batch_stride_x = 0;
         g.inst_per_replica = n_dev;
+        g.cache = d_cache.p;
         return g;
     }
 };

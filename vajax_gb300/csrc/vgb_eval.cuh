@@ -17,6 +17,8 @@
 // masks NaN to 0 and scatter-adds into the CSR data and the dense vectors.
 #pragma once
 
+#include <type_traits>
+
 #include "vgb_common.cuh"
 
 namespace vgb {
@@ -32,6 +34,29 @@ struct GroupArgs {
     double* __restrict__ contrib;         // [NJ + 2 NN][n_dev]
     long long batch_stride_x;             // stride of X between circuit replicas (batched mode)
     int inst_per_replica;                 // instances per replica (batched mode), else n_dev
+    const double* __restrict__ cache;     // [NCACHE][n_dev] parameter-only values, or nullptr
+};
+
+// Models whose generated struct carries a cache program (codegen/coop.py):
+// the values of the body that depend on parameters and temperature only are
+// computed once per instance (cache_kernel) and read by every evaluation
+// through eval_cached.
+template <class M, class = void>
+struct HasCache : std::false_type {};
+template <class M>
+struct HasCache<M, std::void_t<decltype(M::NCACHE)>> : std::true_type {};
+
+// Reader / writer of one instance's cache column, [NCACHE][n] layout.
+struct CacheCol {
+    const double* c;
+    size_t n, i;
+    __device__ __forceinline__ double operator()(int k) const { return __ldg(c + (size_t)k * n + i); }
+    __device__ __forceinline__ bool b(int k) const { return __double_as_longlong(__ldg(c + (size_t)k * n + i)) != 0; }
+};
+struct CacheColW {
+    double* c;
+    size_t n, i;
+    __device__ __forceinline__ void operator()(int k, double v) const { c[(size_t)k * n + i] = v; }
 };
 
 // Named barrier of the warps that share one cooperative model evaluation
@@ -80,6 +105,29 @@ struct ParamReader {
     }
 };
 
+// One instance's model body: the cached one when the group has a cache.
+template <class M, class PF>
+__device__ __forceinline__ void eval_instance(const GroupArgs& g, int i, const PF& P, double T, const double* V,
+                                              double* rr, double* rq, double* jr, double* jq) {
+    if constexpr (HasCache<M>::value) {
+        if (g.cache) {
+            M::eval_cached(P, CacheCol{g.cache, (size_t)g.n_dev, (size_t)i}, T, V, rr, rq, jr, jq);
+            return;
+        }
+    }
+    M::eval(P, T, V, rr, rq, jr, jq);
+}
+
+// The cache program, one thread per instance.
+template <class M>
+__global__ void __launch_bounds__(128) cache_kernel(GroupArgs g, double* cache) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n_dev) return;
+    const double T = g.temperature ? __ldg(g.temperature + i) : g.temp_shared;
+    ParamReader<M> P{g, i};
+    M::cache(P, T, CacheColW{cache, (size_t)g.n_dev, (size_t)i});
+}
+
 // Device evaluation is FP64-pipe bound: small blocks spread the instances over
 // every SM instead of packing them onto a few.  The block size is a launch
 // parameter (default 64) that the autotuner may change; EVAL_BLOCK_MAX bounds it.
@@ -101,7 +149,7 @@ __global__ void __launch_bounds__(EVAL_BLOCK_MAX) eval_kernel(GroupArgs g, const
     const double T = g.temperature ? __ldg(g.temperature + i) : g.temp_shared;
     double rr[M::NN], rq[M::NN], jr[M::NJ > 0 ? M::NJ : 1], jq[M::NJ > 0 ? M::NJ : 1];
     ParamReader<M> P{g, i};
-    M::eval(P, T, V, rr, rq, jr, jq);
+    eval_instance<M>(g, i, P, T, V, rr, rq, jr, jq);
     const size_t n = g.n_dev;
 #pragma unroll
     for (int k = 0; k < M::NJ; ++k) g.contrib[k * n + i] = nan0(jr[k] + c0 * jq[k]);
@@ -125,7 +173,7 @@ __global__ void __launch_bounds__(128) eval_raw_kernel(GroupArgs g, const double
     const double T = g.temperature ? __ldg(g.temperature + i) : g.temp_shared;
     double rr[M::NN], rq[M::NN], jr[M::NJ > 0 ? M::NJ : 1], jq[M::NJ > 0 ? M::NJ : 1];
     ParamReader<M> P{g, i};
-    M::eval(P, T, V, rr, rq, jr, jq);
+    eval_instance<M>(g, i, P, T, V, rr, rq, jr, jq);
     const size_t n = g.n_dev;
     for (int r = 0; r < M::NN; ++r) {
         out[(size_t)r * n + i] = rr[r];
@@ -144,6 +192,8 @@ struct ModelEntry {
     const int* jcol;
     void (*launch)(const GroupArgs&, const double* X, const double* kdev, int block, cudaStream_t s);
     void (*launch_raw)(const GroupArgs&, const double* X, double* out, cudaStream_t s);
+    int ncache;  // cache values per instance, 0 without a cache program
+    void (*launch_cache)(const GroupArgs&, double* cache, cudaStream_t s);
 };
 
 template <class M>
@@ -161,9 +211,21 @@ void launch_eval_raw(const GroupArgs& g, const double* X, double* out, cudaStrea
 }
 
 template <class M>
+void launch_cache(const GroupArgs& g, double* cache, cudaStream_t s)
+{
+    if constexpr (HasCache<M>::value) {
+        if (g.n_dev == 0) return;
+        cache_kernel<M><<<ceil_div(g.n_dev, 128), 128, 0, s>>>(g, cache);
+    }
+}
+
+template <class M>
 ModelEntry make_model_entry(const char* name)
 {
-    return ModelEntry{name, M::NN, M::NJ, M::NP, M::JROW, M::JCOL, &launch_eval<M>, &launch_eval_raw<M>};
+    int ncache = 0;
+    if constexpr (HasCache<M>::value) ncache = M::NCACHE;
+    return ModelEntry{name, M::NN, M::NJ, M::NP, M::JROW, M::JCOL, &launch_eval<M>, &launch_eval_raw<M>,
+                      ncache, &launch_cache<M>};
 }
 
 // Defined in the generated translation unit.
