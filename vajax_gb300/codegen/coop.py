@@ -59,9 +59,11 @@ from vajax_gb300.codegen.cuda import MirProgram
 
 W_DEFAULT = 4
 # cost of handing a value to another warp, FP64-instruction units (64 cycles):
-# a store, a named barrier and a load take about 190 cycles on GB300, and
-# measured over 1.0-4.5 the larger cost (fewer, longer segments) ran fastest
-DELTA = 4.5
+# a store, a named barrier and a load take about 190 cycles on GB300, and the
+# segments' real durations drift from the modelled ones, so every barrier
+# also costs the spread of its warps' arrivals; measured over 1 to 40 for
+# EKV, 24 ran fastest (56 barriers; 40 was slower again)
+DELTA = 24.0
 MIN_COST = 0.05
 # FP64-instruction equivalents per opcode, measured on GB300 for the
 # table-driven functions of csrc/vgb_math.cuh (division 8.7, exp 13.5,

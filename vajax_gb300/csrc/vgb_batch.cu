@@ -89,6 +89,10 @@ struct BatchArgs {
     long long n_items, n_contrib;
     long long n_coop_units;  // item warps evaluated by a group of COOP_WARPS warps
     long long coop_stride;   // doubles of shared memory per group (exchange slots x 32 lanes)
+    // assembly gather lists staged in shared memory at the start of the kernel
+    // (when they fit): counts and the byte offset of the staged area
+    int n_csr_src, n_res_src, stage;
+    long long stage_off;
     double gmin, reltol, abstol, vntol, damping;
     const BGroup* groups;
     // pattern and gather lists (one replica)
@@ -294,7 +298,10 @@ __device__ void eval_phase(const BatchArgs& a) {
     }
     const long long n_iw = (a.n_items + 31) / 32;
     const long long step = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long iw = (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; iw < n_iw; iw += step) {
+    // one-warp items start at the CTA's last warps, which hold no cooperative group
+    // when the batch has fewer cooperative units than groups: they run beside it
+    const int wr = (int)(blockDim.x >> 5) - 1 - (int)(threadIdx.x >> 5);
+    for (long long iw = (long long)wr * gridDim.x + blockIdx.x; iw < n_iw; iw += step) {
         const long long it = iw * 32 + lane;
         if (it >= a.n_items) continue;
         int gi = 0;
@@ -331,20 +338,32 @@ __device__ __forceinline__ double warp_max(double v) {
 struct WarpWS {
     double* M; double* f; double* Q; double* maxc; double* fres;
     BRep* rep;  // the replica's controller state for the tick (read once, written back at its end)
+    double* sc; // the assembly's gathered contributions (ws_scratch doubles), or null
 };
 
 constexpr size_t BREP_DOUBLES = (sizeof(BRep) + 7) / 8;
+constexpr int WS_SCRATCH_MAX = 1024;  // doubles of gather scratch per warp, at most
 
-__host__ __device__ inline size_t ws_doubles(int n_aug, int n_unk) {
-    return (size_t)n_aug * n_aug + n_aug + 3 * (size_t)(n_unk > 0 ? n_unk : 1) + BREP_DOUBLES;
+// Gather scratch per warp: every Jacobian contribution, or every resistive and
+// reactive residual contribution, of one replica; 0 (no scratch) when larger
+// than WS_SCRATCH_MAX.
+__host__ __device__ inline int ws_scratch(int n_csr_src, int n_res_src) {
+    const int need = n_csr_src > 2 * n_res_src ? n_csr_src : 2 * n_res_src;
+    return need <= WS_SCRATCH_MAX ? need : 0;
+}
+
+__host__ __device__ inline size_t ws_doubles(int n_aug, int n_unk, int scratch) {
+    return (size_t)n_aug * n_aug + n_aug + 3 * (size_t)(n_unk > 0 ? n_unk : 1) + BREP_DOUBLES + scratch;
 }
 
 __device__ __forceinline__ WarpWS warp_ws(const BatchArgs& a) {
     extern __shared__ double batch_smem[];
     const size_t n = a.n_aug, nu = a.n_unk > 0 ? a.n_unk : 1;
-    double* base = batch_smem + (threadIdx.x >> 5) * ws_doubles(a.n_aug, a.n_unk);
+    const int sc = ws_scratch(a.n_csr_src, a.n_res_src);
+    double* base = batch_smem + (threadIdx.x >> 5) * ws_doubles(a.n_aug, a.n_unk, sc);
+    double* rep = base + n * n + n + 3 * nu;
     return WarpWS{base, base + n * n, base + n * n + n, base + n * n + n + nu, base + n * n + n + 2 * nu,
-                  reinterpret_cast<BRep*>(base + n * n + n + 3 * nu)};
+                  reinterpret_cast<BRep*>(rep), sc ? rep + BREP_DOUBLES : nullptr};
 }
 
 // Warp-cooperative copy of a controller state (32-bit words).
@@ -398,21 +417,43 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
     const long long t0 = prof ? clock64() : 0;
     if (jac) {
         for (int t = lane; t < n * n; t += 32) w.M[t] = 0.0;
+        if (w.sc) {
+            // every contribution's jr + c0 jq over the lanes (eight loads of each lane in flight
+            // at once), then each entry's sum in its own order from shared memory: a supply
+            // rail's entry no longer waits on its chain of loads
+            const int ncs = a.n_csr_src;
+            for (int t0 = lane; t0 < ncs; t0 += 256) {
+                double jr[8], jq[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (t0 + 32 * u < ncs) {
+                        jr[u] = cval(a, a.csr_jr[t0 + 32 * u], r);
+                        jq[u] = cval(a, a.csr_jq[t0 + 32 * u], r);
+                    }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (t0 + 32 * u < ncs) w.sc[t0 + 32 * u] = nan0_bits(jr[u] + c0 * jq[u]);
+            }
+        }
         __syncwarp();
         for (int e = lane; e < a.nnz; e += 32) {
             double s = 0.0;
             const int q1 = a.csr_ptr[e + 1];
-            for (int q = a.csr_ptr[e]; q < q1; q += 8) {  // every load of a chunk in flight at once
-                double jr[8], jq[8];
+            if (w.sc) {
+                for (int q = a.csr_ptr[e]; q < q1; ++q) s += w.sc[q];
+            } else {
+                for (int q = a.csr_ptr[e]; q < q1; q += 8) {  // every load of a chunk in flight at once
+                    double jr[8], jq[8];
 #pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (q + t < q1) {
-                        jr[t] = cval(a, a.csr_jr[q + t], r);
-                        jq[t] = cval(a, a.csr_jq[q + t], r);
-                    }
+                    for (int t = 0; t < 8; ++t)
+                        if (q + t < q1) {
+                            jr[t] = cval(a, a.csr_jr[q + t], r);
+                            jq[t] = cval(a, a.csr_jq[q + t], r);
+                        }
 #pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (q + t < q1) s += nan0_bits(jr[t] + c0 * jq[t]);
+                    for (int t = 0; t < 8; ++t)
+                        if (q + t < q1) s += nan0_bits(jr[t] + c0 * jq[t]);
+                }
             }
             if (a.csr_diag[e]) s += a.gmin + gshunt;
             s += a.csr_const[e];
@@ -422,27 +463,56 @@ __device__ __noinline__ bool replica_assemble(const BatchArgs& a, const WarpWS& 
     }
     const long long t1 = prof ? clock64() : 0;
     bool ok = true, nf = false;
+    const int nrs = a.n_res_src;
+    if (w.sc) {  // the residual contributions over the lanes, as for the Jacobian
+        __syncwarp();
+        for (int t0 = lane; t0 < nrs; t0 += 256) {
+            double rv[8], qv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (t0 + 32 * u < nrs) {
+                    rv[u] = cval(a, a.res_rr[t0 + 32 * u], r);
+                    qv[u] = cval(a, a.res_rq[t0 + 32 * u], r);
+                }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (t0 + 32 * u < nrs) {
+                    w.sc[t0 + 32 * u] = nan0_bits(rv[u]);
+                    w.sc[nrs + t0 + 32 * u] = nan0_bits(qv[u]);
+                }
+        }
+        __syncwarp();
+    }
     for (int row = lane; row < n; row += 32) {
         double fn, tol;
         if (row < a.n_unk) {
             double fr = 0.0, q = 0.0, mc = 0.0;
             const int e1 = a.res_ptr[row + 1];
-            for (int e = a.res_ptr[row]; e < e1; e += 8) {  // every load of a chunk in flight at once
-                double rv[8], qv[8];
+            if (w.sc) {
+                for (int e = a.res_ptr[row]; e < e1; ++e) {
+                    const double v = w.sc[e];
+                    fr += v;
+                    mc = max_abs_bits(mc, v);
+                    q += w.sc[nrs + e];
+                }
+            } else {
+                for (int e = a.res_ptr[row]; e < e1; e += 8) {  // every load of a chunk in flight at once
+                    double rv[8], qv[8];
 #pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (e + t < e1) {
-                        rv[t] = cval(a, a.res_rr[e + t], r);
-                        qv[t] = cval(a, a.res_rq[e + t], r);
-                    }
+                    for (int t = 0; t < 8; ++t)
+                        if (e + t < e1) {
+                            rv[t] = cval(a, a.res_rr[e + t], r);
+                            qv[t] = cval(a, a.res_rq[e + t], r);
+                        }
 #pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (e + t < e1) {
-                        const double v = nan0_bits(rv[t]);
-                        fr += v;
-                        mc = max_abs_bits(mc, v);
-                        q += nan0_bits(qv[t]);
-                    }
+                    for (int t = 0; t < 8; ++t)
+                        if (e + t < e1) {
+                            const double v = nan0_bits(rv[t]);
+                            fr += v;
+                            mc = max_abs_bits(mc, v);
+                            q += nan0_bits(qv[t]);
+                        }
+                }
             }
             for (int e = a.ni_ptr[row]; e < a.ni_ptr[row + 1]; ++e) {
                 const int kk = a.ni_idx[e];
@@ -546,7 +616,7 @@ __device__ __noinline__ int replica_lu_solve(int n, double* M, double* b, int la
             piv = 1e-30;
             if (!bad) bad = k + 1;
         }
-        const double rinv = vgb_div(1.0, piv);
+        const double rinv = vgb_rcp(piv);  // on the chain of dependent pivot steps: the short reciprocal
         __syncwarp();
         if (lane == 0) M[k + (size_t)k * n] = rinv;  // the diagonal keeps 1 / pivot
         for (int i = k + 1 + lane; i < n; i += 32) M[i + (size_t)k * n] *= rinv;
@@ -824,8 +894,60 @@ __device__ __noinline__ void replica_tick(const BatchArgs& a, int r, int lane) {
     __syncwarp();
 }
 
+// Bytes of the staged gather lists, each array 16-byte aligned, in the order
+// stage_pattern lays them out.
+__host__ __device__ inline size_t stage_bytes(int nnz, int ncs, int nu, int nrs) {
+    auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    return al(4 * (size_t)(nnz + 1)) + 2 * al(4 * (size_t)ncs) + 2 * al(4 * (size_t)nnz) + al(8 * (size_t)nnz) +
+           al((size_t)nnz) + al(4 * (size_t)(nu + 1)) + 2 * al(4 * (size_t)nrs);
+}
+
+// The assembly's gather lists (the same for every replica and tick) copied
+// into this CTA's shared memory; `s` gets pointers to the copies.  Each
+// contribution's gather is then one global load (the value) instead of a
+// chain of three.
+__device__ void stage_pattern(const BatchArgs& a, BatchArgs& s) {
+    extern __shared__ double batch_smem[];
+    unsigned char* base = reinterpret_cast<unsigned char*>(batch_smem) + a.stage_off;
+    auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const int nnz = a.nnz, ncs = a.n_csr_src, nu = a.n_unk > 0 ? a.n_unk : 0, nrs = a.n_res_src;
+    auto take = [&](size_t bytes) { unsigned char* p = base; base += al(bytes); return p; };
+    int* csr_ptr = (int*)take(4 * (size_t)(nnz + 1));
+    int* csr_jr = (int*)take(4 * (size_t)ncs);
+    int* csr_jq = (int*)take(4 * (size_t)ncs);
+    int* csr_row = (int*)take(4 * (size_t)nnz);
+    int* indices = (int*)take(4 * (size_t)nnz);
+    double* csr_const = (double*)take(8 * (size_t)nnz);
+    unsigned char* csr_diag = take((size_t)nnz);
+    int* res_ptr = (int*)take(4 * (size_t)(nu + 1));
+    int* res_rr = (int*)take(4 * (size_t)nrs);
+    int* res_rq = (int*)take(4 * (size_t)nrs);
+    for (int i = threadIdx.x; i <= nnz; i += blockDim.x) csr_ptr[i] = a.csr_ptr[i];
+    for (int i = threadIdx.x; i < ncs; i += blockDim.x) {
+        csr_jr[i] = a.csr_jr[i];
+        csr_jq[i] = a.csr_jq[i];
+    }
+    for (int i = threadIdx.x; i < nnz; i += blockDim.x) {
+        csr_row[i] = a.csr_row[i];
+        indices[i] = a.indices[i];
+        csr_const[i] = a.csr_const[i];
+        csr_diag[i] = a.csr_diag[i];
+    }
+    for (int i = threadIdx.x; i <= nu; i += blockDim.x) res_ptr[i] = a.res_ptr[i];
+    for (int i = threadIdx.x; i < nrs; i += blockDim.x) {
+        res_rr[i] = a.res_rr[i];
+        res_rq[i] = a.res_rq[i];
+    }
+    __syncthreads();
+    s.csr_ptr = csr_ptr; s.csr_jr = csr_jr; s.csr_jq = csr_jq; s.csr_row = csr_row; s.indices = indices;
+    s.csr_const = csr_const; s.csr_diag = csr_diag; s.res_ptr = res_ptr; s.res_rr = res_rr; s.res_rq = res_rq;
+}
+
 __global__ void __launch_bounds__(BATCH_THREADS, 1) batch_kernel(BatchArgs a) {
     const int lane = threadIdx.x & 31;
+    // the replica step reads the gather lists from this CTA's shared memory when they are staged
+    BatchArgs ra = a;
+    if (a.stage) stage_pattern(a, ra);
     const int warps = blockDim.x >> 5;
     // replicas dealt round-robin over the CTAs, like the evaluation warps
     const int gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
@@ -840,7 +962,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, 1) batch_kernel(BatchArgs a) {
         const long long c2 = clock64();
         int mine = 0;
         for (int r = gw; r < a.n_rep; r += nw) {
-            replica_tick(a, r, lane);
+            replica_tick(ra, r, lane);
             __syncwarp();
             mine += a.rep[r].state != RS_DONE;
         }
@@ -1108,7 +1230,8 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     int sms = 0, per_sm = 0, smem_optin = 0;
     VGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     VGB_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t ws_bytes = sizeof(double) * ws_doubles(n, nu) * (BATCH_THREADS / 32);
+    const size_t ws_bytes = sizeof(double) *
+                            ws_doubles(n, nu, ws_scratch((int)b.d_csr_jr.n, (int)b.d_res_rr.n)) * (BATCH_THREADS / 32);
     const long long coop_stride = 32LL * VGB_COOP_SLOTS_MAX;
     const size_t coop_bytes = sizeof(double) * coop_stride * (BATCH_THREADS / 32 / COOP_WARPS);
     // FP64 issue on GB300 is an SM-wide budget (about one warp-instruction per
@@ -1245,8 +1368,15 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     a.n_coop_units = b.n_coop_units;
     a.coop_stride = coop_stride;
     // the exchange slots of the evaluation phase and the per-warp workspaces of
-    // the replica phase share the dynamic shared memory (grid barriers between)
-    const size_t smem = std::max(ws_bytes, b.n_coop_units ? coop_bytes : (size_t)0);
+    // the replica phase share the dynamic shared memory (grid barriers between);
+    // the staged gather lists follow, for the whole launch
+    const size_t phase_bytes = (std::max(ws_bytes, b.n_coop_units ? coop_bytes : (size_t)0) + 15) & ~(size_t)15;
+    a.n_csr_src = (int)b.d_csr_jr.n;
+    a.n_res_src = (int)b.d_res_rr.n;
+    const size_t sbytes = stage_bytes(c.nnz, a.n_csr_src, std::max(nu, 0), a.n_res_src);
+    a.stage = (sbytes <= 48 * 1024 && phase_bytes + sbytes <= (size_t)smem_optin) ? 1 : 0;
+    a.stage_off = (long long)phase_bytes;
+    const size_t smem = phase_bytes + (a.stage ? sbytes : 0);
     VGB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BATCH_THREADS, smem));
     batch_require(per_sm >= 1, "batched transient: the kernel does not fit on an SM");
