@@ -293,15 +293,15 @@ int vgb_tran_destroy(void* session);
  *                I_out [n_rep][max_steps][max(n_vsrc,1)], stats [n_rep][8] =
  *                {n_steps, rejected, total_nr_iters, min_dt_used, max_dt_used,
  *                device_ms, nr_failures, pivot_failures}.
- *   set_coop:    allow (default) or forbid the cooperative evaluation:
+ *   set_coop:    0 forbids, 1 (default) allows, 2 forces the cooperative evaluation:
  *                the models that carry a generated several-warp body (EKV)
- *                are evaluated by groups of four warps that split each
+ *                are evaluated by groups of eight warps that split each
  *                instance's dataflow graph and exchange values through
  *                shared memory, with the body's parameter-only part computed
- *                once per run into a per-instance cache.  Used when the
- *                batch has no more such item warps than the GPU has SMs
- *                (beyond that, one warp per 32 items keeps the SMs' FP64
- *                issue fuller).  Results agree with the one-warp evaluation
+ *                once per run into a per-instance cache.  Allowed, it is
+ *                used when the batch has no more such item warps than the
+ *                GPU has SMs (beyond that, one warp per 32 items keeps the
+ *                SMs' FP64 issue fuller); forced, always.  Results agree with the one-warp evaluation
  *                to the last bits (multiply-adds are fused differently).
  *   info:        out[17] = {device ms of the last run, ticks, evaluation items,
  *                contribution slots per replica, then SM clock cycles summed

@@ -76,7 +76,7 @@ def test_batched_ring_all_20000_steps_match_oracle(cuda):
     cfg = G.tran_cfg(rc, True, M.RING_STEPS * 1e-12, 1e-12, M.RING_STEPS + 1)
     out = bt.transient(cfg, fx["X0"][None, :])
     bt.close()
-    assert out["coop_units"] >= 1  # the EKV devices went through the four-warp evaluation
+    assert out["coop_units"] >= 1  # the EKV devices went through the cooperative evaluation
     assert int(out["n_steps"][0]) == M.RING_STEPS + 1
     assert int(out["total_nr_iters"][0]) == int(fx["total_nr_iters"])
     np.testing.assert_allclose(out["times"][0][fx["rows"]], fx["times"], rtol=0, atol=1e-20)
@@ -86,7 +86,7 @@ def test_batched_ring_all_20000_steps_match_oracle(cuda):
 
 @pytest.mark.gpu
 def test_cooperative_evaluation_matches_single_warp(cuda):
-    """96 ring corners (adaptive gear2, 0.4 ns) with the four-warp model
+    """96 ring corners (adaptive gear2, 0.4 ns) with the cooperative model
     evaluation and with one warp per item: the same steps, rejections and
     Newton iterations in every replica, step times within 1e-9 relative and
     node voltages within 1e-9 V (a multiply-add split between warps is not

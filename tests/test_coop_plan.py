@@ -1,4 +1,4 @@
-"""The cooperative (four-warp) model evaluation plan, checked on the CPU.
+"""The cooperative (several-warp) model evaluation plan, checked on the CPU.
 
 codegen/coop.py splits a model body over the warps of a group, which
 exchange values through shared-memory slots between named barriers.  These
@@ -195,17 +195,17 @@ def test_plan_covers_every_output_once(name):
 
 
 def test_plan_balance_and_size():
-    """EKV: the four parts within 50 % of each other, the modelled span under
+    """EKV: the parts within a factor of two of each other, the modelled span under
     half the single-warp work (the model charges every cross-warp value the
     measured-best 24 units), fewer than 100 barriers, the exchange area within
-    a CTA's shared memory for two groups, the parameter-only part hoisted."""
+    a CTA's shared memory, the parameter-only part hoisted."""
     plan = CoopPlan(_model("ekv"))
     info = plan.info()
-    assert max(info["per_warp"]) < 1.5 * min(info["per_warp"])
+    assert max(info["per_warp"]) < 2.0 * min(info["per_warp"])
     assert info["hoisted_work"] > 0.1 * (info["work"] + info["hoisted_work"])
     assert info["makespan"] < 0.5 * info["work"]
     assert info["barriers"] < 100
-    assert 2 * plan.n_slots * 32 * 8 <= 227 * 1024
+    assert plan.n_slots * 32 * 8 <= 227 * 1024
 
 
 def test_small_models_stay_single_warp():

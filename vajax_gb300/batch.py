@@ -57,7 +57,7 @@ class BatchedTransient:
     """All replicas in one run.  ``replicas`` are resolved circuits of one
     pattern (``same_pattern``); the first is the template."""
 
-    def __init__(self, replicas: Sequence[ResolvedCircuit], gmin: float = 1e-12, coop: bool = True):
+    def __init__(self, replicas: Sequence[ResolvedCircuit], gmin: float = 1e-12, coop=True):
         if not replicas:
             raise ValueError("no replicas")
         tpl = replicas[0]
@@ -77,9 +77,10 @@ class BatchedTransient:
         self.h = h
         self._keep = []
         try:
-            # cooperative evaluation: four warps share each instance of a model that has a generated
-            # several-warp body (results agree with coop=False to the last bits)
-            self._check(self.lib.vgb_batch_set_coop(self.h, int(bool(coop))))
+            # cooperative evaluation: eight warps share each instance of a model that has a generated
+            # several-warp body (results agree with coop=False to the last bits); True lets the
+            # engine use it when it pays, False forbids it, "force" always uses it
+            self._check(self.lib.vgb_batch_set_coop(self.h, 2 if coop == "force" else int(bool(coop))))
             self._set_params()
             self._set_sources()
         except Exception:

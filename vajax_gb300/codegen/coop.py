@@ -5,8 +5,8 @@ sub-partitions, whatever the number of active lanes.  A model evaluated by
 one warp therefore takes (FP64 instructions x 64) cycles even when only one
 lane has an instance to evaluate, which is what bounds small batches (one
 ring oscillator, a few hundred corners).  The EKV body holds ~5,000 FP64
-instructions but its longest dependent chain is ~370, so four warps -- one
-per sub-partition -- can share one evaluation.
+instructions but its longest dependent chain is ~370, so several warps --
+eight, two per sub-partition, measured fastest -- can share one evaluation.
 
 The emitter partitions the MIR dataflow graph over ``W`` warps:
 
@@ -57,7 +57,7 @@ from typing import Dict, List, Tuple
 
 from vajax_gb300.codegen.cuda import MirProgram
 
-W_DEFAULT = 4
+W_DEFAULT = 8  # two warps per SM sub-partition: measured 104.7 k cycles per EKV evaluation against 128.6 k with four
 # cost of handing a value to another warp, FP64-instruction units (64 cycles):
 # a store, a named barrier and a load take about 190 cycles on GB300, and the
 # segments' real durations drift from the modelled ones, so every barrier

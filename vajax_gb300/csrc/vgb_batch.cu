@@ -47,7 +47,7 @@ constexpr int BATCH_MAX_N = 48;       // n_aug limit: each warp's dense system l
 constexpr int BATCH_THREADS = 256;
 constexpr int BATCH_MAX_GROUPS = 16;
 constexpr unsigned BARRIER_POLLS = 1u << 26;
-constexpr int COOP_WARPS = 4;  // warps that share one cooperative evaluation: one per SM sub-partition
+constexpr int COOP_WARPS = 8;  // warps that share one cooperative evaluation: the whole CTA, two per SM sub-partition
 
 // Replica states between ticks: INIT (uic start: charges from the evaluation
 // at X0), START (given initial state: step 1 from X0), NR (a Newton
@@ -250,6 +250,8 @@ __global__ void __launch_bounds__(128) batch_cache_kernel(BGroup g, int n_rep) {
 template <class M>
 __device__ __noinline__ void eval_coop_item(const BatchArgs& a, const BGroup& g, int d, int r, bool act, int w,
                                             vgb_xs_t xs, int bar) {
+    // every warp of the group runs one part, and every part passes the group's barriers
+    static_assert(M::COOP_W == COOP_WARPS, "the model's cooperative body is split for another group size");
     double V[M::NN];
 #pragma unroll
     for (int t = 0; t < M::NN; ++t)
@@ -264,8 +266,8 @@ __device__ __noinline__ void eval_coop_item(const BatchArgs& a, const BGroup& g,
 // Item warps (32 consecutive items: one device of 32 consecutive replicas)
 // are dealt round-robin over the CTAs, so every SM holds as few evaluation
 // warps as the batch allows.  Item warps of a model with a cooperative body
-// go to groups of COOP_WARPS warps (two per CTA, one warp per sub-partition
-// each), dealt round-robin over the CTAs first; the rest to single warps.
+// go to groups of COOP_WARPS warps (the whole CTA, two warps per SM
+// sub-partition), dealt round-robin over the CTAs; the rest to single warps.
 __device__ void eval_phase(const BatchArgs& a) {
     const int lane = threadIdx.x & 31;
     if (a.n_coop_units) {
@@ -1042,7 +1044,7 @@ struct Batch {
     std::vector<DevBuf<int>> d_node_map, d_vidx;
     std::vector<DevBuf<double>> d_shared, d_varying, d_temps, d_cache;
     long long n_contrib = 0, n_items = 0, n_coop_units = 0;
-    bool coop = true;  // cooperative evaluation of the models that have one
+    int coop = 1;  // cooperative evaluation: 0 never, 1 when its item warps fit one per SM, 2 always
     double run_ms = 0.0;
     long long ticks = 0;
     long long phase_cycles[12] = {0};
@@ -1236,13 +1238,13 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     const size_t coop_bytes = sizeof(double) * coop_stride * (BATCH_THREADS / 32 / COOP_WARPS);
     // FP64 issue on GB300 is an SM-wide budget (about one warp-instruction per
     // 19 cycles) that one warp can use only a third of (one per 64 cycles):
-    // four warps sharing an instance finish it 1.7x sooner than one warp, but
+    // eight warps sharing an instance finish it 2.5x sooner than one warp, but
     // the if-converted body holds more instructions, so the cooperative
     // evaluation pays only while no SM holds more than one group's work.
     long long units = 0;
     for (const BGroup& B : b.groups)
         if (model_has_coop(B.model)) units += ((long long)B.n_dev * R + 31) / 32;
-    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin && units <= sms;
+    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin && (units <= sms || b.coop == 2);
     b.n_coop_units = 0;
     b.d_cache.resize(c.groups.size());
     for (size_t g = 0; g < c.groups.size(); ++g) {
@@ -1532,7 +1534,11 @@ int vgb_batch_transient(void* bh, const double* cfg, const double* X0, const dou
 int vgb_batch_set_coop(void* bh, int enable) {
     Batch* b = static_cast<Batch*>(bh);
     if (!b) return VGB_ERR_INVALID;
-    b->coop = enable != 0;
+    if (enable < 0 || enable > 2) {
+        b->last_error = "vgb_batch_set_coop: 0 (never), 1 (when it fits one group per SM) or 2 (always)";
+        return VGB_ERR_INVALID;
+    }
+    b->coop = enable;
     return VGB_OK;
 }
 
