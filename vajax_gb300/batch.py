@@ -142,6 +142,7 @@ class BatchedTransient:
         return {"times": times, "V": V, "I": I, "n_steps": stats[:, 0].astype(np.int64),
                 "rejected": stats[:, 1].astype(np.int64), "total_nr_iters": stats[:, 2].astype(np.int64),
                 "nr_failures": stats[:, 6].astype(np.int64), "pivot_failures": stats[:, 7].astype(np.int64),
+                "min_dt_used": stats[:, 3].copy(), "max_dt_used": stats[:, 4].copy(),
                 "device_ms": float(info[0]), "ticks": int(info[1]), "coop_units": int(info[12]),
                 "phase_cycles": dict(zip(("eval", "barrier1", "replica", "barrier2", "r0_assemble", "r0_lu",
                                           "r0_update", "r0_finish_plan", "r0_assemble_jacobian",

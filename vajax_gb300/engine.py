@@ -344,13 +344,37 @@ class CircuitEngine:
                     method=METHODS[str(cfg.integration_method).lower()], n_external=self.rc.n_external,
                     max_steps=self.max_steps, tran_itl=self.options.tran_itl)
 
+    def _transient_batched(self, cfg, X0, Q0, I0, maxc0):
+        """A circuit small enough for the batched engine (FP64 LU, at most 48
+        unknowns, no NOI nodes) runs there as one replica: the same transient
+        loop, step for step and Newton iteration for Newton iteration, with
+        the device evaluation split over a CTA's warps instead of one warp.
+        None when the circuit does not fit."""
+        from vajax_gb300.batch import BatchedTransient, fits
+        if self.precision != "fp64" or not fits(self.rc):
+            return None
+        bt = BatchedTransient([self.rc], gmin=self.options.gmin)
+        try:
+            o = bt.transient(cfg, X0[None, :], None if Q0 is None else np.asarray(Q0)[None, :],
+                             None if I0 is None else np.asarray(I0)[None, :],
+                             None if maxc0 is None else np.asarray(maxc0)[None, :])
+        finally:
+            bt.close()
+        n = int(o["n_steps"][0])
+        return {"times": o["times"][0][:n], "V": o["V"][0][:n], "I": o["I"][0][:n], "n_steps": n,
+                "rejected": int(o["rejected"][0]), "total_nr_iters": int(o["total_nr_iters"][0]),
+                "min_dt_used": float(o["min_dt_used"][0]), "max_dt_used": float(o["max_dt_used"][0]),
+                "device_ms": o["device_ms"], "nr_failures": int(o["nr_failures"][0]), "engine": "batched"}
+
     def run_transient(self) -> TransientResult:
         if not self._prepared:
             raise RuntimeError("call prepare(t_stop=..., dt=...) first")
         X0, Q0, I0, maxc0, dc_conv = self.initial_state()
         cfg = self.transient_cfg()
         t0 = time.perf_counter()
-        out = self.device.transient(cfg, X0, Q0, I0, maxc0)
+        out = self._transient_batched(cfg, X0, Q0, I0, maxc0)
+        if out is None:
+            out = self.device.transient(cfg, X0, Q0, I0, maxc0)
         wall = time.perf_counter() - t0
         rc = self.rc
         n = out["n_steps"]
@@ -364,7 +388,8 @@ class CircuitEngine:
                      min_dt_used=out["min_dt_used"], max_dt_used=out["max_dt_used"],
                      nr_failures=out["nr_failures"], dc_converged=dc_conv,
                      strategy="fixed_step_full_mna" if cfg["fixed_step"] else "adaptive_full_mna",
-                     solver=f"gb300-sparse-{self.precision}", X0=X0)
+                     solver="gb300-batched-dense-fp64" if out.get("engine") == "batched"
+                     else f"gb300-sparse-{self.precision}", X0=X0)
         return TransientResult(times=out["times"], voltages=voltages, currents=currents, stats=stats)
 
 
