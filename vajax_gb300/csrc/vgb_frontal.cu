@@ -98,7 +98,7 @@ struct MFArgs {
     unsigned spin_limit;
 };
 
-constexpr int MF_THREADS = 128;
+constexpr int MF_THREADS = 256;  // tree-solve CTAs: eight warps (measured 1.02 ms against 1.28 with four on the 80k network)
 constexpr int LD = FRONT_TILE_LD;
 constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
 // shared memory of a factorisation CTA: one small front, or three tiles
@@ -869,10 +869,12 @@ void mf_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
     else mf_factor_t<double>(c, A, c.lu.d_pool64.p, s);
 }
 
-// bwd: z and x_tail (m) plus the partial sums of U12 x_tail (at most max(4 w, 128) <= 4 m + 128)
+// bwd: z and x_tail (m) plus the partial sums of U12 x_tail ([G][w] with G = MF_THREADS / P
+// groups of P lanes, P >= min(w, 32): at most (MF_THREADS / 32) w + MF_THREADS <= (MF_THREADS / 32) m
+// + MF_THREADS); fwd uses m
 template <typename T>
 static size_t mf_solve_smem(const SparseLU& L) {
-    return (size_t)(5 * std::max<long long>(L.mf_max_m, 1) + MF_THREADS) * sizeof(T);
+    return (size_t)((1 + MF_THREADS / 32) * std::max<long long>(L.mf_max_m, 1) + MF_THREADS) * sizeof(T);
 }
 
 // Opt the solve kernels in to more than 48 KB of dynamic shared memory (once per size).
