@@ -98,7 +98,7 @@ struct MFArgs {
     unsigned spin_limit;
 };
 
-constexpr int MF_THREADS = 256;  // tree-solve CTAs: eight warps (measured 1.02 ms against 1.28 with four on the 80k network)
+constexpr int MF_THREADS = 512;  // tree-solve CTAs: 16 warps (80k network: 0.92 ms per solve pair, 1.02 with 8 warps, 1.28 with 4)
 constexpr int LD = FRONT_TILE_LD;
 constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
 // shared memory of a factorisation CTA: one small front, or three tiles
