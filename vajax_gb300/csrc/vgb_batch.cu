@@ -32,6 +32,7 @@
 // barriers by a poll limit that sets an error flag and stops the kernel.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -93,6 +94,8 @@ struct BatchArgs {
     // (when they fit): counts and the byte offset of the staged area
     int n_csr_src, n_res_src, stage;
     long long stage_off;
+    // doubles of gather scratch in each warp's workspace (0: gather from global)
+    int ws_sc;
     double gmin, reltol, abstol, vntol, damping;
     const BGroup* groups;
     // pattern and gather lists (one replica)
@@ -361,7 +364,7 @@ __host__ __device__ inline size_t ws_doubles(int n_aug, int n_unk, int scratch) 
 __device__ __forceinline__ WarpWS warp_ws(const BatchArgs& a) {
     extern __shared__ double batch_smem[];
     const size_t n = a.n_aug, nu = a.n_unk > 0 ? a.n_unk : 1;
-    const int sc = ws_scratch(a.n_csr_src, a.n_res_src);
+    const int sc = a.ws_sc;
     double* base = batch_smem + (threadIdx.x >> 5) * ws_doubles(a.n_aug, a.n_unk, sc);
     double* rep = base + n * n + n + 3 * nu;
     return WarpWS{base, base + n * n, base + n * n + n, base + n * n + n + nu, base + n * n + n + 2 * nu,
@@ -1054,6 +1057,28 @@ static void batch_require(bool ok, const std::string& m) {
     if (!ok) throw Error(VGB_ERR_INVALID, m);
 }
 
+// The dynamic shared memory a batch launch may take beside the kernel's static
+// shared memory.  The kernel's maximum is raised to that bound once per
+// device and never lowered: batches sized differently run from several host
+// threads, and a per-launch setting could shrink the limit between another
+// thread's setting and its launch.
+static size_t batch_smem_limit(int smem_optin) {
+    static std::mutex mu;
+    static std::vector<size_t> done;
+    int dev = 0;
+    VGB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (!done[dev]) {
+        cudaFuncAttributes fa{};
+        VGB_CUDA(cudaFuncGetAttributes(&fa, batch_kernel));
+        const size_t lim = (size_t)smem_optin > fa.sharedSizeBytes ? (size_t)smem_optin - fa.sharedSizeBytes : 0;
+        VGB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim));
+        done[dev] = lim;
+    }
+    return done[dev];
+}
+
 // Host-side set-up: checks, the gather lists mapped onto the batch
 // contribution layout, per-replica parameters from the template.  Uploads
 // nothing (batch_run does), so the checks run without a GPU.
@@ -1232,8 +1257,13 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     int sms = 0, per_sm = 0, smem_optin = 0;
     VGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     VGB_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t ws_bytes = sizeof(double) *
-                            ws_doubles(n, nu, ws_scratch((int)b.d_csr_jr.n, (int)b.d_res_rr.n)) * (BATCH_THREADS / 32);
+    // dynamic shared memory left beside the kernel's static shared memory
+    const size_t smem_limit = batch_smem_limit(smem_optin);
+    // per-warp gather scratch only when the workspaces still fit with it
+    int ws_sc = ws_scratch((int)b.d_csr_jr.n, (int)b.d_res_rr.n);
+    if (sizeof(double) * ws_doubles(n, nu, ws_sc) * (BATCH_THREADS / 32) > smem_limit) ws_sc = 0;
+    const size_t ws_bytes = sizeof(double) * ws_doubles(n, nu, ws_sc) * (BATCH_THREADS / 32);
+    batch_require(ws_bytes <= smem_limit, "batched transient: the circuit's dense Newton matrix does not fit in shared memory");
     const long long coop_stride = 32LL * VGB_COOP_SLOTS_MAX;
     const size_t coop_bytes = sizeof(double) * coop_stride * (BATCH_THREADS / 32 / COOP_WARPS);
     // FP64 issue on GB300 is an SM-wide budget (about one warp-instruction per
@@ -1244,7 +1274,7 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     long long units = 0;
     for (const BGroup& B : b.groups)
         if (model_has_coop(B.model)) units += ((long long)B.n_dev * R + 31) / 32;
-    const bool coop = b.coop && coop_bytes <= (size_t)smem_optin && (units <= sms || b.coop == 2);
+    const bool coop = b.coop && coop_bytes <= smem_limit && (units <= sms || b.coop == 2);
     b.n_coop_units = 0;
     b.d_cache.resize(c.groups.size());
     for (size_t g = 0; g < c.groups.size(); ++g) {
@@ -1376,10 +1406,10 @@ static void batch_run(Batch& b, const double* cfg, const double* X0, const doubl
     a.n_csr_src = (int)b.d_csr_jr.n;
     a.n_res_src = (int)b.d_res_rr.n;
     const size_t sbytes = stage_bytes(c.nnz, a.n_csr_src, std::max(nu, 0), a.n_res_src);
-    a.stage = (sbytes <= 48 * 1024 && phase_bytes + sbytes <= (size_t)smem_optin) ? 1 : 0;
+    a.ws_sc = ws_sc;
+    a.stage = (sbytes <= 48 * 1024 && phase_bytes + sbytes <= smem_limit) ? 1 : 0;
     a.stage_off = (long long)phase_bytes;
     const size_t smem = phase_bytes + (a.stage ? sbytes : 0);
-    VGB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BATCH_THREADS, smem));
     batch_require(per_sm >= 1, "batched transient: the kernel does not fit on an SM");
     // about two warps of work per CTA, at most one CTA per SM (a cooperative launch)
