@@ -139,6 +139,26 @@ int vgb_solver_info(void* h, int64_t* out);
  * (vajax/sparse/umfpack_ffi.cpp:140-185). */
 int vgb_solver_order(void* h, int* perm_r, int* order);
 
+/* Weighted matching and scaling for the static-pivot LU, computed from the
+ * Jacobian values csr_vals (host, nnz; e.g. those at the start of a DC
+ * solve): the row permutation of maximum diagonal product (the MC64 method of
+ * Duff and Koster) replaces the voltage-source transversal, and the
+ * factorised block is scaled so that its diagonal entries have magnitude 1
+ * and no entry exceeds 1.  Re-runs the ordering, symbolic factorisation and
+ * task schedule, and reallocates the front storage; call it with no transient
+ * session open.  csr_vals NULL restores the transversal without scaling.
+ * VGB_ERR_NUMERIC when no perfect matching exists on the nonzero values.
+ * Takes the place of the pivoting that the reference's UMFPACK path does
+ * during its numeric factorisation (vajax/sparse/umfpack_ffi.cpp:153, pivot
+ * tolerance 0.1), which a static-pivot factorisation cannot do. */
+int vgb_solver_match(void* h, const double* csr_vals);
+
+/* The same matching on a host CSR matrix (no circuit, no GPU): perm_r[n]
+ * (row r of the permuted matrix is row perm_r[r]), rscale[n] by row and
+ * cscale[n] by column (either may be NULL). */
+int vgb_weighted_matching(int n, const int* indptr, const int* indices, const double* vals, int* perm_r,
+                          double* rscale, double* cscale);
+
 /* Per-phase device timing of the Newton loop (CUDA events on the handle's
  * stream).  mode 1 enables and resets, 0 disables and resets, -1 only reads.
  * out[7] (may be NULL) = {eval_ms, assemble_ms, factor_ms, solve_ms,

@@ -47,6 +47,8 @@ SIGNATURES = {
     "vgb_circuit_analyze": (C.c_int, [vp]),
     "vgb_profile": (C.c_int, [vp, C.c_int, f64p]),
     "vgb_solver_order": (C.c_int, [vp, i32p, i32p]),
+    "vgb_solver_match": (C.c_int, [vp, f64p]),
+    "vgb_weighted_matching": (C.c_int, [C.c_int, i32p, i32p, f64p, i32p, f64p, f64p]),
     "vgb_solver_info": (C.c_int, [vp, i64p]),
     "vgb_circuit_finalize": (C.c_int, [vp, C.c_double, C.c_int, C.c_int]),
     "vgb_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),

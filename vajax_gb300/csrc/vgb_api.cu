@@ -63,6 +63,84 @@ static void ensure_pools(Circuit& c, int precision) {
     }
 }
 
+// Device copies of the sparse LU's host structures (after an analysis, or a
+// re-analysis with a new row permutation), the front pools of the current
+// precision and the scaling of a weighted matching.
+static void upload_lu(Circuit& c, int precision) {
+    SparseLU& L = c.lu;
+    std::vector<int> brow(std::max(L.nM, 1), 0);
+    for (int i = 0; i < L.nM; ++i) brow[i] = L.perm_r[L.q[i]];
+    L.d_brow.upload(brow);
+    L.d_q.upload(L.q.empty() ? std::vector<int>{0} : L.q);
+    auto up = [](DevBuf<int>& d, const std::vector<int>& h) { d.upload(h.empty() ? std::vector<int>{0} : h); };
+    up(L.d_f_col, L.f_col);
+    up(L.d_f_arow, L.f_arow);
+    up(L.d_f_diag_e, L.f_diag_e);
+    up(L.d_l_col, L.l_col);
+    up(L.d_l_arow, L.l_arow);
+    up(L.d_l_diag_e, L.l_diag_e);
+    up(L.d_l_ptr, L.l_ptr);
+    up(L.d_l_e, L.l_e);
+    up(L.d_l_x, L.l_x);
+    up(L.d_pre_ptr, L.pre_ptr);
+    up(L.d_pre_e, L.pre_e);
+    up(L.d_pre_f, L.pre_f);
+    // multifrontal structure
+    auto up64 = [](DevBuf<long long>& d, const std::vector<long long>& h) {
+        d.upload(h.empty() ? std::vector<long long>{0} : h);
+    };
+    up64(L.d_fr_ptr, L.fr_ptr);
+    up64(L.d_fr_off, L.fr_off);
+    up64(L.d_em_ptr, L.em_ptr);
+    up64(L.d_asm_ptr, L.asm_ptr);
+    up64(L.d_cv_off, L.fr_cv_off);
+    up64(L.d_tasm_ptr, L.tasm_ptr);
+    up64(L.d_tch_ptr, L.tch_ptr);
+    up64(L.d_fg_ptr, L.fg_ptr);
+    up(L.d_fwd_order, L.fwd_order);
+    up(L.d_bwd_order, L.bwd_order);
+    up64(L.d_fg_src, L.fg_src);
+    up(L.d_fr_idx, L.fr_idx);
+    up(L.d_fr_w, L.fr_w);
+    up(L.d_sn_parent, L.sn_parent);
+    up(L.d_ch_ptr, L.ch_ptr);
+    up(L.d_ch_idx, L.ch_idx);
+    up(L.d_em_idx, L.em_idx);
+    up(L.d_asm_e, L.asm_e);
+    up(L.d_asm_pos, L.asm_pos);
+    up(L.d_task_type, L.task_type);
+    up(L.d_task_front, L.task_front);
+    up(L.d_task_i, L.task_i);
+    up(L.d_task_j, L.task_j);
+    up(L.d_task_k, L.task_k);
+    up(L.d_fr_big, L.fr_big);
+    up(L.d_fr_kb, L.fr_kb);
+    up(L.d_fr_nb, L.fr_nb);
+    up(L.d_fr_tile0, L.fr_tile0);
+    up(L.d_tasm_e, L.tasm_e);
+    up(L.d_tasm_pos, L.tasm_pos);
+    up(L.d_tch, L.tch);
+    L.d_tver.alloc(std::max<long long>(L.n_tiles, 1));
+    ensure_pools(c, precision);
+    L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
+    L.d_mf_flags.zero(c.stream);
+    L.d_mf_count.alloc(std::max(L.nsn, 1));
+    L.d_counters.alloc(8);
+    L.d_slot_scale.release();
+    L.d_scaled.release();
+    L.d_rscale.release();
+    L.d_cscale.release();
+    if (!L.rscale.empty()) {
+        std::vector<double> slot(std::max(c.nnz, 1), 1.0);
+        for (int r = 0; r < c.n_aug; ++r)
+            for (int e = c.indptr[r]; e < c.indptr[r + 1]; ++e) slot[e] = L.rscale[r] * L.cscale[c.indices[e]];
+        L.d_slot_scale.upload(slot);
+        L.d_scaled.alloc(std::max(c.nnz, 1));
+        L.d_rscale.upload(L.rscale);
+        L.d_cscale.upload(L.cscale);
+    }
+}
+
 static void require_analyzed(Circuit* c) {
     if (!c->analyzed) throw Error(VGB_ERR_STATE, "circuit is not analyzed (call vgb_circuit_analyze)");
 }
@@ -427,6 +505,64 @@ int vgb_solver_info(void* h, int64_t* out) {
     });
 }
 
+int vgb_weighted_matching(int n, const int* indptr, const int* indices, const double* vals, int* perm_r,
+                          double* rscale, double* cscale) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        VGB_REQUIRE(n >= 0, "n must be >= 0");
+        VGB_REQUIRE(n == 0 || (indptr && indices && vals && perm_r), "indptr, indices, vals and perm_r are required");
+        if (n == 0) return;
+        for (int r = 0; r < n; ++r) VGB_REQUIRE(indptr[r] <= indptr[r + 1], "indptr must be non-decreasing");
+        VGB_REQUIRE(indptr[0] == 0, "indptr[0] must be 0");
+        for (int e = 0; e < indptr[n]; ++e) VGB_REQUIRE(indices[e] >= 0 && indices[e] < n, "column index out of range");
+        std::vector<int> p;
+        std::vector<double> rs, cs;
+        std::string why;
+        if (!weighted_matching(n, indptr, indices, vals, p, rs, cs, why)) throw Error(VGB_ERR_NUMERIC, why);
+        std::memcpy(perm_r, p.data(), n * sizeof(int));
+        if (rscale) std::memcpy(rscale, rs.data(), n * sizeof(double));
+        if (cscale) std::memcpy(cscale, cs.data(), n * sizeof(double));
+    });
+}
+
+int vgb_solver_match(void* h, const double* csr_vals) {
+    Circuit* c = nullptr;
+    return guarded(c, [&] {
+        c = as_circuit(h);
+        require_final(c);
+        SparseLU& L = c->lu;
+        if (csr_vals) {
+            std::vector<int> p;
+            std::vector<double> rs, cs;
+            std::string why;
+            if (!weighted_matching(c->n_aug, c->indptr.data(), c->indices.data(), csr_vals, p, rs, cs, why))
+                throw Error(VGB_ERR_NUMERIC, "weighted matching: " + why);
+            L.match_r = std::move(p);
+            L.rscale = std::move(rs);
+            L.cscale = std::move(cs);
+        } else {
+            if (L.match_r.empty()) return;
+            L.match_r.clear();
+            L.rscale.clear();
+            L.cscale.clear();
+        }
+        // new row permutation: ordering, symbolic factorisation, schedule and
+        // device structures again; front pools re-sized for the new fronts
+        VGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->config_epoch++;
+        build_sparse_symbolic(*c);
+        const bool had32 = L.d_pool32.p != nullptr, had64 = L.d_pool64.p != nullptr;
+        L.d_pool32.release();
+        L.d_cv32.release();
+        L.d_pool64.release();
+        L.d_cv64.release();
+        upload_lu(*c, c->solver_kind);
+        if (had32) ensure_pools(*c, 1);
+        if (had64) ensure_pools(*c, 0);
+        VGB_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
 int vgb_solver_order(void* h, int* perm_r, int* order) {
     Circuit* c = nullptr;
     return guarded(c, [&] {
@@ -565,67 +701,7 @@ int vgb_circuit_finalize(void* h, double gmin, int precision, int refine_sweeps)
             s->d_cnt.upload(s->cnt);
             s->d_data.upload(s->data);
         }
-        SparseLU& L = c->lu;
-        std::vector<int> brow(std::max(L.nM, 1), 0);
-        for (int i = 0; i < L.nM; ++i) brow[i] = L.perm_r[L.q[i]];
-        L.d_brow.upload(brow);
-        L.d_q.upload(L.q.empty() ? std::vector<int>{0} : L.q);
-        auto up = [](DevBuf<int>& d, const std::vector<int>& h) { d.upload(h.empty() ? std::vector<int>{0} : h); };
-        up(L.d_f_col, L.f_col);
-        up(L.d_f_arow, L.f_arow);
-        up(L.d_f_diag_e, L.f_diag_e);
-        up(L.d_l_col, L.l_col);
-        up(L.d_l_arow, L.l_arow);
-        up(L.d_l_diag_e, L.l_diag_e);
-        up(L.d_l_ptr, L.l_ptr);
-        up(L.d_l_e, L.l_e);
-        up(L.d_l_x, L.l_x);
-        up(L.d_pre_ptr, L.pre_ptr);
-        up(L.d_pre_e, L.pre_e);
-        up(L.d_pre_f, L.pre_f);
-        // multifrontal structure
-        auto up64 = [](DevBuf<long long>& d, const std::vector<long long>& h) {
-            d.upload(h.empty() ? std::vector<long long>{0} : h);
-        };
-        up64(L.d_fr_ptr, L.fr_ptr);
-        up64(L.d_fr_off, L.fr_off);
-        up64(L.d_em_ptr, L.em_ptr);
-        up64(L.d_asm_ptr, L.asm_ptr);
-        up64(L.d_cv_off, L.fr_cv_off);
-        up64(L.d_tasm_ptr, L.tasm_ptr);
-        up64(L.d_tch_ptr, L.tch_ptr);
-        up64(L.d_fg_ptr, L.fg_ptr);
-        up(L.d_fwd_order, L.fwd_order);
-        up(L.d_bwd_order, L.bwd_order);
-        up64(L.d_fg_src, L.fg_src);
-        up(L.d_fr_idx, L.fr_idx);
-        up(L.d_fr_w, L.fr_w);
-        up(L.d_sn_parent, L.sn_parent);
-        up(L.d_ch_ptr, L.ch_ptr);
-        up(L.d_ch_idx, L.ch_idx);
-        up(L.d_em_idx, L.em_idx);
-        up(L.d_asm_e, L.asm_e);
-        up(L.d_asm_pos, L.asm_pos);
-        up(L.d_task_type, L.task_type);
-        up(L.d_task_front, L.task_front);
-        up(L.d_task_i, L.task_i);
-        up(L.d_task_j, L.task_j);
-        up(L.d_task_k, L.task_k);
-        up(L.d_fr_big, L.fr_big);
-        up(L.d_fr_kb, L.fr_kb);
-        up(L.d_fr_nb, L.fr_nb);
-        up(L.d_fr_tile0, L.fr_tile0);
-        up(L.d_tasm_e, L.tasm_e);
-        up(L.d_tasm_pos, L.tasm_pos);
-        up(L.d_tch, L.tch);
-        L.d_tver.alloc(std::max<long long>(L.n_tiles, 1));
-        const long long pool = std::max<long long>(L.fr_off.empty() ? 0 : L.fr_off.back(), 1);
-        const long long cvn = std::max<long long>(L.fr_cv_off.empty() ? 0 : L.fr_cv_off.back(), 1);
-        ensure_pools(*c, precision);
-        L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
-        L.d_mf_flags.zero(c->stream);
-        L.d_mf_count.alloc(std::max(L.nsn, 1));
-        L.d_counters.alloc(8);
+        upload_lu(*c, precision);
         const size_t na = std::max(c->n_aug, 1), nu = std::max(c->n_unk, 1);
         c->d_csr_vals.alloc(std::max(c->nnz, 1));
         c->d_f.alloc(na);

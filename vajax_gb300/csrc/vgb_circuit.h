@@ -105,7 +105,10 @@ enum TaskType : int { TASK_SMALL = 0, TASK_GETRF = 1, TASK_TRSM_L = 2, TASK_TRSM
 struct SparseLU {
     int n = 0;                   // n_aug
     int nM = 0;                  // size of the factorised block M
-    std::vector<int> perm_r;     // row r of B = row perm_r[r] of A (vsource transversal)
+    std::vector<int> perm_r;     // row r of B = row perm_r[r] of A (vsource transversal or match_r)
+    // weighted matching and scaling computed from values (empty: the transversal, no scaling)
+    std::vector<int> match_r;
+    std::vector<double> rscale, cscale;  // by row and by column of A
     std::vector<int> q;          // [nM] block order: C = Q^T B_MM Q, C(i,j) = B(q[i], q[j])
     std::vector<int> qinv;       // [n] B index -> position in M, -1 outside M
     // singletons solved before M (row = diagonal only) and after M (column = diagonal only)
@@ -161,6 +164,8 @@ struct SparseLU {
     DevBuf<int> d_f_col, d_f_arow, d_f_diag_e, d_l_col, d_l_arow, d_l_diag_e, d_l_ptr, d_l_e, d_l_x;
     DevBuf<int> d_pre_ptr, d_pre_e, d_pre_f;
     DevBuf<int> d_counters;  // work counters
+    // scaling of the matching: per CSR slot r_i s_j, the scaled values factorised, r and s
+    DevBuf<double> d_slot_scale, d_scaled, d_rscale, d_cscale;
 };
 
 struct NRStatus {
@@ -254,6 +259,9 @@ struct Circuit {
 // Host-side construction (vgb_host.cpp)
 void build_pattern(Circuit& c);
 void build_sparse_symbolic(Circuit& c);
+// Maximum-product matching with row and column scaling of a CSR matrix (host).
+bool weighted_matching(int n, const int* indptr, const int* indices, const double* vals, std::vector<int>& perm_r,
+                       std::vector<double>& rscale, std::vector<double>& cscale, std::string& why);
 // Streaming multiprocessors of the current device (vgb_frontal.cu).
 int sm_count();
 // Host-side set-up of the factor/solve launches, done before a stream capture.

@@ -527,6 +527,7 @@ struct MFSolveArgs {
     const long long* fg_ptr;   // per front row: children's update entries, in child order
     const long long* fg_src;
     const int* q;          // B index of each permuted M index
+    const double* cscale;  // column scaling of a weighted matching, by B index (null: none)
     const int* order;      // claim order of the fronts
     int n_small;           // fronts solved one per warp: order[0, n_small) forward, order[ns - n_small, ns) backward
     int* flags;            // fwd [ns], bwd [ns]
@@ -603,7 +604,8 @@ __device__ void bwd_small_warp(const MFSolveArgs& a, int S, const T* __restrict_
     }
     if (lane < w) {
         xs[idx[lane]] = z;
-        xout[a.q[idx[lane]]] = (double)z;
+        const int col = a.q[idx[lane]];
+        xout[col] = a.cscale ? (double)z * a.cscale[col] : (double)z;
     }
     __syncwarp();
     if (lane == 0) {
@@ -779,7 +781,8 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
         }
         for (int p = threadIdx.x; p < w; p += blockDim.x) {
             xs[idx[p]] = z[p];
-            xout[a.q[idx[p]]] = (double)z[p];
+            const int col = a.q[idx[p]];
+            xout[col] = a.cscale ? (double)z[p] * a.cscale[col] : (double)z[p];
         }
         publish(bdone + S, a.epoch);
     }
@@ -924,6 +927,7 @@ void mf_solve_t(Circuit& c, const T* rhsM, T* y, T* xs, double* xout, cudaStream
     a.fg_ptr = L.d_fg_ptr.p;
     a.fg_src = L.d_fg_src.p;
     a.q = L.d_q.p;
+    a.cscale = L.d_cscale.p;
     a.n_small = L.n_small_solve;
     a.flags = L.d_mf_flags.p + 2 * (size_t)L.nsn;
     a.counter = L.d_counters.p + 1;

@@ -6,6 +6,7 @@
 //  * ordering and symbolic factorisation for the static-pivot sparse LU.
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <numeric>
 #include <queue>
 #include <unordered_map>
@@ -941,6 +942,140 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
     }
 }
 
+// Maximum-product transversal with scaling: the method of I. S. Duff and
+// J. Koster, "On algorithms for permuting large entries to the diagonal of a
+// sparse matrix", SIAM J. Matrix Anal. Appl. 22(4), 2001 (the MC64 method).
+// With a_j = max_i |a_ij| and the cost c_ij = ln a_j - ln |a_ij| >= 0 on the
+// nonzero entries, a perfect matching of least total cost maximises the
+// product of the matched magnitudes.  It is found by successive shortest
+// augmenting paths (Dijkstra on the reduced costs c_ij - u_i - v_j >= 0 with
+// row duals u and column duals v, equality on matched entries).  The duals
+// give the scaling r_i = exp(u_i), s_j = exp(v_j) / a_j, under which every
+// matched entry has magnitude 1 and no entry exceeds 1.
+//   perm_r[j]: the row matched to column j (row j of P A is row perm_r[j] of A);
+//   rscale[i], cscale[j]: by row and column of A.
+// Entries that are zero at these values are not candidates.  Returns false
+// with a reason when no perfect matching exists on the nonzero entries or a
+// value is not finite.
+bool weighted_matching(int n, const int* indptr, const int* indices, const double* vals, std::vector<int>& perm_r,
+                       std::vector<double>& rscale, std::vector<double>& cscale, std::string& why) {
+    const double INF = std::numeric_limits<double>::infinity();
+    // columns of the nonzero entries, each with its cost
+    std::vector<int> cptr(n + 1, 0);
+    for (int r = 0; r < n; ++r)
+        for (int e = indptr[r]; e < indptr[r + 1]; ++e) {
+            if (!std::isfinite(vals[e])) { why = "a Jacobian value is not finite"; return false; }
+            if (vals[e] != 0.0) cptr[indices[e] + 1]++;
+        }
+    for (int j = 0; j < n; ++j) cptr[j + 1] += cptr[j];
+    std::vector<int> crow(cptr[n]);
+    std::vector<double> ccost(cptr[n]), amax(n, 0.0);
+    {
+        std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+        for (int r = 0; r < n; ++r)
+            for (int e = indptr[r]; e < indptr[r + 1]; ++e)
+                if (vals[e] != 0.0) {
+                    const int j = indices[e];
+                    crow[fill[j]] = r;
+                    ccost[fill[j]++] = std::fabs(vals[e]);
+                    amax[j] = std::max(amax[j], std::fabs(vals[e]));
+                }
+    }
+    for (int j = 0; j < n; ++j) {
+        if (cptr[j] == cptr[j + 1]) { why = "column " + std::to_string(j) + " has no nonzero value"; return false; }
+        const double la = std::log(amax[j]);
+        for (int k = cptr[j]; k < cptr[j + 1]; ++k) ccost[k] = std::max(0.0, la - std::log(ccost[k]));
+    }
+    // initial duals: u_i = least cost of row i, v_j = least reduced cost of column j
+    std::vector<double> u(n, INF), v(n, INF);
+    for (int k = 0; k < cptr[n]; ++k) u[crow[k]] = std::min(u[crow[k]], ccost[k]);
+    for (int i = 0; i < n; ++i)
+        if (u[i] == INF) { why = "row " + std::to_string(i) + " has no nonzero value"; return false; }
+    for (int j = 0; j < n; ++j)
+        for (int k = cptr[j]; k < cptr[j + 1]; ++k) v[j] = std::min(v[j], ccost[k] - u[crow[k]]);
+    auto reduced = [&](int k, int j) { return std::max(0.0, (ccost[k] - u[crow[k]]) - v[j]); };
+    // greedy start on the entries of zero reduced cost
+    std::vector<int> row_of(n, -1), col_of(n, -1);
+    for (int j = 0; j < n; ++j)
+        for (int k = cptr[j]; k < cptr[j + 1]; ++k)
+            if (row_of[crow[k]] < 0 && reduced(k, j) == 0.0) {
+                row_of[crow[k]] = j;
+                col_of[j] = crow[k];
+                break;
+            }
+    // one shortest augmenting path per unmatched column
+    std::vector<double> dist(n, INF), lcol(n, 0.0);
+    std::vector<int> pred(n, -1), touched, scanned_rows, scanned_cols;
+    std::vector<char> final_(n, 0);
+    using Item = std::pair<double, int>;
+    for (int j0 = 0; j0 < n; ++j0) {
+        if (col_of[j0] >= 0) continue;
+        std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+        touched.clear();
+        scanned_rows.clear();
+        scanned_cols.clear();
+        auto relax = [&](int j, double base) {
+            for (int k = cptr[j]; k < cptr[j + 1]; ++k) {
+                const int i = crow[k];
+                if (final_[i]) continue;
+                const double d = base + reduced(k, j);
+                if (d < dist[i]) {
+                    if (dist[i] == INF) touched.push_back(i);
+                    dist[i] = d;
+                    pred[i] = j;
+                    heap.push({d, i});
+                }
+            }
+        };
+        lcol[j0] = 0.0;
+        scanned_cols.push_back(j0);
+        relax(j0, 0.0);
+        int free_row = -1;
+        double D = 0.0;
+        while (!heap.empty()) {
+            const Item it = heap.top();
+            heap.pop();
+            const int i = it.second;
+            if (final_[i] || it.first > dist[i]) continue;
+            final_[i] = 1;
+            scanned_rows.push_back(i);
+            if (row_of[i] < 0) { free_row = i; D = it.first; break; }
+            const int j = row_of[i];
+            lcol[j] = it.first;
+            scanned_cols.push_back(j);
+            relax(j, it.first);
+        }
+        if (free_row < 0) {
+            why = "the Jacobian is structurally singular on its nonzero values (column " + std::to_string(j0) + ")";
+            return false;
+        }
+        // dual update keeps every reduced cost >= 0 and makes the path's costs 0
+        for (int j : scanned_cols) v[j] += D - lcol[j];
+        for (int i : scanned_rows) u[i] -= D - dist[i];
+        // augment along the path
+        for (int i = free_row;;) {
+            const int j = pred[i];
+            const int prev = col_of[j];
+            col_of[j] = i;
+            row_of[i] = j;
+            if (j == j0) break;
+            i = prev;
+        }
+        for (int i : touched) { dist[i] = INF; final_[i] = 0; }
+    }
+    perm_r.assign(col_of.begin(), col_of.end());
+    rscale.resize(n);
+    cscale.resize(n);
+    for (int i = 0; i < n; ++i) rscale[i] = std::exp(u[i]);
+    for (int j = 0; j < n; ++j) cscale[j] = std::exp(v[j]) / amax[j];
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(rscale[i]) || !std::isfinite(cscale[i]) || rscale[i] == 0.0 || cscale[i] == 0.0) {
+            why = "the matching's scaling is out of the double range";
+            return false;
+        }
+    return true;
+}
+
 void build_sparse_symbolic(Circuit& c) {
     SparseLU& L = c.lu;
     const int n = c.n_aug;
@@ -948,10 +1083,12 @@ void build_sparse_symbolic(Circuit& c) {
     // 1. static-pivot transversal for the voltage-source rows: swap the KCL row
     //    of a source terminal with the source's branch row so both diagonals
     //    are exactly +-1 (the branch rows have a structurally zero diagonal).
+    //    A weighted matching computed from values (weighted_matching) replaces it.
     L.perm_r.resize(n);
     std::iota(L.perm_r.begin(), L.perm_r.end(), 0);
     std::vector<char> used(n, 0);
-    for (int k = 0; k < c.n_vsrc; ++k) {
+    if ((int)L.match_r.size() == n) L.perm_r = L.match_r;
+    else for (int k = 0; k < c.n_vsrc; ++k) {
         int b = c.n_unk + k;
         int p = c.vsrc_p[k], m = c.vsrc_n[k];
         int r = -1;

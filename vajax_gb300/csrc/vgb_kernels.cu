@@ -245,17 +245,22 @@ void launch_nr_apply(const NRUpdateArgs& a, cudaStream_t s) {
 
 // Right-hand side of the block M: b restricted to M minus the couplings to the
 // singletons solved first (x_F = b_F / diag).  Also writes x_F.
+// With the scaling of a weighted matching (rscale non-null) the block M is
+// factorised as diag(r) M diag(s): its right-hand side is scaled by r here and
+// its solution by s when the backward solve writes it.
 template <typename T>
 __global__ void lu_pre_kernel(int nM, int nF, const int* brow, const int* pre_ptr, const int* pre_e,
                               const int* pre_f, const int* f_col, const int* f_arow, const int* f_diag_e,
-                              const double* A, const double* b, T* rhsM, double* xout) {
+                              const double* A, const double* b, const double* rscale, T* rhsM, double* xout) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nM) {
-        double v = b[brow[i]];
+        const int ra = brow[i];
+        double v = b[ra];
         for (int e = pre_ptr[i]; e < pre_ptr[i + 1]; ++e) {
             const int f = pre_f[e];
             v -= A[pre_e[e]] * (b[f_arow[f]] / A[f_diag_e[f]]);
         }
+        if (rscale) v *= rscale[ra];
         rhsM[i] = (T)v;
     } else if (i < nM + nF) {
         const int f = i - nM;
@@ -288,7 +293,23 @@ __global__ void __launch_bounds__(POST_THREADS) lu_post_kernel(int nL, const int
 }
 
 
-void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) { mf_factor(c, A, fp32, s); }
+__global__ void scale_slots_kernel(int nnz, const double* __restrict__ A, const double* __restrict__ sc,
+                                   double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nnz) out[e] = A[e] * sc[e];
+}
+
+// The block M is factorised from the scaled values when a weighted matching
+// is in use (one pass over the CSR values before the factorisation).
+void lu_factor(Circuit& c, const double* A, bool fp32, cudaStream_t s) {
+    SparseLU& L = c.lu;
+    if (L.d_slot_scale.p && c.nnz) {
+        scale_slots_kernel<<<ceil_div(c.nnz, 256), 256, 0, s>>>(c.nnz, A, L.d_slot_scale.p, L.d_scaled.p);
+        VGB_CUDA(cudaGetLastError());
+        A = L.d_scaled.p;
+    }
+    mf_factor(c, A, fp32, s);
+}
 
 template <typename T>
 static void lu_solve_once(Circuit& c, const double* A, const double* rhs, double* x, T* rhsM, T* ybuf, T* xbuf,
@@ -298,7 +319,7 @@ static void lu_solve_once(Circuit& c, const double* A, const double* rhs, double
     if (nM + nF)
         lu_pre_kernel<T><<<ceil_div(nM + nF, 256), 256, 0, s>>>(nM, nF, L.d_brow.p, L.d_pre_ptr.p, L.d_pre_e.p,
                                                                 L.d_pre_f.p, L.d_f_col.p, L.d_f_arow.p,
-                                                                L.d_f_diag_e.p, A, rhs, rhsM, x);
+                                                                L.d_f_diag_e.p, A, rhs, L.d_rscale.p, rhsM, x);
     if (nM) mf_solve_t<T>(c, rhsM, ybuf, xbuf, x, s);
     if (nL)
         lu_post_kernel<<<nL, POST_THREADS, 0, s>>>(nL, L.d_l_col.p, L.d_l_arow.p,

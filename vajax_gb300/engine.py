@@ -59,6 +59,12 @@ class SimulationOptions:
     # extension: tune launch shapes and the factorisation schedule on the GPU in
     # prepare() (vajax_gb300.autotune); "cache" reuses earlier results per pattern
     autotune: str = "off"  # "off" | "on" | "cache"
+    # extension: "static" pivots on the diagonal after the voltage-source
+    # transversal (circuits small enough take the dense LU with partial
+    # pivoting instead); "matching" takes the sparse LU at every size, with a
+    # weighted matching and scaling computed from the Jacobian at the DC start
+    # point (vgb_solver_match), for high-gain circuits whose diagonal is small
+    sparse_pivoting: str = "static"  # "static" | "matching"
 
 
 @dataclass
@@ -179,7 +185,9 @@ class CircuitEngine:
         self.max_steps = max_steps if max_steps is not None else int(t_stop / dt * 1.1) + 10
         if self.device is None:
             prec = {"fp64": 0, "fp32": 1, "mixed": 1}[self.precision]
-            if self.rc.n_nodes - 1 + len(self.rc.vsources) <= DENSE_MAX:
+            if self.options.sparse_pivoting not in ("static", "matching"):
+                raise ValueError(f"sparse_pivoting must be 'static' or 'matching', not {self.options.sparse_pivoting!r}")
+            if self.rc.n_nodes - 1 + len(self.rc.vsources) <= DENSE_MAX and self.options.sparse_pivoting == "static":
                 prec = 2  # small circuits: dense LU with partial pivoting, as the reference's dense path
             dev = DeviceCircuit(self.rc, precision=prec, refine_sweeps=getattr(self, "refine_sweeps", 1),
                                 gmin=self.options.gmin, device=False)
@@ -263,6 +271,19 @@ class CircuitEngine:
         finally:
             dev.set_precision(prec, sweeps)
 
+    def _match_at(self, X0, vs0, is0):
+        """With sparse_pivoting="matching", the weighted matching and scaling of
+        the sparse LU from the Jacobian at X0 (once per device circuit)."""
+        import torch
+        dev = self.device
+        if self.options.sparse_pivoting != "matching" or getattr(dev, "precision", 0) == 2:
+            return
+        if getattr(dev, "matched", False):
+            return
+        csr = dev.build_system(torch.as_tensor(np.array(X0, np.float64), device="cuda"),
+                               vs0 if len(self.rc.vsources) else None, is0)[0]
+        dev.set_matching(csr)
+
     def _initial_state(self):
         import torch
         rc = self.rc
@@ -274,6 +295,7 @@ class CircuitEngine:
             X0 = np.zeros(n_x)
             for node, v in self.options.ic.items():
                 X0[rc.node_names[node]] = v
+            self._match_at(X0, vs0, is0)
             Xd = torch.as_tensor(X0, device="cuda")
             _, _, Q, _, fres = dev.build_system(Xd, vs0 if len(rc.vsources) else None, is0)
             I0 = np.where(rc.vsrc_p > 0, -fres.cpu().numpy()[np.maximum(rc.vsrc_p - 1, 0)], 0.0)
@@ -281,6 +303,7 @@ class CircuitEngine:
         X0 = np.zeros(n_x)
         X0[: rc.n_nodes] = self.initial_guess()
         o = self.options
+        self._match_at(X0, vs0, is0)
 
         def solve(X, gshunt=0.0, sf=1.0, node_limit=0.0, itl=None):
             Xd = torch.as_tensor(np.array(X, np.float64), device="cuda")

@@ -27,6 +27,22 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_lib.f64p)
 
 
+def weighted_matching(indptr, indices, vals):
+    """Maximum-product matching with scaling of a host CSR matrix (the C ABI's
+    vgb_weighted_matching): (perm_r, rscale, cscale), row r of the permuted
+    matrix being row perm_r[r]; rscale by row, cscale by column."""
+    indptr = np.ascontiguousarray(indptr, np.int32)
+    indices = np.ascontiguousarray(indices, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    n = len(indptr) - 1
+    perm = np.zeros(max(n, 1), np.int32)
+    rs = np.zeros(max(n, 1), np.float64)
+    cs = np.zeros(max(n, 1), np.float64)
+    lib = _lib.load()
+    _lib.check(lib.vgb_weighted_matching(n, _ip(indptr), _ip(indices), _dp(vals), _ip(perm), _dp(rs), _dp(cs)))
+    return perm[:n], rs[:n], cs[:n]
+
+
 def _ptr(t) -> Optional[int]:
     if t is None:
         return None
@@ -42,6 +58,7 @@ class DeviceCircuit:
                  device: bool = True):
         self.rc = rc
         self.precision = precision
+        self.matched = False  # weighted matching of the sparse LU in use (set_matching)
         self._refine_sweeps = refine_sweeps
         self._gmin = gmin
         self.finalized = False
@@ -168,6 +185,22 @@ class DeviceCircuit:
         order = np.zeros(max(self.n_aug, 1), np.int32)
         self._check(self.lib.vgb_solver_order(self.h, _ip(perm_r), _ip(order)))
         return perm_r[: self.n_aug], order[: self.n_aug]
+
+    def set_matching(self, csr_vals=None):
+        """Weighted matching and scaling of the static-pivot LU from Jacobian
+        values (host or device array of nnz values; see vgb_solver_match).
+        None restores the voltage-source transversal without scaling."""
+        if csr_vals is None:
+            self._check(self.lib.vgb_solver_match(self.h, None))
+            self.matched = False
+            return
+        if hasattr(csr_vals, "detach"):
+            csr_vals = csr_vals.detach().cpu().numpy()
+        vals = np.ascontiguousarray(np.asarray(csr_vals, np.float64)[: self.nnz])
+        if vals.size != self.nnz:
+            raise ValueError(f"expected {self.nnz} Jacobian values, got {vals.size}")
+        self._check(self.lib.vgb_solver_match(self.h, _dp(vals)))
+        self.matched = True
 
     def pattern(self):
         indptr = np.zeros(self.n_aug + 1, np.int32)
