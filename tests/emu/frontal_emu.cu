@@ -26,7 +26,8 @@ extern "C" int emu_solve(void* h, const double* A, const double* b, double* x, i
     SparseLU& L = c.lu;
     const int ns = L.nsn;
     std::vector<double> pool(L.fr_off.empty() ? 1 : L.fr_off.back() + 1, NAN);
-    std::vector<int> tver(std::max<long long>(L.n_tiles, 1), 0), done(ns, 0), cnt(ns, 0);
+    std::vector<int> tver(std::max<long long>(L.n_tiles, 1), 0), tcnt(std::max<long long>(L.n_tiles, 1), 0);
+    std::vector<int> done(ns, 0), cnt(ns, 0);
     *npiv_fix = 0;
     auto fr_m = [&](int s) { return (int)(L.fr_ptr[s + 1] - L.fr_ptr[s]); };
     for (size_t t = 0; t < L.task_type.size(); ++t) {
@@ -67,6 +68,7 @@ extern "C" int emu_solve(void* h, const double* A, const double* b, double* x, i
       const int c0 = tlo(j, kb, w), nc = thi(j, kb, nb, w, m) - c0;
       CHK(nk >= 1 && nk <= TS && nr >= 1 && nr <= TS && nc >= 1 && nc <= TS);
       int* tv = tver.data() + tb;
+      int* tc = tcnt.data() + tb;
       auto load = [&](std::vector<double>& d, int rr, int n_r, int cc, int n_c) {
         d.assign(TS * LDD, 0.0);
         for (int cq = 0; cq < n_c; ++cq) for (int rq = 0; rq < n_r; ++rq) {
@@ -94,15 +96,19 @@ extern "C" int emu_solve(void* h, const double* A, const double* b, double* x, i
       std::vector<double> T0, T1, T2;
       if (type == TASK_GETRF) {
         if (k == 0) { for (int q = L.ch_ptr[S]; q < L.ch_ptr[S + 1]; ++q) CHK(done[L.ch_idx[q]]); assemble(T0, tb, 0, 0); }
-        else {
+        else if (k == 1) {
           CHK(tv[k * nb + k - 1] == TILE_FINAL && tv[(k - 1) * nb + k] == TILE_FINAL);
-          if (k > 1) CHK(tv[k * nb + k] == k - 1); else CHK(tv[k * nb + k] == 0);
+          CHK(tv[k * nb + k] == 0);
           const int p0 = tlo(k - 1, kb, w), np = thi(k - 1, kb, nb, w, m) - p0;
           std::vector<double> Lt, Ut; load(Lt, k0, nk, p0, np); load(Ut, p0, np, k0, nk);
-          if (k > 1) load(T0, k0, nk, k0, nk); else assemble(T0, tb + (long long)k * nb + k, k0, k0);
+          assemble(T0, tb + (long long)k * nb + k, k0, k0);
           for (int cq = 0; cq < nk; ++cq) for (int r = 0; r < TS; ++r) {
             double acc = 0; for (int kk = 0; kk < np; ++kk) acc += Lt[r + kk * LDD] * Ut[kk + cq * LDD];
             T0[r + cq * LDD] -= acc; }
+        } else {
+          // the diagonal tile's last update ran as DUPD_SLICES slice tasks
+          CHK(tc[k * nb + k] == DUPD_SLICES);
+          load(T0, k0, nk, k0, nk);
         }
         for (int p = 0; p < nk; ++p) {
           double piv = T0[p + p * LDD]; if (piv == 0 || !std::isfinite(piv)) { piv = 1e-30; T0[p + p * LDD] = piv; (*npiv_fix)++; }
@@ -111,6 +117,18 @@ extern "C" int emu_solve(void* h, const double* A, const double* b, double* x, i
         }
         store(T0, k0, nk, k0, nk); tv[k * nb + k] = TILE_FINAL;
         if (k == kb - 1 && nb == kb) done[S] = 1;
+      } else if (type >= TASK_DUPD) {
+        CHK(type < TASK_DUPD + DUPD_SLICES && i == j && i == k + 1 && i < kb && i >= 2);
+        CHK(tv[i * nb + k] == TILE_FINAL && tv[k * nb + i] == TILE_FINAL && tv[i * nb + i] == k);
+        CHK(tc[i * nb + i] < DUPD_SLICES);
+        const int cs = (type - TASK_DUPD) * DUPD_W;
+        load(T0, r0, nr, k0, nk); load(T1, k0, nk, r0, nr); load(T2, r0, nr, r0, nr);
+        for (int cq = cs; cq < cs + DUPD_W && cq < nr; ++cq) for (int r = 0; r < TS; ++r) {
+          double acc = 0; for (int kk = 0; kk < nk; ++kk) acc += T0[r + kk * LDD] * T1[kk + cq * LDD];
+          T2[r + cq * LDD] -= acc; }
+        for (int cq = cs; cq < cs + DUPD_W && cq < nr; ++cq) for (int rq = 0; rq < nr; ++rq)
+          FS[(r0 + rq) + (long long)(r0 + cq) * m] = T2[rq + cq * LDD];
+        tc[i * nb + i]++;
       } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
         CHK(tv[k * nb + k] == TILE_FINAL); if (k > 0) CHK(tv[i * nb + j] == k);
         if (type == TASK_TRSM_L) CHK(j == k && i > k); else CHK(i == k && j > k);

@@ -120,7 +120,7 @@ static void upload_lu(Circuit& c, int precision) {
     up(L.d_tasm_e, L.tasm_e);
     up(L.d_tasm_pos, L.tasm_pos);
     up(L.d_tch, L.tch);
-    L.d_tver.alloc(std::max<long long>(L.n_tiles, 1));
+    L.d_tver.alloc(std::max<long long>(2 * L.n_tiles, 1));  // versions, then diagonal update slice counts
     ensure_pools(c, precision);
     L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
     L.d_mf_flags.zero(c.stream);

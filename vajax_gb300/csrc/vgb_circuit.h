@@ -99,7 +99,13 @@ constexpr int SMALL_FRONT = 64;
 constexpr int FRONT_TILE = 32;
 constexpr int FRONT_TILE_LD = 33;          // shared-memory leading dimension of a tile (no bank conflicts)
 constexpr int TILE_FINAL = 1 << 20;        // tile version of a finished L / U / diagonal tile
-enum TaskType : int { TASK_SMALL = 0, TASK_GETRF = 1, TASK_TRSM_L = 2, TASK_TRSM_U = 3, TASK_GEMM = 4 };
+enum TaskType : int { TASK_SMALL = 0, TASK_GETRF = 1, TASK_TRSM_L = 2, TASK_TRSM_U = 3, TASK_GEMM = 4, TASK_DUPD = 5 };
+// The last update of a diagonal pivot tile (d, d), d >= 2 (the GEMM (d, d, d-1)
+// on the chain of dependent pivot tiles), runs as DUPD_SLICES tasks of
+// DUPD_W columns each, on as many CTAs: task type TASK_DUPD + slice, with
+// (i, j, k) = (d, d, d - 1).  GETRF(d) waits for all slices.
+constexpr int DUPD_SLICES = 4;
+constexpr int DUPD_W = FRONT_TILE / DUPD_SLICES;
 
 // Static-pivot sparse LU structures (host symbolic + device numeric).
 struct SparseLU {

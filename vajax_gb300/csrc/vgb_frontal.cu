@@ -91,6 +91,7 @@ struct MFArgs {
     int* done;        // [ns] epoch flag: front factorised (contribution block final)
     int* count;       // [ns] final contribution tiles of a large front
     int* tver;        // [n_tiles] updates applied to a tile, or TILE_FINAL
+    int* tcnt;        // [n_tiles] slices of a diagonal tile's last update applied
     int* counter;
     int* abort_flag;
     int* err;
@@ -436,35 +437,68 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
         T* T1 = sm + TILE_ELEMS;
         T* T2 = sm + 2 * TILE_ELEMS;
         if (type == TASK_GETRF) {
-            // GETRF(k) for k > 0 first applies the last update of its diagonal tile,
-            // A(k,k) -= L(k,k-1) U(k-1,k), which has no task of its own: that keeps one
-            // hand-off per pivot step off the chain of dependent diagonal tiles.
+            // The last update of the diagonal tile, A(k,k) -= L(k,k-1) U(k-1,k), is on
+            // the chain of dependent pivot tiles and has no GEMM task: GETRF(1) applies
+            // it itself (after the first touch of tile (1, 1)), and for k >= 2 it runs
+            // as DUPD_SLICES column slices on as many CTAs, whose count GETRF(k) waits
+            // for.  A 32 x 32 x 32 update takes ~9 us of one SM's FP64 issue; a slice
+            // takes a quarter of that.
             const long long dk = (long long)k * nb + k;
             bool ok;
             if (k == 0) ok = wait_children(a, S);
-            else ok = wait3(a, tv + dk - 1, TILE_FINAL, tv + (long long)(k - 1) * nb + k, TILE_FINAL,
-                            k > 1 ? tv + dk : nullptr, k - 1);
+            else if (k == 1) ok = wait3(a, tv + dk - 1, TILE_FINAL, tv + (long long)(k - 1) * nb + k, TILE_FINAL,
+                                        nullptr, 0);
+            else ok = wait3(a, a.tcnt + tb + dk, DUPD_SLICES, nullptr, 0, nullptr, 0);
             if (!ok) continue;
             if (k == 0) {
                 assemble_tile<T>(a, tb, T2, 0, 0, pool);
-            } else {
+            } else if (k == 1) {
                 const int p0 = tile_lo(k - 1, kb, w), np = tile_hi(k - 1, kb, nb, w, m) - p0;
-                TileRegs<T> lt, ut, dt;
+                TileRegs<T> lt, ut;
                 fetch_tile(lt, FS, m, k0, nk, p0, np);
                 fetch_tile(ut, FS, m, p0, np, k0, nk);
-                if (k > 1) fetch_tile(dt, FS, m, k0, nk, k0, nk);
                 put_tile(T0, lt);
                 put_tile(T1, ut);
-                if (k > 1) put_tile(T2, dt);
-                else assemble_tile<T>(a, tb + dk, T2, k0, k0, pool);  // first touch of tile (1, 1)
+                assemble_tile<T>(a, tb + dk, T2, k0, k0, pool);  // first touch of tile (1, 1)
                 __syncthreads();
                 gemm_tile<T>(T2, T0, T1, np, nk);
+            } else {
+                TileRegs<T> dt;
+                fetch_tile(dt, FS, m, k0, nk, k0, nk);
+                put_tile(T2, dt);
             }
             __syncthreads();
             getrf_tile<T>(T2, nk, a.err, T0);
             store_tile<T>(FS, T2, m, k0, nk, k0, nk);
             publish(tv + dk, TILE_FINAL);
             if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
+        } else if (type >= TASK_DUPD) {
+            // slice of the last update of diagonal tile (i, i) = (k + 1, k + 1): its
+            // columns [cs, cs + DUPD_W) of A(i,i) -= L(i,k) U(k,i); lane = row, warp =
+            // column of the slice.  The sum runs in the order of gemm_tile's, so the
+            // tile is bit for bit what the fused update gives.
+            static_assert(DUPD_W == NWARP, "one slice column per warp");
+            const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+            const long long di = (long long)i * nb + i;
+            if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + i, TILE_FINAL, tv + di, k))
+                continue;
+            const int cs = (type - TASK_DUPD) * DUPD_W;
+            const int col = cs + wp;  // column of the diagonal tile, < nr while in the tile
+            TileRegs<T> lt;
+            fetch_tile(lt, FS, m, r0, nr, k0, nk);
+            const T uv = (lane < nk && col < nr) ? __ldcg(FS + (k0 + lane) + (long long)(r0 + col) * m) : (T)0;
+            const T cv = (lane < nr && col < nr) ? __ldcg(FS + (r0 + lane) + (long long)(r0 + col) * m) : (T)0;
+            put_tile(T0, lt);
+            T1[lane + wp * LD] = uv;
+            __syncthreads();
+            T acc = (T)0;
+            for (int q = 0; q < nk; ++q) acc += T0[lane + q * LD] * T1[q + wp * LD];
+            if (lane < nr && col < nr) __stcg(FS + (r0 + lane) + (long long)(r0 + col) * m, cv - acc);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(a.tcnt + tb + di, 1);
+            }
         } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
             const int* own = tv + (long long)i * nb + j;
             if (!wait3(a, tv + (long long)k * nb + k, TILE_FINAL, k > 0 ? own : nullptr, k, nullptr, 0)) continue;
@@ -841,6 +875,7 @@ static MFArgs mf_args(Circuit& c, const double* A) {
     a.done = L.d_mf_flags.p;
     a.count = L.d_mf_count.p;
     a.tver = L.d_tver.p;
+    a.tcnt = L.d_tver.p + L.n_tiles;
     a.counter = L.d_counters.p;
     a.abort_flag = L.d_counters.p + 3;
     a.err = &c.d_status.p->dev_err;
@@ -857,7 +892,7 @@ static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_flags.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_count.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
-    if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, L.n_tiles * sizeof(int), s));
+    if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, 2 * L.n_tiles * sizeof(int), s));
     MFArgs a = mf_args(c, A);
     a.epoch = 1;
     const int blocks = std::min(sm_count() * std::min(std::max(c.tune_factor_ctas, 1), MF_FACTOR_CTAS_MAX),

@@ -510,7 +510,7 @@ void schedule_tasks(SparseLU& L, int slots) {
     task_of.reserve(2 * (size_t)nt);
     auto key = [&](int s, int type, int i, int j, int k) {
         const long long tile = (long long)L.fr_tile0[s] + (long long)i * L.fr_nb[s] + j;
-        return ((tile << 16) + k) * 8 + type;  // k < nb < 2^16
+        return ((tile << 16) + k) * 16 + type;  // k < nb < 2^16, type < TASK_DUPD + DUPD_SLICES <= 16
     };
     std::vector<int> front_task0(ns, -1);
     for (int t = 0; t < nt; ++t) {
@@ -527,6 +527,7 @@ void schedule_tasks(SparseLU& L, int slots) {
     auto trsm_l = [&](int s, int i, int k) { return find(s, TASK_TRSM_L, i, k, k); };
     auto trsm_u = [&](int s, int k, int j) { return find(s, TASK_TRSM_U, k, j, k); };
     auto gemm = [&](int s, int i, int j, int k) { return find(s, TASK_GEMM, i, j, k); };
+    static_assert(TASK_DUPD + DUPD_SLICES <= 16, "task types must fit the schedule key");
     // the tasks whose completion completes a front
     std::vector<std::vector<int>> finals(ns);
     for (int s = 0; s < ns; ++s) {
@@ -559,13 +560,19 @@ void schedule_tasks(SparseLU& L, int slots) {
             cost[t] = 3000 + (2.0 / 3.0) * tile * tile * tile / 2;
             if (k == 0) {
                 children_done(s, pred[t]);
-            } else {
-                // also applies the diagonal tile's update of step k - 1
+            } else if (k == 1) {
+                // also applies the diagonal tile's update of step 0
                 cost[t] += 2.0 * tile * tile * tile / 2;
-                pred[t].push_back(trsm_l(s, k, k - 1));
-                pred[t].push_back(trsm_u(s, k - 1, k));
-                if (k > 1) pred[t].push_back(gemm(s, k, k, k - 2));
+                pred[t].push_back(trsm_l(s, 1, 0));
+                pred[t].push_back(trsm_u(s, 0, 1));
+            } else {
+                for (int sl = 0; sl < DUPD_SLICES; ++sl) pred[t].push_back(find(s, TASK_DUPD + sl, k, k, k - 1));
             }
+        } else if (type >= TASK_DUPD) {
+            cost[t] = 1500 + 2.0 * tile * tile * DUPD_W / 2;
+            pred[t].push_back(trsm_l(s, i, k));
+            pred[t].push_back(trsm_u(s, k, j));
+            pred[t].push_back(gemm(s, i, j, k - 1));
         } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
             cost[t] = 2500 + tile * tile * tile / 2;
             pred[t].push_back(getrf(s, k));
@@ -766,8 +773,9 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
     // ceil(w/32) pivot tiles and nb = kb + ceil((m-w)/32) tiles per dimension,
     // and for each pivot tile k: GETRF(k), TRSM_L(i,k) and TRSM_U(k,j) for
     // i, j > k, then GEMM(i,j,k) for i, j > k except the next diagonal pivot
-    // tile (k+1, k+1), whose update GETRF(k+1) applies.  Every task waits only
-    // on tasks that precede it in the list.
+    // tile (k+1, k+1): GETRF(1) applies that update itself (it also assembles
+    // tile (1, 1)), and for k + 1 >= 2 it runs as DUPD_SLICES column slices.
+    // Every task waits only on tasks that precede it in the list.
     L.fr_cv_off.assign(ns + 1, 0);
     L.task_type.clear();
     L.task_front.clear();
@@ -806,6 +814,8 @@ void build_fronts(SparseLU& L, const std::vector<int>& parent, const std::vector
             push_task(TASK_GETRF, s, k, k, k);
             for (int i = k + 1; i < nb; ++i) push_task(TASK_TRSM_L, s, i, k, k);
             for (int j = k + 1; j < nb; ++j) push_task(TASK_TRSM_U, s, k, j, k);
+            if (k + 1 < kb && k + 1 >= 2)
+                for (int sl = 0; sl < DUPD_SLICES; ++sl) push_task(TASK_DUPD + sl, s, k + 1, k + 1, k);
             for (int j = k + 1; j < nb; ++j)
                 for (int i = k + 1; i < nb; ++i)
                     if (!(i == k + 1 && j == k + 1 && k + 1 < kb)) push_task(TASK_GEMM, s, i, j, k);
