@@ -41,6 +41,14 @@ __device__ __forceinline__ void st_rel(int* p, int v) {
     cuda::atomic_ref<int, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_release);
 }
 
+// Column flags of one tile task in shared memory (block scope).
+__device__ __forceinline__ int ld_acq_cta(const int* p) {
+    return cuda::atomic_ref<const int, cuda::thread_scope_block>(*p).load(cuda::memory_order_acquire);
+}
+__device__ __forceinline__ void st_rel_cta(int* p, int v) {
+    cuda::atomic_ref<int, cuda::thread_scope_block>(*p).store(v, cuda::memory_order_release);
+}
+
 // Spin until *flag == value; gives up after `limit` polls (sets the timeout
 // error bit and the abort flag) or when another CTA has aborted.
 __device__ bool wait_eq(const int* flag, int value, int* abort_flag, int* err, unsigned limit) {
@@ -105,6 +113,7 @@ constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
 // shared memory of a factorisation CTA: one small front, or three tiles
 constexpr int MF_SMEM_ELEMS = SMALL_FRONT * SMALL_FRONT;
 static_assert(3 * TILE_ELEMS <= MF_SMEM_ELEMS, "three tiles must fit in the small-front buffer");
+static_assert(FRONT_TILE * FRONT_TILE + FRONT_TILE <= TILE_ELEMS, "a tile area holds 32 exchanged columns and 32 reciprocals");
 
 __device__ __forceinline__ int tile_lo(int t, int kb, int w) {
     return t < kb ? t * FRONT_TILE : w + (t - kb) * FRONT_TILE;
@@ -271,50 +280,77 @@ __device__ __forceinline__ void next_pivot(T& col, int p, int lane, int* err, T&
     r = vgb_rcp(piv);  // on the chain of dependent pivot steps: the short reciprocal
 }
 
-// The elimination steps below exchange the step's pivot column (or row) through a
-// double-buffered slot of `xch` (step s uses xch[32 (s & 1) ...]), so one block
-// barrier per step suffices: a warp can only overwrite a slot two steps later, after
-// the barrier that every reader of that slot has passed.
+// The elimination steps below hand each finished column (or row) from the warp
+// that owns it to the others through shared memory: the owner stores it in
+// xch[32 c ...] and releases flag[c]; a warp that needs it acquires the flag
+// (bounded spin) and loads it.  No block barrier per step: the owner of the
+// next column applies the step to that column first and publishes it at
+// once, and each warp applies the step to its other columns afterwards, while
+// the chain of dependent steps goes on in the next owner.  One warp issues at
+// most one FP64 instruction per 64 cycles, so with a barrier per step every
+// step waited for the busiest warp's updates; the per-element operations and
+// their order are those of the barrier form.
+__device__ __forceinline__ void col_publish(int* f) {
+    __threadfence_block();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) st_rel_cta(f, 1);
+}
+__device__ __forceinline__ void col_wait(const int* f, int* err) {
+    unsigned it = 0;
+    while (ld_acq_cta(f) == 0) {
+        if (++it > (1u << 22)) {
+            if ((threadIdx.x & 31) == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+            break;
+        }
+    }
+}
 
 // LU without pivoting of the leading n x n block of a tile.  lane = row; warp
-// g owns columns g, g + NWARP, ... in registers.  The owner of column p + 1
-// updates that column first and forms the next pivot's reciprocal (kept in its
-// registers) while the other warps finish step p, which keeps the FP64
-// division off the chain of dependent steps.
+// g owns columns g, g + NWARP, ... in registers.  xch holds the multiplier
+// columns (32 x 32), flag the 32 column flags.
 template <typename T>
-__device__ void getrf_tile(T* t, int n, int* err, T* xch) {
+__device__ void getrf_tile(T* t, int n, int* err, T* xch, int* flag) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = t[lane + (g + NWARP * q) * LD];
-    T r = (T)0;  // reciprocal of the current pivot, valid in the warp that owns its column
-    if (g == 0 && n > 0) next_pivot<T>(a[0], 0, lane, err, r);
+    if (threadIdx.x < FRONT_TILE) flag[threadIdx.x] = 0;
+    __syncthreads();
+    if (n > 0 && g == 0) {
+        T r;
+        next_pivot<T>(a[0], 0, lane, err, r);
+        if (lane > 0) a[0] *= r;
+        xch[lane] = a[0];
+        col_publish(flag);
+    }
+    for (int p = 0; p + 1 < n; ++p) {
+        if (g + NWARP * (QPW - 1) <= p) break;  // no column of this warp is right of p
+        // multipliers L(:, p): in registers for the owner, else from its flag
+        T l;
+        if (g == (p & (NWARP - 1))) {
+            l = a[p / NWARP];
+        } else {
+            col_wait(flag + p, err);
+            l = xch[p * FRONT_TILE + lane];
+        }
+        const int p1 = p + 1;
+        if (g == (p1 & (NWARP - 1))) {
+            // the next pivot column first: update, pivot, multipliers, publish
+            const int q1 = p1 / NWARP;
+            const T u = __shfl_sync(0xffffffffu, a[q1], p);
+            if (lane > p) a[q1] -= l * u;
+            T r;
+            next_pivot<T>(a[q1], p1, lane, err, r);
+            if (lane > p1) a[q1] *= r;
+            xch[p1 * FRONT_TILE + lane] = a[q1];
+            col_publish(flag + p1);
+        }
 #pragma unroll
-    for (int p = 0; p < FRONT_TILE; ++p) {
-        if (p < n) {
-            T* xb = xch + ((p & 1) << 5);
-            if (g == (p & (NWARP - 1))) {
-                // owner of column p: multipliers L(:, p) for the other warps
-                const int qp = p / NWARP;
-                if (lane > p) a[qp] *= r;
-                xb[lane] = a[qp];
-            }
-            __syncthreads();
-            const T l = xb[lane];
-            const int p1 = p + 1;
-            if (p1 < n && g == (p1 & (NWARP - 1))) {
-                const int q1 = p1 / NWARP;
-                const T u = __shfl_sync(0xffffffffu, a[q1], p);
-                if (lane > p) a[q1] -= l * u;
-                next_pivot<T>(a[q1], p1, lane, err, r);
-            }
-#pragma unroll
-            for (int q = 0; q < QPW; ++q) {
-                const int c = g + NWARP * q;
-                if (c > p1) {  // warp-uniform: finished columns issue no FP64 work
-                    const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
-                    if (c < n && lane > p) a[q] -= l * u;
-                }
+        for (int q = 0; q < QPW; ++q) {
+            const int c = g + NWARP * q;
+            if (c > p1 && c < n) {  // warp-uniform: finished columns issue no FP64 work
+                const T u = __shfl_sync(0xffffffffu, a[q], p);  // U(p, c)
+                if (lane > p) a[q] -= l * u;
             }
         }
     }
@@ -324,31 +360,44 @@ __device__ void getrf_tile(T* t, int n, int* err, T* xch) {
 }
 
 // x := x U^-1 with U the upper triangle (with diagonal) of the n x n tile d.
-// lane = row of x; warp g owns columns g, g + NWARP, ...
+// lane = row of x; warp g owns columns g, g + NWARP, ...; xch holds the solved
+// columns (32 x 32) and then the diagonal's reciprocals.
 template <typename T>
-__device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
+__device__ void trsm_l_tile(T* x, const T* d, int n, T* xch, int* flag, int* err) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
-    T* dinv = xch + 64;  // reciprocals of the diagonal, formed once in parallel
+    T* dinv = xch + FRONT_TILE * FRONT_TILE;  // reciprocals of the diagonal, formed once in parallel
     if (threadIdx.x < n) dinv[threadIdx.x] = vgb_rcp(d[threadIdx.x + threadIdx.x * LD]);
+    if (threadIdx.x < FRONT_TILE) flag[threadIdx.x] = 0;
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = x[lane + (g + NWARP * q) * LD];
     __syncthreads();
+    if (n > 0 && g == 0) {
+        a[0] *= dinv[0];
+        xch[lane] = a[0];
+        col_publish(flag);
+    }
+    for (int c = 0; c + 1 < n; ++c) {
+        if (g + NWARP * (QPW - 1) <= c) break;
+        T xc;
+        if (g == (c & (NWARP - 1))) {
+            xc = a[c / NWARP];
+        } else {
+            col_wait(flag + c, err);
+            xc = xch[c * FRONT_TILE + lane];
+        }
+        const int c1 = c + 1;
+        if (g == (c1 & (NWARP - 1))) {
+            const int q1 = c1 / NWARP;
+            a[q1] -= xc * d[c + c1 * LD];
+            a[q1] *= dinv[c1];
+            xch[c1 * FRONT_TILE + lane] = a[q1];
+            col_publish(flag + c1);
+        }
 #pragma unroll
-    for (int c = 0; c < FRONT_TILE; ++c) {
-        if (c < n) {
-            T* xb = xch + ((c & 1) << 5);
-            if (g == (c & (NWARP - 1))) {
-                a[c / NWARP] *= dinv[c];
-                xb[lane] = a[c / NWARP];
-            }
-            __syncthreads();
-            const T xc = xb[lane];
-#pragma unroll
-            for (int q = 0; q < QPW; ++q) {
-                const int c2 = g + NWARP * q;
-                if (c2 > c && c2 < n) a[q] -= xc * d[c + c2 * LD];
-            }
+        for (int q = 0; q < QPW; ++q) {
+            const int c2 = g + NWARP * q;
+            if (c2 > c1 && c2 < n) a[q] -= xc * d[c + c2 * LD];
         }
     }
 #pragma unroll
@@ -357,25 +406,39 @@ __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch) {
 }
 
 // x := L^-1 x with L the unit lower triangle of the n x n tile d.  lane =
-// column of x; warp g owns rows g, g + NWARP, ...
+// column of x; warp g owns rows g, g + NWARP, ...; xch holds the solved rows.
 template <typename T>
-__device__ void trsm_u_tile(T* x, const T* d, int n, T* xch) {
+__device__ void trsm_u_tile(T* x, const T* d, int n, T* xch, int* flag, int* err) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    if (threadIdx.x < FRONT_TILE) flag[threadIdx.x] = 0;
     T a[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) a[q] = x[(g + NWARP * q) + lane * LD];
+    __syncthreads();
+    if (n > 0 && g == 0) {
+        xch[lane] = a[0];  // row 0 is final (unit diagonal)
+        col_publish(flag);
+    }
+    for (int r = 0; r + 1 < n; ++r) {
+        if (g + NWARP * (QPW - 1) <= r) break;
+        T yr;
+        if (g == (r & (NWARP - 1))) {
+            yr = a[r / NWARP];
+        } else {
+            col_wait(flag + r, err);
+            yr = xch[r * FRONT_TILE + lane];
+        }
+        const int r1 = r + 1;
+        if (g == (r1 & (NWARP - 1))) {
+            const int q1 = r1 / NWARP;
+            a[q1] -= d[r1 + r * LD] * yr;
+            xch[r1 * FRONT_TILE + lane] = a[q1];
+            col_publish(flag + r1);
+        }
 #pragma unroll
-    for (int r = 0; r < FRONT_TILE; ++r) {
-        if (r < n) {
-            T* xb = xch + ((r & 1) << 5);
-            if (g == (r & (NWARP - 1))) xb[lane] = a[r / NWARP];  // row r is final
-            __syncthreads();
-            const T yr = xb[lane];
-#pragma unroll
-            for (int q = 0; q < QPW; ++q) {
-                const int r2 = g + NWARP * q;
-                if (r2 > r && r2 < n) a[q] -= d[r2 + r * LD] * yr;
-            }
+        for (int q = 0; q < QPW; ++q) {
+            const int r2 = g + NWARP * q;
+            if (r2 > r1 && r2 < n) a[q] -= d[r2 + r * LD] * yr;
         }
     }
 #pragma unroll
@@ -407,6 +470,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
     extern __shared__ double smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_task;
+    __shared__ int s_col[FRONT_TILE];  // column flags of the tile kernels
     while (true) {
         if (threadIdx.x == 0) s_task = *(volatile int*)a.abort_flag ? a.n_tasks : atomicAdd(a.counter, 1);
         __syncthreads();
@@ -468,7 +532,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
                 put_tile(T2, dt);
             }
             __syncthreads();
-            getrf_tile<T>(T2, nk, a.err, T0);
+            getrf_tile<T>(T2, nk, a.err, T0, s_col);
             store_tile<T>(FS, T2, m, k0, nk, k0, nk);
             publish(tv + dk, TILE_FINAL);
             if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
@@ -509,8 +573,8 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T1, r0, c0, pool);
             else put_tile(T1, xt);
             __syncthreads();
-            if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk, T2);
-            else trsm_u_tile<T>(T1, T0, nk, T2);
+            if (type == TASK_TRSM_L) trsm_l_tile<T>(T1, T0, nk, T2, s_col, a.err);
+            else trsm_u_tile<T>(T1, T0, nk, T2, s_col, a.err);
             store_tile<T>(FS, T1, m, r0, nr, c0, nc);
             publish(tv + (long long)i * nb + j, TILE_FINAL);
         } else {  // TASK_GEMM
