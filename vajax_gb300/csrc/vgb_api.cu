@@ -125,7 +125,7 @@ static void upload_lu(Circuit& c, int precision) {
     L.d_mf_flags.alloc(4 * (size_t)std::max(L.nsn, 1));
     L.d_mf_flags.zero(c.stream);
     L.d_mf_count.alloc(std::max(L.nsn, 1));
-    L.d_counters.alloc(8);
+    L.d_counters.alloc(8 + MF_SM_SLOTS);
     L.d_slot_scale.release();
     L.d_scaled.release();
     L.d_rscale.release();

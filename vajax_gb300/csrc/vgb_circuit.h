@@ -169,7 +169,7 @@ struct SparseLU {
     DevBuf<int> d_brow, d_q;
     DevBuf<int> d_f_col, d_f_arow, d_f_diag_e, d_l_col, d_l_arow, d_l_diag_e, d_l_ptr, d_l_e, d_l_x;
     DevBuf<int> d_pre_ptr, d_pre_e, d_pre_f;
-    DevBuf<int> d_counters;  // work counters
+    DevBuf<int> d_counters;  // 8 work counters, then MF_SM_SLOTS per-SM counts
     // scaling of the matching: per CSR slot r_i s_j, the scaled values factorised, r and s
     DevBuf<double> d_slot_scale, d_scaled, d_rscale, d_cscale;
 };
@@ -279,5 +279,8 @@ void schedule_tasks(SparseLU& L, int slots);
 // per SM; a tuning value above that runs as that.
 constexpr int MF_FACTOR_THREADS = 256;
 constexpr int MF_FACTOR_CTAS_MAX = 2;
+// Per-SM counters of the factorisation (indexed by %smid), after the 8 work
+// counters of SparseLU::d_counters.
+constexpr int MF_SM_SLOTS = 1024;
 
 } // namespace vgb

@@ -41,6 +41,12 @@ __device__ __forceinline__ void st_rel(int* p, int v) {
     cuda::atomic_ref<int, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_release);
 }
 
+__device__ __forceinline__ unsigned mf_smid() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+    return r;
+}
+
 // Column flags of one tile task in shared memory (block scope).
 __device__ __forceinline__ int ld_acq_cta(const int* p) {
     return cuda::atomic_ref<const int, cuda::thread_scope_block>(*p).load(cuda::memory_order_acquire);
@@ -100,6 +106,7 @@ struct MFArgs {
     int* count;       // [ns] final contribution tiles of a large front
     int* tver;        // [n_tiles] updates applied to a tile, or TILE_FINAL
     int* tcnt;        // [n_tiles] slices of a diagonal tile's last update applied
+    int* sm_busy;     // [MF_SM_SLOTS] chain tasks running on each SM
     int* counter;
     int* abort_flag;
     int* err;
@@ -471,8 +478,19 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_task;
     __shared__ int s_col[FRONT_TILE];  // column flags of the tile kernels
+    // Tasks on the chain of dependent pivot tiles (GETRF, the diagonal update
+    // slices, and the TRSMs of the tiles next to the diagonal) mark their SM
+    // while they compute.  A CTA on a marked SM claims nothing new for up to
+    // ~20 us, so that the chain task's FP64 instructions do not queue behind a
+    // second CTA's (the SM issues one FP64 warp-instruction per ~19 cycles).
+    const unsigned my_sm = mf_smid();
+    int* busy = my_sm < MF_SM_SLOTS ? a.sm_busy + my_sm : nullptr;
     while (true) {
-        if (threadIdx.x == 0) s_task = *(volatile int*)a.abort_flag ? a.n_tasks : atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) {
+            if (busy)
+                for (int it = 0; it < 200 && *(volatile int*)busy > 0; ++it) __nanosleep(100);
+            s_task = *(volatile int*)a.abort_flag ? a.n_tasks : atomicAdd(a.counter, 1);
+        }
         __syncthreads();
         const int t = s_task;
         __syncthreads();
@@ -514,6 +532,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
                                         nullptr, 0);
             else ok = wait3(a, a.tcnt + tb + dk, DUPD_SLICES, nullptr, 0, nullptr, 0);
             if (!ok) continue;
+            if (threadIdx.x == 0 && busy) atomicAdd(busy, 1);
             if (k == 0) {
                 assemble_tile<T>(a, tb, T2, 0, 0, pool);
             } else if (k == 1) {
@@ -536,6 +555,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             store_tile<T>(FS, T2, m, k0, nk, k0, nk);
             publish(tv + dk, TILE_FINAL);
             if (k == kb - 1 && nb == kb) publish(a.done + S, a.epoch);  // no contribution block
+            if (threadIdx.x == 0 && busy) atomicSub(busy, 1);
         } else if (type >= TASK_DUPD) {
             // slice of the last update of diagonal tile (i, i) = (k + 1, k + 1): its
             // columns [cs, cs + DUPD_W) of A(i,i) -= L(i,k) U(k,i); lane = row, warp =
@@ -546,6 +566,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             const long long di = (long long)i * nb + i;
             if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + i, TILE_FINAL, tv + di, k))
                 continue;
+            if (threadIdx.x == 0 && busy) atomicAdd(busy, 1);
             const int cs = (type - TASK_DUPD) * DUPD_W;
             const int col = cs + wp;  // column of the diagonal tile, < nr while in the tile
             TileRegs<T> lt;
@@ -562,10 +583,13 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             if (threadIdx.x == 0) {
                 __threadfence();
                 atomicAdd(a.tcnt + tb + di, 1);
+                if (busy) atomicSub(busy, 1);
             }
         } else if (type == TASK_TRSM_L || type == TASK_TRSM_U) {
             const int* own = tv + (long long)i * nb + j;
             if (!wait3(a, tv + (long long)k * nb + k, TILE_FINAL, k > 0 ? own : nullptr, k, nullptr, 0)) continue;
+            const bool chain = (type == TASK_TRSM_L ? i : j) == k + 1;  // the tile next to the diagonal
+            if (chain && threadIdx.x == 0 && busy) atomicAdd(busy, 1);
             TileRegs<T> dt, xt;
             fetch_tile(dt, FS, m, k0, nk, k0, nk);
             if (k > 0) fetch_tile(xt, FS, m, r0, nr, c0, nc);
@@ -577,6 +601,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             else trsm_u_tile<T>(T1, T0, nk, T2, s_col, a.err);
             store_tile<T>(FS, T1, m, r0, nr, c0, nc);
             publish(tv + (long long)i * nb + j, TILE_FINAL);
+            if (chain && threadIdx.x == 0 && busy) atomicSub(busy, 1);
         } else {  // TASK_GEMM
             int* own = tv + (long long)i * nb + j;
             if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + j, TILE_FINAL,
@@ -940,6 +965,7 @@ static MFArgs mf_args(Circuit& c, const double* A) {
     a.count = L.d_mf_count.p;
     a.tver = L.d_tver.p;
     a.tcnt = L.d_tver.p + L.n_tiles;
+    a.sm_busy = L.d_counters.p + 8;
     a.counter = L.d_counters.p;
     a.abort_flag = L.d_counters.p + 3;
     a.err = &c.d_status.p->dev_err;
@@ -954,6 +980,7 @@ static void mf_factor_t(Circuit& c, const double* A, T* pool, cudaStream_t s) {
     // flags start at 0 and a finished front is marked 1 (a fixed epoch): every launch
     // resets them, so the launch replays unchanged inside a captured graph
     VGB_CUDA(cudaMemsetAsync(L.d_counters.p, 0, 4 * sizeof(int), s));
+    VGB_CUDA(cudaMemsetAsync(L.d_counters.p + 8, 0, MF_SM_SLOTS * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_flags.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
     VGB_CUDA(cudaMemsetAsync(L.d_mf_count.p, 0, std::max(L.nsn, 1) * sizeof(int), s));
     if (L.n_tiles) VGB_CUDA(cudaMemsetAsync(L.d_tver.p, 0, 2 * L.n_tiles * sizeof(int), s));
