@@ -662,6 +662,26 @@ struct MFSolveArgs {
     unsigned spin_limit;
 };
 
+// s = sum over p in [p0, p1), ascending, of F[i + p m] u[p].  A full block of 32
+// pivots issues all 32 loads of the row before the first FMA, so one L2 round
+// trip, not four, precedes the chain of dependent FMAs; the sum's order is
+// the same either way.
+template <typename T>
+__device__ __forceinline__ T block_dot(const T* __restrict__ F, long long m, int i, int p0, int p1, const T* u) {
+    T s = (T)0;
+    if (p1 - p0 == 32) {
+        T f[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) f[q] = F[i + (long long)(p0 + q) * m];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) s += f[q] * u[p0 + q];
+    } else {
+#pragma unroll 8
+        for (int p = p0; p < p1; ++p) s += F[i + (long long)p * m] * u[p];
+    }
+    return s;
+}
+
 // One warp solves a front of order m <= 32 (lane = row): forward with its
 // unit-lower columns, the update vector for the parent in the same pass.
 template <typename T>
@@ -800,12 +820,7 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
                 if (r < p1) u[r] = val;
             }
             __syncthreads();
-            for (int i = p1 + threadIdx.x; i < m; i += blockDim.x) {
-                T s = (T)0;
-#pragma unroll 8
-                for (int p = p0; p < p1; ++p) s += F[i + (long long)p * m] * u[p];
-                u[i] -= s;
-            }
+            for (int i = p1 + threadIdx.x; i < m; i += blockDim.x) u[i] -= block_dot<T>(F, m, i, p0, p1, u);
             __syncthreads();
         }
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -894,12 +909,7 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
                 if (r < p1) z[r] = val;
             }
             __syncthreads();
-            for (int i = threadIdx.x; i < p0; i += blockDim.x) {
-                T s = (T)0;
-#pragma unroll 8
-                for (int p = p0; p < p1; ++p) s += F[i + (long long)p * m] * z[p];
-                z[i] -= s;
-            }
+            for (int i = threadIdx.x; i < p0; i += blockDim.x) z[i] -= block_dot<T>(F, m, i, p0, p1, z);
             __syncthreads();
         }
         for (int p = threadIdx.x; p < w; p += blockDim.x) {
