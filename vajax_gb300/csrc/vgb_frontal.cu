@@ -865,18 +865,22 @@ __global__ void __launch_bounds__(MF_THREADS) mf_bwd_kernel(MFSolveArgs a, const
         // z = y_S - U12 x_tail: one pivot row per thread, coalesced down each column
         {
             // P lanes over pivot rows (coalesced down each column), G groups over tail columns;
-            // the G partial sums of a row are added in group order
+            // the G partial sums of a row are added in group order.  G is capped so that a
+            // group covers at least 8 tail columns: the sum of the partial sums is a chain of
+            // G dependent adds (64 cycles each), which for a one-pivot front with 512 groups
+            // took longer than the rest of its solve.
             int P = 32;
             while (P > 1 && P / 2 >= w) P >>= 1;
-            const int G = MF_THREADS / P;
+            const int G = max(1, min(MF_THREADS / P, (m - w + 7) / 8));
             T* part = z + m;  // [G][w]
             const int pl = threadIdx.x % P, g = threadIdx.x / P;
-            for (int p = pl; p < w; p += P) {
-                T s = (T)0;
+            if (g < G)
+                for (int p = pl; p < w; p += P) {
+                    T s = (T)0;
 #pragma unroll 4
-                for (int j = g; j < m - w; j += G) s += F[p + (long long)(w + j) * m] * xt[j];
-                part[g * w + p] = s;
-            }
+                    for (int j = g; j < m - w; j += G) s += F[p + (long long)(w + j) * m] * xt[j];
+                    part[g * w + p] = s;
+                }
             __syncthreads();
             for (int p = threadIdx.x; p < w; p += blockDim.x) {
                 T s = (T)0;
