@@ -86,6 +86,7 @@ extern "C" int emu_solve(void* h, const double* A, const double* b, double* x, i
           CHK(done[C]);
           const int mc = fr_m(C), wc = L.fr_w[C]; const double* FC = pool.data() + L.fr_off[C]; const int* em = L.em_idx.data() + L.em_ptr[C];
           const int rc = mc - wc; CHK(rlo >= 0 && rhi <= rc && clo >= 0 && chi <= rc && rlo < rhi && clo < chi);
+          CHK(rhi - rlo <= TS && chi - clo <= TS);  // a child's block spans at most one tile's rows and columns
           for (int cj = clo; cj < chi; ++cj) for (int ci = rlo; ci < rhi; ++ci) {
             const int lr = em[ci] - rr, lc = em[cj] - cc; CHK(lr >= 0 && lr < TS && lc >= 0 && lc < TS);
             const double v = FC[(wc + ci) + (long long)(wc + cj) * mc]; CHK(!std::isnan(v));

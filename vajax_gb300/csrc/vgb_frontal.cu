@@ -251,27 +251,87 @@ __device__ void store_tile(T* F, const T* src, long long m, int r0, int nr, int 
 }
 
 // First touch: A entries of the tile, then the children's blocks in child order.
+// A child's block lands in at most 32 rows and 32 columns of the tile.  Each warp
+// adds only into the tile columns it owns (column % NWARP == warp), so no two warps
+// touch one element and every element still receives its children's values in child
+// order, with no block barrier between children.  The headers of up to 32 blocks
+// are loaded at once (one per lane), and the next block's row and column maps are
+// loaded while the current block's values are added, so a block costs about one
+// L2 round trip instead of four dependent ones.
 template <typename T>
 __device__ void assemble_tile(const MFArgs& a, long long tile, T* dst, int r0, int c0, const T* pool) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int t = threadIdx.x; t < TILE_ELEMS; t += blockDim.x) dst[t] = (T)0;
     __syncthreads();
     for (long long t = a.tasm_ptr[tile] + threadIdx.x; t < a.tasm_ptr[tile + 1]; t += blockDim.x)
         dst[a.tasm_pos[t]] = (T)a.A[a.tasm_e[t]];
     __syncthreads();
-    for (long long q = a.tch_ptr[tile]; q < a.tch_ptr[tile + 1]; q += 5) {
-        const int C = a.tch[q], rlo = a.tch[q + 1], rhi = a.tch[q + 2], clo = a.tch[q + 3], chi = a.tch[q + 4];
-        const long long mc = a.fr_ptr[C + 1] - a.fr_ptr[C];
-        const int wc = a.fr_w[C];
-        const T* FC = pool + a.fr_off[C];
-        const int* em = a.em_idx + a.em_ptr[C];
-        for (int cj = clo + warp; cj < chi; cj += nw) {
-            const int dj = (em[cj] - c0) * LD;
-            const T* src = FC + (wc + cj) * mc + wc;
-            for (int ci = rlo + lane; ci < rhi; ci += 32) dst[(em[ci] - r0) + dj] += __ldcg(src + ci);
+    const long long qb = a.tch_ptr[tile];
+    const int nblk = (int)((a.tch_ptr[tile + 1] - qb) / 5);
+    for (int b0 = 0; b0 < nblk; b0 += 32) {
+        // lane k: header of block b0 + k (source base offset, leading dimension, ranges, map offset)
+        long long hbase = 0, hem = 0;
+        int hmc = 0, hrlo = 0, hnr = 0, hclo = 0, hnc = 0;
+        if (b0 + lane < nblk) {
+            const int* h = a.tch + qb + 5LL * (b0 + lane);
+            const int C = h[0];
+            hrlo = h[1];
+            hnr = h[2] - h[1];
+            hclo = h[3];
+            hnc = h[4] - h[3];
+            const long long mc = a.fr_ptr[C + 1] - a.fr_ptr[C];
+            const int wc = a.fr_w[C];
+            hmc = (int)mc;
+            hbase = a.fr_off[C] + (long long)wc * mc + wc;
+            hem = a.em_ptr[C];
+            if (hnr > FRONT_TILE || hnc > FRONT_TILE) {
+                atomicOr(a.err, DEV_ERR_BOUNDS);
+                hnr = min(hnr, FRONT_TILE);
+                hnc = min(hnc, FRONT_TILE);
+            }
         }
-        __syncthreads();
+        const int nb = min(32, nblk - b0);
+        // this lane's destination row and column in block k (-1: none)
+        auto maps = [&](int k, int& drow, int& dcol) {
+            const long long em = __shfl_sync(0xffffffffu, hem, k);
+            const int rlo = __shfl_sync(0xffffffffu, hrlo, k), nr = __shfl_sync(0xffffffffu, hnr, k);
+            const int clo = __shfl_sync(0xffffffffu, hclo, k), nc = __shfl_sync(0xffffffffu, hnc, k);
+            drow = lane < nr ? a.em_idx[em + rlo + lane] - r0 : -1;
+            dcol = lane < nc ? a.em_idx[em + clo + lane] - c0 : -1;
+            if ((unsigned)drow >= (unsigned)FRONT_TILE) drow = -1;
+            if ((unsigned)dcol >= (unsigned)FRONT_TILE) dcol = -1;
+        };
+        int drow, dcol;
+        maps(0, drow, dcol);
+        for (int k = 0; k < nb; ++k) {
+            const long long base = __shfl_sync(0xffffffffu, hbase, k);
+            const int mc = __shfl_sync(0xffffffffu, hmc, k);
+            const int rlo = __shfl_sync(0xffffffffu, hrlo, k), clo = __shfl_sync(0xffffffffu, hclo, k);
+            int ndrow = -1, ndcol = -1;
+            if (k + 1 < nb) maps(k + 1, ndrow, ndcol);
+            // the block's columns that this warp owns: at most FRONT_TILE / warps of them
+            unsigned mine = __ballot_sync(0xffffffffu, dcol >= 0 && dcol % NWARP == warp);
+            T v[FRONT_TILE / NWARP];
+            int dc[FRONT_TILE / NWARP];
+#pragma unroll
+            for (int t = 0; t < FRONT_TILE / NWARP; ++t) {
+                dc[t] = -1;
+                v[t] = (T)0;
+                if (mine) {
+                    const int l = __ffs(mine) - 1;
+                    mine &= mine - 1;
+                    dc[t] = __shfl_sync(0xffffffffu, dcol, l);
+                    if (drow >= 0) v[t] = __ldcg(pool + base + (long long)(clo + l) * mc + rlo + lane);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < FRONT_TILE / NWARP; ++t)
+                if (dc[t] >= 0 && drow >= 0) dst[drow + dc[t] * LD] += v[t];
+            drow = ndrow;
+            dcol = ndcol;
+        }
     }
+    __syncthreads();
 }
 
 // Pivot of step p (checked, replaced by 1e-30 and flagged when zero) and its
