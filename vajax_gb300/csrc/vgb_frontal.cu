@@ -6,13 +6,14 @@
 //   TASK_SMALL   front of order m <= SMALL_FRONT: one CTA assembles it in shared
 //                memory (A entries, then the children's contribution blocks in
 //                child order), eliminates its w pivots and stores it;
-//   TASK_GETRF   large front, diagonal tile k: LU of a 32 x 32 tile in registers
-//                of one warp;
+//   TASK_GETRF   large front, diagonal tile k: LU of a 32 x 32 tile in the
+//                registers of the CTA's warps;
 //   TASK_TRSM_L  tile (i, k) below it: L(i,k) = A(i,k) U(k,k)^-1;
 //   TASK_TRSM_U  tile (k, j) right of it: U(k,j) = L(k,k)^-1 A(k,j);
 //   TASK_GEMM    trailing tile (i, j): A(i,j) -= L(i,k) U(k,j), except the
-//                update of the next diagonal tile (k+1, k+1) of the pivot block,
-//                which GETRF(k+1) applies itself before it factorises the tile.
+//                update of the next diagonal tile (k+1, k+1) of the pivot block:
+//                GETRF(1) applies that one itself, and for k + 1 >= 2 it runs as
+//   TASK_DUPD    DUPD_SLICES column slices of that update on separate CTAs.
 //
 // Large fronts are never assembled as a whole: the first task that touches a
 // tile (the k = 0 task of that tile) builds it in shared memory from its A
@@ -208,11 +209,11 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
 
 // ---- tiles of large fronts -----------------------------------------------------
 
-// The tile kernels below spread each elimination step over the CTA's four
-// eight warps (two per SM sub-partition: each warp issues FP64 at a third of
-// the SM's rate, so the chain of dependent elimination steps shortens with
-// fewer columns per warp) and exchange the step's pivot row or column through
-// shared memory.
+// The tile kernels below spread each elimination step over the CTA's NWARP
+// warps (two per SM sub-partition: each warp issues FP64 at a third of the
+// SM's rate, so the chain of dependent elimination steps shortens with fewer
+// columns per warp) and hand the step's pivot row or column between warps
+// through shared memory.
 constexpr int NWARP = MF_FACTOR_THREADS / 32;
 constexpr int QPW = FRONT_TILE / NWARP;  // columns (or rows) per warp
 static_assert((NWARP & (NWARP - 1)) == 0 && FRONT_TILE % NWARP == 0, "warps per tile: a power of two dividing 32");
