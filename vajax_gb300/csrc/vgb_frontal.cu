@@ -516,13 +516,23 @@ __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch, int* flag, int* err
 
 // c -= l u over the first nk columns of l / rows of u (all tiles zero-padded):
 // lane = row, warp w takes columns w, w + NWARP, ...
+// busy (may be null): the SM's count of chain tasks computing.  A GEMM reads it
+// at step 8 (the load overlaps the FMAs) and, when a chain task was computing,
+// pauses at step 16 (bounded, ~8 us) so that the chain task does not share the
+// SM's FP64 issue with it.
 template <typename T>
-__device__ void gemm_tile(T* c, const T* l, const T* u, int nk, int nj) {
+__device__ void gemm_tile(T* c, const T* l, const T* u, int nk, int nj, const int* busy = nullptr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T acc[QPW];
 #pragma unroll
     for (int q = 0; q < QPW; ++q) acc[q] = (T)0;
+    int chain_seen = 0;
     for (int k = 0; k < nk; ++k) {
+        if (busy) {
+            if (k == 8) chain_seen = *(volatile const int*)busy;
+            if (k == 16 && chain_seen > 0)
+                for (int it = 0; it < 80 && *(volatile const int*)busy > 0; ++it) __nanosleep(100);
+        }
         const T lv = l[lane + k * LD];
 #pragma unroll
         for (int q = 0; q < QPW; ++q)
@@ -677,7 +687,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             if (k == 0) assemble_tile<T>(a, tb + (long long)i * nb + j, T2, r0, c0, pool);
             else put_tile(T2, ct);
             __syncthreads();
-            gemm_tile<T>(T2, T0, T1, nk, nc);
+            gemm_tile<T>(T2, T0, T1, nk, nc, busy);
             store_tile<T>(FS, T2, m, r0, nr, c0, nc);
             publish(own, k + 1);
             if (k == kb - 1 && i >= kb && j >= kb && threadIdx.x == 0) {
