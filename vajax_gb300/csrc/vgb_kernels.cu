@@ -15,6 +15,20 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, doub
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// The same maximum, one atomic per group of lanes that reach the call together:
+// the non-negative doubles compare as their bit patterns, whose maximum is
+// taken exactly as the maximum of the high words and then of the low words
+// among the lanes that hold it.  Tens of thousands of same-address atomics per
+// Newton iteration (one per row) serialised at L2.
+__device__ __forceinline__ void warp_max_nonneg(unsigned long long* addr, double v) {
+    const unsigned mask = __activemask();
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32);
+    const unsigned mh = __reduce_max_sync(mask, hi);
+    const unsigned ml = __reduce_max_sync(mask, hi == mh ? (unsigned)b : 0u);
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicMax(addr, ((unsigned long long)mh << 32) | ml);
+}
+
 __device__ __forceinline__ int ld_acquire(const int* p) {
     return cuda::atomic_ref<const int, cuda::thread_scope_device>(*p).load(cuda::memory_order_acquire);
 }
@@ -74,13 +88,18 @@ __device__ __forceinline__ void finish_row(const AssembleArgs& a, int r, double 
     }
     a.f[r] = fn;
     // NOI rows (mask 2) are replaced by an identity row before the solve, so their
-    // residual (a 1e40 conductance in PSP103) neither stops nor enters the test
-    if (a.conv_mask[r] != 2 && !isfinite(fn)) atomicOr(&a.st->nonfinite, 1);
-    if (a.conv_mask[r] == 1) {
-        double af = fabs(fn);
-        if (!(af < tol)) atomicAnd(&a.st->res_ok, 0);
-        atomic_max_nonneg(&a.st->max_f, af != af ? INFINITY : af);
-    }
+    // residual (a 1e40 conductance in PSP103) neither stops nor enters the test.
+    // The flags and the maximum go out once per group of lanes here together.
+    const int cm = a.conv_mask[r];
+    const double af = fabs(fn);
+    const bool nonfin = cm != 2 && !isfinite(fn);
+    const bool bad = cm == 1 && !(af < tol);
+    const unsigned mask = __activemask();
+    const bool lead = (int)(threadIdx.x & 31) == __ffs(mask) - 1;
+    const bool any_nonfin = __any_sync(mask, nonfin), any_bad = __any_sync(mask, bad);
+    if (lead && any_nonfin) atomicOr(&a.st->nonfinite, 1);
+    if (lead && any_bad) atomicAnd(&a.st->res_ok, 0);
+    warp_max_nonneg(&a.st->max_f, cm == 1 ? (af != af ? INFINITY : af) : 0.0);
 }
 
 // One thread per CSR entry / row with a short gather list.  Entries whose
@@ -201,15 +220,22 @@ void launch_status_reset(NRStatus* st, cudaStream_t s) { status_reset_kernel<<<1
 
 __global__ void nr_reduce_kernel(NRUpdateArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_aug) return;
-    const double d = a.delta[i];
-    const bool is_v = i < a.n_unk;
-    const double conv = is_v ? d * a.damping : d;
-    const double tol = fmax(fabs(a.X[i + 1]) * a.reltol, is_v ? a.vntol : a.abstol);
-    if (!(fabs(conv) < tol)) atomicAnd(&a.st->delta_ok, 0);
-    const double ad = fabs(d);
-    atomic_max_nonneg(&a.st->max_delta, ad != ad ? INFINITY : ad);
-    if (is_v) atomic_max_nonneg(&a.st->max_dv, ad != ad ? INFINITY : ad);
+    bool bad = false;
+    double md = 0.0, mv = 0.0;
+    if (i < a.n_aug) {
+        const double d = a.delta[i];
+        const bool is_v = i < a.n_unk;
+        const double conv = is_v ? d * a.damping : d;
+        const double tol = fmax(fabs(a.X[i + 1]) * a.reltol, is_v ? a.vntol : a.abstol);
+        bad = !(fabs(conv) < tol);
+        const double ad = fabs(d);
+        md = ad != ad ? INFINITY : ad;
+        if (is_v) mv = md;
+    }
+    // one atomic per warp (the maxima are exact, so the grouping changes nothing)
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicAnd(&a.st->delta_ok, 0);
+    warp_max_nonneg(&a.st->max_delta, md);
+    warp_max_nonneg(&a.st->max_dv, mv);
 }
 
 __global__ void nr_apply_kernel(NRUpdateArgs a) {
@@ -272,7 +298,9 @@ __global__ void lu_pre_kernel(int nM, int nF, const int* brow, const int* pre_pt
 // Singletons solved last: x_c = (b_c - sum_j B(c, j) x_j) / B(c, c), one block
 // per row (the supply-rail rows hold one entry per connected device) with a
 // fixed-order tree reduction.
-constexpr int POST_THREADS = 256;
+// The supply-rail row holds one entry per connected device (tens of thousands):
+// 1024 threads, each with four entries' loads in flight per step.
+constexpr int POST_THREADS = 1024;
 __global__ void __launch_bounds__(POST_THREADS) lu_post_kernel(int nL, const int* l_col, const int* l_arow,
                                                               const int* l_diag_e, const int* l_ptr, const int* l_e,
                                                               const int* l_x, const double* A, const double* b,
@@ -281,6 +309,7 @@ __global__ void __launch_bounds__(POST_THREADS) lu_post_kernel(int nL, const int
     const int row = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double acc = 0.0;
+#pragma unroll 4
     for (int e = l_ptr[row] + threadIdx.x; e < l_ptr[row + 1]; e += POST_THREADS) acc += A[l_e[e]] * xout[l_x[e]];
     for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) part[warp] = acc;
