@@ -771,6 +771,7 @@ __device__ void fwd_small_warp(const MFSolveArgs& a, int S, const T* __restrict_
     T u = (T)0;
     if (lane < m) {
         u = lane < w ? rhs[idx[lane]] : (T)0;
+#pragma unroll 4
         for (long long e = gp[lane]; e < gp[lane + 1]; ++e) u += __ldcg(cv + a.fg_src[e]);
     }
     for (int p = 0; p < w; ++p) {
@@ -870,6 +871,8 @@ __global__ void __launch_bounds__(MF_THREADS) mf_fwd_kernel(MFSolveArgs a, const
             const long long* gp = a.fg_ptr + a.fr_ptr[S];
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 T v = i < w ? rhs[idx[i]] : (T)0;
+                // several entries' index and value loads in flight; the sum keeps child order
+#pragma unroll 4
                 for (long long e = gp[i]; e < gp[i + 1]; ++e) v += __ldcg(cv + a.fg_src[e]);
                 u[i] = v;
             }

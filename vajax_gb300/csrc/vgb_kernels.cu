@@ -112,6 +112,8 @@ __global__ void assemble_kernel(AssembleArgs a) {
         const int e0 = a.csr_src_ptr[t], e1 = a.csr_src_ptr[t + 1];
         if (e1 - e0 > HEAVY_LIST) return;
         double s = 0.0;
+        // several entries' index and value loads in flight; the sum keeps list order
+#pragma unroll 4
         for (int e = e0; e < e1; ++e) s += a.contrib[a.csr_src[e]];
         if (a.csr_diag[t]) s += a.gmin + a.k[4];
         s += a.csr_const[t];
@@ -124,6 +126,7 @@ __global__ void assemble_kernel(AssembleArgs a) {
     if (r < a.n_unk) {
         const int e0 = a.res_src_ptr[r], e1 = a.res_src_ptr[r + 1];
         if (e1 - e0 > HEAVY_LIST) return;
+#pragma unroll 4
         for (int e = e0; e < e1; ++e) {
             double v = nan0(a.contrib[a.res_src[e]]);
             fr += v;
@@ -144,6 +147,7 @@ __global__ void __launch_bounds__(HEAVY_THREADS) assemble_heavy_kernel(AssembleA
     const int it = a.hchunk_item[ch];
     const bool is_csr = it < a.n_heavy_csr;
     double s = 0.0, q = 0.0, m = 0.0;
+#pragma unroll 4
     for (int e = a.hchunk_lo[ch] + threadIdx.x; e < a.hchunk_hi[ch]; e += HEAVY_THREADS) {
         if (is_csr) {
             s += a.contrib[a.csr_src[e]];
