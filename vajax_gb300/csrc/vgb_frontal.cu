@@ -120,6 +120,7 @@ constexpr int LD = FRONT_TILE_LD;
 constexpr int TILE_ELEMS = FRONT_TILE * FRONT_TILE_LD;
 // shared memory of a factorisation CTA: one small front, or three tiles
 constexpr int MF_SMEM_ELEMS = SMALL_FRONT * SMALL_FRONT;
+static_assert(SMALL_FRONT <= MF_FACTOR_THREADS, "one thread per row of a small front's column");
 static_assert(3 * TILE_ELEMS <= MF_SMEM_ELEMS, "three tiles must fit in the small-front buffer");
 static_assert(FRONT_TILE * FRONT_TILE + FRONT_TILE <= TILE_ELEMS, "a tile area holds 32 exchanged columns and 32 reciprocals");
 
@@ -196,8 +197,8 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
             F[p + p * m] = piv;
             atomicOr(err, DEV_ERR_PIVOT);
         }
-        const T rinv = vgb_rcp(piv);
-        for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) F[i + p * m] *= rinv;
+        // only the threads that scale the column form the reciprocal (m <= SMALL_FRONT < blockDim)
+        if (p + 1 + (int)threadIdx.x < m) F[p + 1 + threadIdx.x + p * m] *= vgb_rcp(piv);
         __syncthreads();
         for (int j = p + 1 + warp; j < m; j += nw) {
             const T u = F[p + j * m];
