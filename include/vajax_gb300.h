@@ -361,8 +361,8 @@ int vgb_batch_destroy(void* b);
  * convention); it is written on the stream, so read it after the stream
  * synchronises.  The call itself is asynchronous.
  * The first call on each device (with that device current) looks up the
- * array's address and loads the module; make that first call before any
- * stream capture.  The cached address does not survive cudaDeviceReset.
+ * array's address and loads the module.  The cached address does not
+ * survive cudaDeviceReset.
  * Nothing in the array must start at zero.  Calls that overlap in time on one
  * device (other streams or threads) share the array and race: serialise them.
  * No counterpart in the reference (its dense path solves in JAX,
