@@ -192,14 +192,15 @@ __device__ void partial_lu_small(T* F, int m, int w, int* err) {
     for (int p = 0; p < w; ++p) {
         T piv = F[p + p * m];
         if (piv == (T)0 || !isfinite((double)piv)) piv = (T)1e-30;
+        // only the threads that scale the column form the reciprocal (m <= SMALL_FRONT < blockDim)
+        if (p + 1 + (int)threadIdx.x < m) F[p + 1 + threadIdx.x + p * m] *= vgb_rcp(piv);
         __syncthreads();
+        // a replaced pivot goes back once every thread has read it; the update below
+        // does not read the diagonal element
         if (threadIdx.x == 0 && piv != F[p + p * m]) {
             F[p + p * m] = piv;
             atomicOr(err, DEV_ERR_PIVOT);
         }
-        // only the threads that scale the column form the reciprocal (m <= SMALL_FRONT < blockDim)
-        if (p + 1 + (int)threadIdx.x < m) F[p + 1 + threadIdx.x + p * m] *= vgb_rcp(piv);
-        __syncthreads();
         for (int j = p + 1 + warp; j < m; j += nw) {
             const T u = F[p + j * m];
             for (int i = p + 1 + lane; i < m; i += 32) F[i + j * m] -= F[i + p * m] * u;
