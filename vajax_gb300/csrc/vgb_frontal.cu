@@ -438,9 +438,12 @@ __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch, int* flag, int* err
     T* dinv = xch + FRONT_TILE * FRONT_TILE;  // reciprocals of the diagonal, formed once in parallel
     if (threadIdx.x < n) dinv[threadIdx.x] = vgb_rcp(d[threadIdx.x + threadIdx.x * LD]);
     if (threadIdx.x < FRONT_TILE) flag[threadIdx.x] = 0;
-    T a[QPW];
+    T a[QPW], u[QPW];
 #pragma unroll
-    for (int q = 0; q < QPW; ++q) a[q] = x[lane + (g + NWARP * q) * LD];
+    for (int q = 0; q < QPW; ++q) {
+        a[q] = x[lane + (g + NWARP * q) * LD];
+        u[q] = d[lane + (g + NWARP * q) * LD];  // U(lane, c2) of this warp's columns c2, shuffled at step lane
+    }
     __syncthreads();
     if (n > 0 && g == 0) {
         a[0] *= dinv[0];
@@ -467,7 +470,7 @@ __device__ void trsm_l_tile(T* x, const T* d, int n, T* xch, int* flag, int* err
 #pragma unroll
         for (int q = 0; q < QPW; ++q) {
             const int c2 = g + NWARP * q;
-            if (c2 > c1 && c2 < n) a[q] -= xc * d[c + c2 * LD];
+            if (c2 > c1 && c2 < n) a[q] -= xc * __shfl_sync(0xffffffffu, u[q], c);
         }
     }
 #pragma unroll
@@ -481,9 +484,12 @@ template <typename T>
 __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch, int* flag, int* err) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     if (threadIdx.x < FRONT_TILE) flag[threadIdx.x] = 0;
-    T a[QPW];
+    T a[QPW], l[QPW];
 #pragma unroll
-    for (int q = 0; q < QPW; ++q) a[q] = x[(g + NWARP * q) + lane * LD];
+    for (int q = 0; q < QPW; ++q) {
+        a[q] = x[(g + NWARP * q) + lane * LD];
+        l[q] = d[(g + NWARP * q) + lane * LD];  // L(r2, lane) of this warp's rows r2, shuffled at step lane
+    }
     __syncthreads();
     if (n > 0 && g == 0) {
         xch[lane] = a[0];  // row 0 is final (unit diagonal)
@@ -508,7 +514,7 @@ __device__ void trsm_u_tile(T* x, const T* d, int n, T* xch, int* flag, int* err
 #pragma unroll
         for (int q = 0; q < QPW; ++q) {
             const int r2 = g + NWARP * q;
-            if (r2 > r1 && r2 < n) a[q] -= d[r2 + r * LD] * yr;
+            if (r2 > r1 && r2 < n) a[q] -= __shfl_sync(0xffffffffu, l[q], r) * yr;
         }
     }
 #pragma unroll
