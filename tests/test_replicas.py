@@ -119,3 +119,54 @@ def test_independent_units_dispatched_to_two_ranks():
     assert all(p.exitcode == 0 for p in procs)
     out = dict(q.get(timeout=5) for _ in range(2))
     assert out[0] == serial and out[1] == serial
+
+
+class _StandInEngine:
+    """run_corners with a result that depends only on the corner (its name and
+    temperature), as a real sweep's would."""
+
+    def run_corners(self, corners, **kwargs):
+        from vajax_gb300.corners import CornerResult, CornerSweepResult
+        res = [CornerResult(corner=c, result={"v": c.temperature * 2.0, "name": c.name}, converged=True)
+               for c in corners]
+        return CornerSweepResult(corners=list(corners), results=res)
+
+
+def _corners_worker(rank, world, port, q):
+    import torch.distributed as dist
+    from vajax_gb300.corners import create_monte_carlo_corners
+    from vajax_gb300.replicas import run_corners_sharded
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sweep = run_corners_sharded(_StandInEngine(), create_monte_carlo_corners(9, seed=3), rank, world)
+        q.put((rank, [(r.corner.name, r.result["name"], r.result["v"], r.converged) for r in sweep.results]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_corner_sweep_sharded_over_two_ranks():
+    """Nine corners over two gloo ranks: each rank's sweep holds all nine
+    results in corner order, each result belonging to its own corner, equal
+    to one process running the sweep."""
+    import socket
+    import torch.multiprocessing as mp
+    from vajax_gb300.corners import create_monte_carlo_corners
+    from vajax_gb300.replicas import run_corners_sharded
+    corners = create_monte_carlo_corners(9, seed=3)
+    one = run_corners_sharded(_StandInEngine(), corners)
+    expect = [(r.corner.name, r.result["name"], r.result["v"], r.converged) for r in one.results]
+    assert [e[0] for e in expect] == [c.name for c in corners] and all(e[0] == e[1] for e in expect)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_corners_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    assert all(p.exitcode == 0 for p in procs)
+    out = dict(q.get(timeout=5) for _ in range(2))
+    assert out[0] == expect and out[1] == expect
