@@ -104,7 +104,7 @@ enum TaskType : int { TASK_SMALL = 0, TASK_GETRF = 1, TASK_TRSM_L = 2, TASK_TRSM
 // on the chain of dependent pivot tiles), runs as DUPD_SLICES tasks of
 // DUPD_W columns each, on as many CTAs: task type TASK_DUPD + slice, with
 // (i, j, k) = (d, d, d - 1).  GETRF(d) waits for all slices.
-constexpr int DUPD_SLICES = 4;
+constexpr int DUPD_SLICES = 8;
 constexpr int DUPD_W = FRONT_TILE / DUPD_SLICES;
 
 // Static-pivot sparse LU structures (host symbolic + device numeric).

@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             // it itself (after the first touch of tile (1, 1)), and for k >= 2 it runs
             // as DUPD_SLICES column slices on as many CTAs, whose count GETRF(k) waits
             // for.  A 32 x 32 x 32 update takes ~9 us of one SM's FP64 issue; a slice
-            // takes a quarter of that.
+            // takes 1 / DUPD_SLICES of that.
             const long long dk = (long long)k * nb + k;
             bool ok;
             if (k == 0) ok = wait_children(a, S);
@@ -640,14 +640,14 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             // columns [cs, cs + DUPD_W) of A(i,i) -= L(i,k) U(k,i); lane = row, warp =
             // column of the slice.  The sum runs in the order of gemm_tile's, so the
             // tile is bit for bit what the fused update gives.
-            static_assert(DUPD_W == NWARP, "one slice column per warp");
+            static_assert(DUPD_W <= NWARP, "at most one slice column per warp");
             const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
             const long long di = (long long)i * nb + i;
             if (!wait3(a, tv + (long long)i * nb + k, TILE_FINAL, tv + (long long)k * nb + i, TILE_FINAL, tv + di, k))
                 continue;
             if (threadIdx.x == 0 && busy) atomicAdd(busy, 1);
             const int cs = (type - TASK_DUPD) * DUPD_W;
-            const int col = cs + wp;  // column of the diagonal tile, < nr while in the tile
+            const int col = wp < DUPD_W ? cs + wp : FRONT_TILE;  // column of the diagonal tile (warps past the slice: none)
             TileRegs<T> lt;
             fetch_tile(lt, FS, m, r0, nr, k0, nk);
             const T uv = (lane < nk && col < nr) ? __ldcg(FS + (k0 + lane) + (long long)(r0 + col) * m) : (T)0;
@@ -655,9 +655,11 @@ __global__ void __launch_bounds__(MF_FACTOR_THREADS, MF_FACTOR_CTAS_MAX) mf_fact
             put_tile(T0, lt);
             T1[lane + wp * LD] = uv;
             __syncthreads();
-            T acc = (T)0;
-            for (int q = 0; q < nk; ++q) acc += T0[lane + q * LD] * T1[q + wp * LD];
-            if (lane < nr && col < nr) __stcg(FS + (r0 + lane) + (long long)(r0 + col) * m, cv - acc);
+            if (col < nr) {  // warp-uniform
+                T acc = (T)0;
+                for (int q = 0; q < nk; ++q) acc += T0[lane + q * LD] * T1[q + wp * LD];
+                if (lane < nr) __stcg(FS + (r0 + lane) + (long long)(r0 + col) * m, cv - acc);
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
                 __threadfence();
